@@ -1,0 +1,161 @@
+/*
+ *  mars_gpu.h -- C ABI of the GB300 MARS forward pass.
+ *
+ *  Plain C types only (pointers, sizes, status codes): no CUDA or torch types
+ *  cross this boundary, and no C++ exception escapes it. Every entry point
+ *  returns MARS_GPU_OK (0) or a nonzero status; mars_gpu_last_error() then
+ *  holds a message (per calling thread). Host pointers in, host pointers out:
+ *  the library owns all device memory.
+ *
+ *  A handle is the device-resident state of one fit (the reference's
+ *  MarsAlgo plus its mars::cuda::Context). Calls on one handle must not
+ *  overlap; different handles may be driven from different threads.
+ *
+ *  Reference interfaces replaced (file:line in aleon1138/mars):
+ *    mars_gpu_create     MarsAlgo::MarsAlgo            marsalgo.cc:266-370
+ *                        mars::cuda::context_create    cuda/mars_cuda.h:43
+ *                        (+ set_target/sync_xcols      cuda/mars_cuda.h:80,95)
+ *    mars_gpu_destroy    MarsAlgo::~MarsAlgo           marsalgo.cc:372-380
+ *                        mars::cuda::context_destroy   cuda/mars_cuda.h:48
+ *    mars_gpu_nbasis     MarsAlgo::nbasis              marsalgo.h:37
+ *    mars_gpu_yvar       MarsAlgo::yvar                marsalgo.h:40
+ *    mars_gpu_dsse       MarsAlgo::dsse                marsalgo.h:39
+ *    mars_gpu_eval       marslib eval (all X columns)  marslib.cc:41-148
+ *                        -> MarsAlgo::eval per column  marsalgo.cc:402-662
+ *                        -> MarsAlgo::eval_batch       marsalgo.cc:664-758
+ *    mars_gpu_append     MarsAlgo::append              marsalgo.cc:760-875
+ *    mars_gpu_orthonormalize   mars::orthonormalize    kernels.h:52-62
+ *                              mars::cuda::orthonormalize  cuda/mars_cuda.h:127-131
+ *    mars_gpu_orthonormalize_col  mars::orthonormalize_col  kernels.h:91-96
+ */
+#ifndef MARS_GPU_H
+#define MARS_GPU_H
+
+#include <stdbool.h>
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define MARS_GPU_API __attribute__((visibility("default")))
+#else
+#define MARS_GPU_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MARS_GPU_OK 0
+#define MARS_GPU_EINVAL 1   /* invalid argument (same messages as the reference) */
+#define MARS_GPU_ECUDA 2    /* CUDA runtime / launch failure */
+#define MARS_GPU_ENOMEM 3   /* device allocation failed */
+#define MARS_GPU_EFULL 4    /* basis matrix is full */
+#define MARS_GPU_ETIMEOUT 5 /* a bounded device-side wait ran out */
+
+/* Arithmetic used for candidate evaluation. */
+#define MARS_GPU_PREC_FP64 0  /* plain FP64 forward pass */
+#define MARS_GPU_PREC_MIXED 1 /* FP32/tensor-core fast path, near-ties re-decided in FP64 */
+
+typedef struct mars_gpu_algo mars_gpu_algo;
+
+typedef struct {
+    long long evals;            /* mars_gpu_eval calls */
+    long long candidates;       /* (input, parent) pairs evaluated */
+    long long knot_evals;       /* grid cuts scored by the hinge sweep */
+    long long dgks_fired;       /* candidate columns re-orthogonalised */
+    long long redecided;        /* candidates re-evaluated in FP64 (mixed mode) */
+    long long kernel_launches;  /* kernels launched by this handle */
+    double ms_project;          /* device time per phase, summed (CUDA events) */
+    double ms_dgks;
+    double ms_normalize;
+    double ms_sweep;
+    double ms_sort;
+    double ms_append;
+    double ms_redecide;
+} mars_gpu_stats;
+
+/* Message of the last failing call on this thread ("" if none). */
+MARS_GPU_API const char *mars_gpu_last_error(void);
+
+/* Number of CUDA devices visible (0 when none); never fails. */
+MARS_GPU_API int mars_gpu_device_count(void);
+
+/*
+ *  Build the fit state. X: (n, p) column-major f32, column stride ldx (>= n);
+ *  y, w: (n) f32 (w are inverse-variance weights; non-finite y rows get
+ *  weight 0). max_terms: basis capacity including the intercept.
+ *  Errors: "target Y is all zero or NANs", "not all columns in X are finite".
+ *  X is copied to the device; the caller may free it afterwards.
+ */
+MARS_GPU_API int mars_gpu_create(const float *X, const float *y, const float *w, size_t n, size_t p,
+                    size_t ldx, size_t max_terms, mars_gpu_algo **out);
+MARS_GPU_API int mars_gpu_destroy(mars_gpu_algo *algo);
+
+MARS_GPU_API int mars_gpu_nbasis(const mars_gpu_algo *algo, int *out);
+MARS_GPU_API int mars_gpu_yvar(const mars_gpu_algo *algo, double *out);
+MARS_GPU_API int mars_gpu_dsse(const mars_gpu_algo *algo, double *out);
+
+/* Select MARS_GPU_PREC_FP64 or MARS_GPU_PREC_MIXED (the default). */
+MARS_GPU_API int mars_gpu_set_precision(mars_gpu_algo *algo, int mode);
+
+/*
+ *  Evaluate every (input, parent) pair selected by `mask` in one call.
+ *  mask: (rows, nbasis) row-major bool, row stride mask_stride (elements);
+ *  rows <= p; row i is input column i. min_span >= 1; end_span rows are
+ *  skipped at both ends of the sorted column; linear_only skips the sweep.
+ *  Outputs (rows, nbasis) row-major f64, contiguous:
+ *    linear[i,j] = delta SSE of adding x_i * B_j
+ *    hinge[i,j]  = delta SSE of the best mirror-hinge pair (0 if none)
+ *    cut[i,j]    = its knot X[k, i] (NaN if none or linear_only)
+ *  sse0 (optional) receives mars_gpu_dsse().
+ */
+MARS_GPU_API int mars_gpu_eval(mars_gpu_algo *algo, const bool *mask, int rows, int mask_stride,
+                  int min_span, int end_span, int linear_only, double *sse0, double *linear,
+                  double *hinge, double *cut);
+
+/*
+ *  Append basis type 'l' (x * B_bcol), '+' (B_bcol * max(x - h, 0)) or
+ *  '-' (B_bcol * max(h - x, 0)) on input xcol. *mse receives the new MSE, or
+ *  -1 when the column is numerically degenerate (the basis is unchanged).
+ *  Errors: "basis matrix is full", "invalid basis column number: N",
+ *  "invalid X column index", "invalid basis type".
+ */
+MARS_GPU_API int mars_gpu_append(mars_gpu_algo *algo, char type, int xcol, int bcol, float h, double *mse);
+
+/* Counters and per-phase device times of this handle. */
+MARS_GPU_API int mars_gpu_get_stats(const mars_gpu_algo *algo, mars_gpu_stats *out);
+
+/*
+ *  max |Q^T Q - I| over the live orthonormal basis Q (f32 storage, FP64
+ *  arithmetic), and the RSS of the current fit, 1 - sum(ybo^2), recomputed
+ *  in FP64 from Q and y.
+ */
+MARS_GPU_API int mars_gpu_orth_error(mars_gpu_algo *algo, double *max_abs, double *rss);
+
+/*
+ *  Kernel-level entry points (host arrays in and out), for tests and
+ *  micro-benchmarks.
+ *
+ *  mars_gpu_orthonormalize: for j < p, Bx[:,j] = B[:,mask[j]] * x, project out
+ *  the m columns of Bo, DGKS retry when 9 s < ||Bo^T Bx||^2, normalise by
+ *  1/sqrt(s+tol) (zero when s <= tol). B: (n, *) column-major, column stride
+ *  ldB; Bo: (n, >= m) row-major, row stride ldBo; Bx: (n, p) column-major,
+ *  column stride ldBx [out]; s: (p) squared norms before scaling [out,
+ *  optional]; dgks: number of columns retried [out, optional].
+ */
+MARS_GPU_API int mars_gpu_orthonormalize(size_t n, size_t m, size_t p, const float *B, size_t ldB,
+                            const float *x, const int *mask, const float *Bo, size_t ldBo,
+                            float *Bx, size_t ldBx, double *s, double tol, long *dgks);
+
+/*
+ *  mars_gpu_orthonormalize_col: modified Gram-Schmidt of v (n, f64, in/out)
+ *  against the m columns of Bo (row-major, stride ldBo) with one DGKS retry;
+ *  v is normalised when ||v||^2 > tol. *w receives the pre-normalisation norm.
+ */
+MARS_GPU_API int mars_gpu_orthonormalize_col(size_t n, size_t m, double *v, const float *Bo, size_t ldBo,
+                                double tol, double *w, long *dgks);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MARS_GPU_H */

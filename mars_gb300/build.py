@@ -1,0 +1,81 @@
+"""Build recipe for the GB300 forward-pass library.
+
+Compiles every ``csrc/*.cu`` for sm_103a with nvcc (one translation unit per
+process, in parallel) and links ``mars_gb300/lib/libmars_gpu.so``, a plain
+C-ABI shared library (include/mars_gpu.h) with the CUDA runtime linked
+statically. Objects go to ``mars_gb300/_build/``.
+
+Floating-point contraction is off in both device (``--fmad=false``) and host
+(``-ffp-contract=off``) code: the kernels spell out every fused multiply-add
+they want, so their rounding follows the arithmetic written in the source.
+"""
+import concurrent.futures
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB_DIR = os.path.join(HERE, "lib")
+LIB = os.path.join(LIB_DIR, "libmars_gpu.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.isfile(cand):
+            return cand
+    raise RuntimeError("nvcc not found (set NVCC or add CUDA to PATH)")
+
+
+def flags():
+    return ARCH + [
+        "-O3", "-lineinfo", "-std=c++17", "--fmad=false",
+        "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden,-O3",
+        "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
+    ]
+
+
+def sources():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
+def _compile(src, extra):
+    obj = os.path.join(OBJ, os.path.basename(src)[:-3] + ".o")
+    deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".cuh")]
+    deps.append(os.path.join(ROOT, "include", "mars_gpu.h"))
+    if os.path.isfile(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
+        return obj, ""
+    cmd = [nvcc()] + flags() + extra + ["-c", src, "-o", obj]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), out.stderr))
+    return obj, out.stderr
+
+
+def build(verbose=False, extra=()):
+    """Compile and link; returns the path of libmars_gpu.so."""
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(LIB_DIR, exist_ok=True)
+    srcs = sources()
+    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, len(srcs))) as ex:
+        results = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
+    objs = [r[0] for r in results]
+    if verbose:
+        for _, log in results:
+            if log:
+                sys.stderr.write(log)
+    newest = max(os.path.getmtime(o) for o in objs)
+    if not (os.path.isfile(LIB) and os.path.getmtime(LIB) >= newest):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+        out = subprocess.run(cmd, capture_output=True, text=True)
+        if out.returncode != 0:
+            raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), out.stderr))
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

@@ -1,0 +1,838 @@
+// Host side of the GB300 MARS forward pass: the fit state behind the C ABI
+// (include/mars_gpu.h). One handle = the reference's MarsAlgo
+// (marsalgo.cc:266-875) plus its device context (cuda/orthonormalize.cu),
+// re-designed so that every candidate of an epoch is evaluated on the device
+// in one call and the basis lives only in device memory.
+#include "../../include/mars_gpu.h"
+#include "common.cuh"
+#include "fp64.cuh"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace mgpu;
+
+namespace {
+thread_local std::string g_last_error;
+
+template <class F>
+int guarded(F &&f)
+{
+    try {
+        f();
+        return MARS_GPU_OK;
+    } catch (const Error &e) {
+        g_last_error = e.what();
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        g_last_error = "host allocation failed";
+        return MARS_GPU_ENOMEM;
+    } catch (const std::exception &e) {
+        g_last_error = e.what();
+        return MARS_GPU_ECUDA;
+    }
+}
+
+double env_double(const char *name, double dflt)
+{
+    const char *v = std::getenv(name);
+    return (v && *v) ? std::atof(v) : dflt;
+}
+
+enum Phase { PH_PROJECT, PH_DGKS, PH_NORMALIZE, PH_SWEEP, PH_SORT, PH_APPEND, PH_REDECIDE, PH_N };
+
+// Device time per phase, resolved after the stream is synchronised.
+struct PhaseTimer {
+    cudaStream_t st = nullptr;
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> open;
+    size_t used = 0;
+    cudaEvent_t get()
+    {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            CUDA_CHECK(cudaEventCreate(&e));
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    cudaEvent_t begin()
+    {
+        cudaEvent_t e = get();
+        CUDA_CHECK(cudaEventRecord(e, st));
+        return e;
+    }
+    void end(int phase, cudaEvent_t b)
+    {
+        cudaEvent_t e = get();
+        CUDA_CHECK(cudaEventRecord(e, st));
+        open.push_back({phase, {b, e}});
+    }
+    void resolve(double *ms)
+    {
+        for (auto &o : open) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, o.second.first, o.second.second) == cudaSuccess) {
+                ms[o.first] += t;
+            }
+        }
+        open.clear();
+        used = 0;
+    }
+    ~PhaseTimer()
+    {
+        for (auto e : pool) {
+            cudaEventDestroy(e);
+        }
+    }
+};
+
+}  // namespace
+
+struct mars_gpu_algo {
+    size_t n = 0, p = 0, max_terms = 0, ldbo = 0, m = 1;
+    double tol = 0, yvar = 0;
+    int precision = MARS_GPU_PREC_FP64;
+    std::vector<double> ybo;
+    cudaStream_t st = nullptr;
+    PhaseTimer timer;
+    double phase_ms[PH_N] = {0};
+    mars_gpu_stats stats;
+
+    // Resident state.
+    DevBuf X, s, y, B, Bo, BoC, ybo_d, perm, xsort;
+    std::vector<char> sorted;
+    // Per-eval scratch (grow-only).
+    DevBuf Bx, T, Tpart, part, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks;
+    DevBuf sort_keys, sort_vals, sort_tmp;
+    DevBuf ap_v, ap_part, ap_coef, ap_scal;
+
+    ~mars_gpu_algo()
+    {
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+    }
+};
+
+namespace {
+
+void sync(mars_gpu_algo *a) { CUDA_CHECK(cudaStreamSynchronize(a->st)); }
+
+AppendScratch append_scratch(mars_gpu_algo *a)
+{
+    const int nb = append_blocks((int)a->n);
+    a->ap_v.ensure(sizeof(double) * a->n);
+    a->ap_part.ensure(sizeof(double) * 2 * nb);
+    a->ap_coef.ensure(sizeof(double) * (a->max_terms + 1));
+    a->ap_scal.ensure(sizeof(double) * 8);
+    AppendScratch ws;
+    ws.v = a->ap_v.as<double>();
+    ws.part = a->ap_part.as<double>();
+    ws.coef = a->ap_coef.as<double>();
+    ws.scal = a->ap_scal.as<double>();
+    ws.nblocks = nb;
+    return ws;
+}
+
+__global__ void k_col_to_rows(const float *__restrict__ col, int n, float *__restrict__ Bo,
+                              size_t ldbo, int c)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        Bo[(size_t)i * ldbo + c] = col[i];
+    }
+}
+
+void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *w, size_t n,
+                 size_t p, size_t ldx, size_t max_terms)
+{
+    verify(!std::isfinite(NAN), "NAN check is disabled, recompile without --fast-math");
+    verify(max_terms >= 1, "max_terms must be >= 1");
+    verify(ldx >= n || p <= 1, "X column stride smaller than the row count");
+    verify(p <= 65535, "more than 65535 X columns");
+    verify(n < (size_t)INT32_MAX, "more rows than the GPU path supports (2^31 - 1)");
+    a->n = n;
+    a->p = p;
+    a->max_terms = max_terms;
+    a->ldbo = round_up(max_terms, 4);
+    a->m = 1;
+    a->tol = ((double)n * 0.02) * DBL_EPSILON;
+    std::memset(&a->stats, 0, sizeof(a->stats));
+    CUDA_CHECK(cudaStreamCreateWithFlags(&a->st, cudaStreamNonBlocking));
+    a->timer.st = a->st;
+
+    // Weighted, normalised target (marsalgo.cc:278-352), in the reference's
+    // order of operations; fused multiply-adds where the reference fuses.
+    std::vector<double> yd(n), sw(n);
+    for (size_t i = 0; i < n; ++i) {
+        double yi = (double)y[i];
+        double swi = std::sqrt((double)w[i]);
+        if (!std::isfinite(yi)) {
+            yi = swi = 0.0;
+        }
+        sw[i] = swi;
+        yd[i] = yi * swi;
+    }
+    double y_sq = 0.0, w_sq = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        y_sq = std::fma(yd[i], yd[i], y_sq);
+        w_sq = std::fma(sw[i], sw[i], w_sq);
+    }
+    const double y_norm = std::sqrt(y_sq), w_norm = std::sqrt(w_sq);
+    verify(y_norm > 0.0 && w_norm > 0.0, "target Y is all zero or NANs");
+    std::vector<float> yf(n), b0(n);
+    for (size_t i = 0; i < n; ++i) {
+        yd[i] /= y_norm;
+        sw[i] /= w_norm;
+        yf[i] = (float)yd[i];
+        b0[i] = (float)sw[i];
+    }
+    double ybo0 = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        ybo0 = std::fma((double)b0[i], (double)yf[i], ybo0);
+    }
+    a->ybo.assign(1, ybo0);
+    double ymean_sum = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        ymean_sum += yd[i];
+    }
+    const double ymean = ymean_sum / (double)n;
+    double vsum = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        const double dv = yd[i] - ymean;
+        vsum = std::fma(dv, dv, vsum);
+    }
+    a->yvar = vsum / (double)n;
+
+    // Device-resident state.
+    a->X.ensure(sizeof(float) * std::max<size_t>(1, n * p));
+    if (n * p) {
+        CUDA_CHECK(cudaMemcpy2DAsync(a->X.ptr, n * sizeof(float), X, ldx * sizeof(float),
+                                     n * sizeof(float), p, cudaMemcpyHostToDevice, a->st));
+    }
+    a->y.ensure(sizeof(float) * n);
+    CUDA_CHECK(cudaMemcpyAsync(a->y.ptr, yf.data(), sizeof(float) * n, cudaMemcpyHostToDevice,
+                               a->st));
+    a->B.ensure(sizeof(float) * n * max_terms);
+    a->BoC.ensure(sizeof(float) * n * max_terms);
+    a->Bo.ensure(sizeof(float) * n * a->ldbo);
+    CUDA_CHECK(cudaMemsetAsync(a->Bo.ptr, 0, sizeof(float) * n * a->ldbo, a->st));
+    CUDA_CHECK(cudaMemcpyAsync(a->B.ptr, b0.data(), sizeof(float) * n, cudaMemcpyHostToDevice,
+                               a->st));
+    CUDA_CHECK(cudaMemcpyAsync(a->BoC.ptr, b0.data(), sizeof(float) * n, cudaMemcpyHostToDevice,
+                               a->st));
+    k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(a->BoC.as<float>(), (int)n,
+                                                                a->Bo.as<float>(), a->ldbo, 0);
+    LAUNCH_CHECK();
+    a->ybo_d.ensure(sizeof(double) * max_terms);
+    CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.ptr, &a->ybo[0], sizeof(double), cudaMemcpyHostToDevice,
+                               a->st));
+
+    // Column scales s = 1/rms (marsalgo.cc:359-369).
+    a->s.ensure(sizeof(float) * std::max<size_t>(1, p));
+    if (p) {
+        const int nb = append_blocks((int)n);
+        DevBuf part, sums;
+        part.ensure(sizeof(double) * nb * p);
+        sums.ensure(sizeof(double) * p);
+        column_sumsq(a->st, a->X.as<float>(), n, (int)n, (int)p, sums.as<double>(),
+                     part.as<double>(), &a->stats.kernel_launches);
+        std::vector<double> sq(p);
+        CUDA_CHECK(cudaMemcpyAsync(sq.data(), sums.ptr, sizeof(double) * p, cudaMemcpyDeviceToHost,
+                                   a->st));
+        sync(a);
+        std::vector<float> sv(p);
+        for (size_t j = 0; j < p; ++j) {
+            const double rms = std::sqrt(sq[j] / (double)n);
+            verify(std::isfinite(rms), "not all columns in X are finite");
+            sv[j] = rms > 0.0 ? (float)(1.0 / rms) : 1.0f;
+        }
+        CUDA_CHECK(cudaMemcpyAsync(a->s.ptr, sv.data(), sizeof(float) * p, cudaMemcpyHostToDevice,
+                                   a->st));
+    }
+    a->sorted.assign(p, 0);
+    sync(a);
+}
+
+// Candidate blocks: contiguous ranges of the (xcol-major) candidate list that
+// never split an input column, each at most `cap` candidates.
+std::vector<std::pair<int, int>> block_candidates(const std::vector<int> &cx, size_t cap)
+{
+    std::vector<std::pair<int, int>> blocks;
+    const int P = (int)cx.size();
+    int b0 = 0;
+    while (b0 < P) {
+        int b1 = b0;
+        while (b1 < P) {
+            int e = b1;
+            while (e < P && cx[e] == cx[b1]) {
+                ++e;
+            }
+            if (b1 > b0 && (size_t)(e - b0) > cap) {
+                break;
+            }
+            b1 = e;
+        }
+        blocks.push_back({b0, b1});
+        b0 = b1;
+    }
+    return blocks;
+}
+
+void ensure_sorted(mars_gpu_algo *a, const std::vector<int> &cols)
+{
+    std::vector<int> todo;
+    for (int c : cols) {
+        if (!a->sorted[c]) {
+            todo.push_back(c);
+        }
+    }
+    if (todo.empty()) {
+        return;
+    }
+    const size_t np = a->n * a->p;
+    a->perm.ensure(sizeof(int) * np);
+    a->xsort.ensure(sizeof(float) * np);
+    cudaEvent_t t0 = a->timer.begin();
+    sort_columns(a->st, a->X.as<float>(), a->n, a->s.as<float>(), (int)a->n, todo.data(),
+                 (int)todo.size(), a->perm.as<int>(), a->xsort.as<float>(), a->sort_keys,
+                 a->sort_vals, a->sort_tmp, &a->stats.kernel_launches);
+    a->timer.end(PH_SORT, t0);
+    for (int c : todo) {
+        a->sorted[c] = 1;
+    }
+}
+
+// The FP64 evaluation of candidates [0, Pc) (device arrays cx/cb). Fills
+// ybx, and hsse/hrow unless linear_only.
+void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
+                     const std::vector<int> &cx_h, int c0, int min_span, int head, int tail,
+                     bool linear_only)
+{
+    const int n = (int)a->n, m = (int)a->m;
+    float *Bx = a->Bx.as<float>();
+    ProjectScratch ws;
+    ws.T = a->T.as<double>();
+    ws.Tpart = a->Tpart.as<double>();
+    ws.part = a->part.as<double>();
+    ws.part_elems = a->part.bytes / sizeof(double);
+    ws.tpart_elems = a->Tpart.bytes / sizeof(double);
+    double *s = a->svec.as<double>();
+
+    cudaEvent_t t0 = a->timer.begin();
+    FillSrc src{a->B.as<float>(), a->n, a->X.as<float>(), a->n, a->s.as<float>(), cx_d, cb_d};
+    project_fp64(a->st, src, a->Bo.as<float>(), a->ldbo, n, m, Pc, nullptr, Bx, a->n, s, ws,
+                 &a->stats.kernel_launches);
+    a->timer.end(PH_PROJECT, t0);
+
+    t0 = a->timer.begin();
+    dgks_gate(a->st, ws.T, m, Pc, s, a->tol, a->fired.as<int>(), a->nfired.as<int>(),
+              &a->stats.kernel_launches);
+    int nf = 0;
+    CUDA_CHECK(cudaMemcpyAsync(&nf, a->nfired.ptr, sizeof(int), cudaMemcpyDeviceToHost, a->st));
+    sync(a);
+    if (nf > 0) {
+        StoredSrc src2{Bx, a->n, a->fired.as<int>()};
+        project_fp64(a->st, src2, a->Bo.as<float>(), a->ldbo, n, m, nf, a->fired.as<int>(), Bx,
+                     a->n, a->snew.as<double>(), ws, &a->stats.kernel_launches);
+        scatter_s(a->st, a->fired.as<int>(), nf, a->snew.as<double>(), s,
+                  &a->stats.kernel_launches);
+        a->stats.dgks_fired += nf;
+    }
+    a->timer.end(PH_DGKS, t0);
+
+    t0 = a->timer.begin();
+    normalize_ybx(a->st, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), !linear_only,
+                  a->ybx.as<double>(), a->part.as<double>(), &a->stats.kernel_launches);
+    a->timer.end(PH_NORMALIZE, t0);
+
+    if (linear_only) {
+        return;
+    }
+    std::vector<SweepTask> tasks;
+    for (int b = 0; b < Pc;) {
+        int e = b;
+        while (e < Pc && cx_h[c0 + e] == cx_h[c0 + b]) {
+            ++e;
+        }
+        for (int t = b; t < e; t += 8) {
+            tasks.push_back({cx_h[c0 + b], t, std::min(8, e - t)});
+        }
+        b = e;
+    }
+    a->tasks.ensure(sizeof(SweepTask) * tasks.size());
+    CUDA_CHECK(cudaMemcpyAsync(a->tasks.ptr, tasks.data(), sizeof(SweepTask) * tasks.size(),
+                               cudaMemcpyHostToDevice, a->st));
+    t0 = a->timer.begin();
+    sweep_fp64(a->st, a->tasks.as<SweepTask>(), (int)tasks.size(), a->perm.as<int>(),
+               a->xsort.as<float>(), a->y.as<float>(), a->B.as<float>(), a->n, cb_d, Bx, a->n,
+               a->Bo.as<float>(), a->ldbo, a->ybo_d.as<double>(), a->ybx.as<double>(), n, m,
+               head, tail, min_span, a->tol, a->hsse.as<double>(), a->hrow.as<int>(),
+               &a->stats.kernel_launches);
+    a->timer.end(PH_SWEEP, t0);
+    a->stats.knot_evals += (long long)Pc *
+                           (tail - 1 >= head + 1 ? ((tail - 1 - (head + 1)) / min_span + 1) : 0);
+}
+
+void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, int min_span,
+               int end_span, int linear_only, double *sse0, double *lin, double *hin, double *cut)
+{
+    verify(rows >= 0 && (size_t)rows <= a->p, "invalid X column index");
+    verify(min_span >= 1, "min_span must be >= 1");
+    verify(end_span >= 0, "end_span must be >= 0");
+    verify(rows == 0 || mask != nullptr, "mask is null");
+    const int m = (int)a->m, n = (int)a->n;
+    verify(mask_stride >= m || rows <= 1, "mask row stride smaller than nbasis");
+    a->stats.evals += 1;
+
+    std::vector<int> cx, cb, cols;
+    for (int i = 0; i < rows; ++i) {
+        bool any = false;
+        for (int j = 0; j < m; ++j) {
+            if (mask[(size_t)i * mask_stride + j]) {
+                cx.push_back(i);
+                cb.push_back(j);
+                any = true;
+            }
+        }
+        if (any) {
+            cols.push_back(i);
+        }
+    }
+    const int P = (int)cx.size();
+    a->stats.candidates += P;
+    const size_t cnt = (size_t)rows * m;
+    a->out.ensure(sizeof(double) * 3 * std::max<size_t>(cnt, 1));
+    double *o_lin = a->out.as<double>(), *o_hin = o_lin + cnt, *o_cut = o_hin + cnt;
+    fill_outputs(a->st, rows, m, o_lin, o_hin, o_cut, &a->stats.kernel_launches);
+
+    const int head = end_span;
+    const int tail = head < n ? n - head : 0;
+    if (P > 0) {
+        if (!linear_only) {
+            ensure_sorted(a, cols);
+        }
+        const double budget = env_double("MARS_GPU_BLOCK_GB", 32.0) * 1e9;
+        // Candidate columns per block: the Bx scratch budget, and at most
+        // 2^18 so every per-column grid dimension stays within 65535 blocks.
+        size_t cap = (size_t)std::max(1.0, budget / (4.0 * n + 64.0 * m + 64.0));
+        cap = std::min<size_t>(cap, 262144);
+        const auto blocks = block_candidates(cx, cap);
+        size_t maxPc = 0;
+        for (auto &b : blocks) {
+            maxPc = std::max<size_t>(maxPc, b.second - b.first);
+        }
+        a->Bx.ensure(sizeof(float) * a->n * maxPc);
+        a->T.ensure(sizeof(double) * std::max<size_t>(1, (size_t)m * maxPc));
+        a->Tpart.ensure(sizeof(double) * std::max<size_t>(1, project_tpart_elems(n, m, (int)maxPc)));
+        a->part.ensure(sizeof(double) * std::max(project_part_elems(n, (int)maxPc),
+                                                 normalize_part_elems(n, (int)maxPc)));
+        a->svec.ensure(sizeof(double) * maxPc);
+        a->snew.ensure(sizeof(double) * maxPc);
+        a->ybx.ensure(sizeof(double) * maxPc);
+        a->hsse.ensure(sizeof(double) * maxPc);
+        a->hrow.ensure(sizeof(int) * maxPc);
+        a->fired.ensure(sizeof(int) * maxPc);
+        a->nfired.ensure(sizeof(int) * 4);
+        a->cand.ensure(sizeof(int) * 2 * (size_t)P);
+        int *cx_all = a->cand.as<int>(), *cb_all = cx_all + P;
+        CUDA_CHECK(cudaMemcpyAsync(cx_all, cx.data(), sizeof(int) * P, cudaMemcpyHostToDevice,
+                                   a->st));
+        CUDA_CHECK(cudaMemcpyAsync(cb_all, cb.data(), sizeof(int) * P, cudaMemcpyHostToDevice,
+                                   a->st));
+        for (auto &b : blocks) {
+            const int c0 = b.first, Pc = b.second - b.first;
+            const int *cx_d = cx_all + c0, *cb_d = cb_all + c0;
+            eval_block_fp64(a, Pc, cx_d, cb_d, cx, c0, min_span, head, tail, linear_only != 0);
+            assemble_outputs(a->st, Pc, cx_d, cb_d, m, a->ybx.as<double>(), a->hsse.as<double>(),
+                             a->hrow.as<int>(), a->X.as<float>(), a->n, linear_only != 0, o_lin,
+                             o_hin, o_cut, &a->stats.kernel_launches);
+        }
+    }
+    if (cnt) {
+        CUDA_CHECK(cudaMemcpyAsync(lin, o_lin, sizeof(double) * cnt, cudaMemcpyDeviceToHost, a->st));
+        CUDA_CHECK(cudaMemcpyAsync(hin, o_hin, sizeof(double) * cnt, cudaMemcpyDeviceToHost, a->st));
+        CUDA_CHECK(cudaMemcpyAsync(cut, o_cut, sizeof(double) * cnt, cudaMemcpyDeviceToHost, a->st));
+    }
+    sync(a);
+    a->timer.resolve(a->phase_ms);
+    if (sse0) {
+        double s = 0.0;
+        for (double v : a->ybo) {
+            s = std::fma(v, v, s);
+        }
+        *sse0 = s;
+    }
+}
+
+double append_impl(mars_gpu_algo *a, char type, int xcol, int bcol, float h)
+{
+    verify(a->m < a->max_terms, "basis matrix is full", MARS_GPU_EFULL);
+    if (bcol < 0 || (size_t)bcol >= a->m) {
+        char msg[80];
+        std::snprintf(msg, sizeof(msg), "invalid basis column number: %d", bcol);
+        throw Error(MARS_GPU_EINVAL, msg);
+    }
+    verify(xcol >= 0 && (size_t)xcol < a->p, "invalid X column index");
+    verify(type == 'l' || type == '+' || type == '-', "invalid basis type");
+    const int n = (int)a->n, m = (int)a->m;
+    AppendScratch ws = append_scratch(a);
+    double scal[3];
+    cudaEvent_t t0 = a->timer.begin();
+    append_fill(a->st, type, a->X.as<float>(), a->n, a->s.as<float>(), xcol, a->B.as<float>(),
+                a->n, bcol, m, h, n, ws, &a->stats.kernel_launches);
+    mgs_pass(a->st, a->BoC.as<float>(), n, m, ws, &a->stats.kernel_launches);
+    CUDA_CHECK(cudaMemcpyAsync(scal, ws.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, a->st));
+    sync(a);
+    double v_norm2 = scal[1];
+    if (v_norm2 > a->tol && v_norm2 * 9.0 < scal[0]) {
+        mgs_pass(a->st, a->BoC.as<float>(), n, m, ws, &a->stats.kernel_launches);
+        CUDA_CHECK(cudaMemcpyAsync(scal, ws.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                   a->st));
+        sync(a);
+        v_norm2 = scal[1];
+    }
+    const double w = std::sqrt(v_norm2);
+    double result = -1.0;
+    if (w * w > a->tol) {
+        append_store(a->st, w, a->Bo.as<float>(), a->ldbo, a->BoC.as<float>(), n, m,
+                     a->y.as<float>(), ws, &a->stats.kernel_launches);
+        CUDA_CHECK(cudaMemcpyAsync(scal + 2, ws.scal + 2, sizeof(double), cudaMemcpyDeviceToHost,
+                                   a->st));
+        sync(a);
+        const double ybo_m = scal[2];
+        double ybo_sq = ybo_m * ybo_m;
+        for (double e : a->ybo) {
+            ybo_sq = std::fma(e, e, ybo_sq);
+        }
+        const double mse = (1. - ybo_sq) / (double)n;
+        if (mse >= -a->tol) {
+            a->ybo.push_back(ybo_m);
+            CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.as<double>() + m, &a->ybo.back(), sizeof(double),
+                                       cudaMemcpyHostToDevice, a->st));
+            a->m += 1;
+            result = mse < 0.0 ? 0.0 : mse;
+        }
+    }
+    a->timer.end(PH_APPEND, t0);
+    sync(a);
+    a->timer.resolve(a->phase_ms);
+    return result;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char *mars_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int mars_gpu_device_count(void)
+{
+    int c = 0;
+    if (cudaGetDeviceCount(&c) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return c;
+}
+
+int mars_gpu_create(const float *X, const float *y, const float *w, size_t n, size_t p,
+                    size_t ldx, size_t max_terms, mars_gpu_algo **out)
+{
+    if (!out) {
+        g_last_error = "null output handle";
+        return MARS_GPU_EINVAL;
+    }
+    *out = nullptr;
+    mars_gpu_algo *a = nullptr;
+    int rc = guarded([&] {
+        verify(mars_gpu_device_count() > 0, "no CUDA device is visible", MARS_GPU_ECUDA);
+        verify((X || n * p == 0) && y && w, "null input array");
+        a = new mars_gpu_algo();
+        create_impl(a, X, y, w, n, p, ldx, max_terms);
+    });
+    if (rc != MARS_GPU_OK) {
+        delete a;
+        return rc;
+    }
+    *out = a;
+    return MARS_GPU_OK;
+}
+
+int mars_gpu_destroy(mars_gpu_algo *algo)
+{
+    delete algo;
+    return MARS_GPU_OK;
+}
+
+int mars_gpu_nbasis(const mars_gpu_algo *a, int *out)
+{
+    if (!a || !out) {
+        g_last_error = "null argument";
+        return MARS_GPU_EINVAL;
+    }
+    *out = (int)a->m;
+    return MARS_GPU_OK;
+}
+
+int mars_gpu_yvar(const mars_gpu_algo *a, double *out)
+{
+    if (!a || !out) {
+        g_last_error = "null argument";
+        return MARS_GPU_EINVAL;
+    }
+    *out = a->yvar;
+    return MARS_GPU_OK;
+}
+
+int mars_gpu_dsse(const mars_gpu_algo *a, double *out)
+{
+    if (!a || !out) {
+        g_last_error = "null argument";
+        return MARS_GPU_EINVAL;
+    }
+    double s = 0.0;
+    for (double v : a->ybo) {
+        s = std::fma(v, v, s);
+    }
+    *out = s;
+    return MARS_GPU_OK;
+}
+
+int mars_gpu_set_precision(mars_gpu_algo *a, int mode)
+{
+    return guarded([&] {
+        verify(a != nullptr, "null handle");
+        verify(mode == MARS_GPU_PREC_FP64 || mode == MARS_GPU_PREC_MIXED,
+               "unknown precision mode");
+        verify(mode == MARS_GPU_PREC_FP64, "the mixed-precision path is not built yet");
+        a->precision = mode;
+    });
+}
+
+int mars_gpu_eval(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, int min_span,
+                  int end_span, int linear_only, double *sse0, double *linear, double *hinge,
+                  double *cut)
+{
+    return guarded([&] {
+        verify(a != nullptr, "null handle");
+        verify(rows == 0 || (linear && hinge && cut), "null output array");
+        eval_impl(a, mask, rows, mask_stride, min_span, end_span, linear_only, sse0, linear, hinge,
+                  cut);
+    });
+}
+
+int mars_gpu_append(mars_gpu_algo *a, char type, int xcol, int bcol, float h, double *mse)
+{
+    return guarded([&] {
+        verify(a != nullptr && mse != nullptr, "null argument");
+        *mse = append_impl(a, type, xcol, bcol, h);
+    });
+}
+
+int mars_gpu_get_stats(const mars_gpu_algo *a, mars_gpu_stats *out)
+{
+    if (!a || !out) {
+        g_last_error = "null argument";
+        return MARS_GPU_EINVAL;
+    }
+    *out = a->stats;
+    out->ms_project = a->phase_ms[PH_PROJECT];
+    out->ms_dgks = a->phase_ms[PH_DGKS];
+    out->ms_normalize = a->phase_ms[PH_NORMALIZE];
+    out->ms_sweep = a->phase_ms[PH_SWEEP];
+    out->ms_sort = a->phase_ms[PH_SORT];
+    out->ms_append = a->phase_ms[PH_APPEND];
+    out->ms_redecide = a->phase_ms[PH_REDECIDE];
+    return MARS_GPU_OK;
+}
+
+int mars_gpu_orth_error(mars_gpu_algo *a, double *max_abs, double *rss)
+{
+    return guarded([&] {
+        verify(a != nullptr, "null handle");
+        const int n = (int)a->n, m = (int)a->m;
+        DevBuf T, Tpart;
+        T.ensure(sizeof(double) * (size_t)m * (m + 1));
+        Tpart.ensure(sizeof(double) * std::max<size_t>(1, project_tpart_elems(n, m, m)));
+        StoredSrc q{a->BoC.as<float>(), a->n, nullptr};
+        tgemm_fp64(a->st, q, a->Bo.as<float>(), a->ldbo, n, m, m, T.as<double>(),
+                   Tpart.as<double>(), Tpart.bytes / sizeof(double), &a->stats.kernel_launches);
+        std::vector<double> G((size_t)m * m);
+        CUDA_CHECK(cudaMemcpyAsync(G.data(), T.ptr, sizeof(double) * m * m,
+                                   cudaMemcpyDeviceToHost, a->st));
+        StoredSrc yy{a->y.as<float>(), a->n, nullptr};
+        tgemm_fp64(a->st, yy, a->Bo.as<float>(), a->ldbo, n, m, 1, T.as<double>(),
+                   Tpart.as<double>(), Tpart.bytes / sizeof(double), &a->stats.kernel_launches);
+        std::vector<double> r(m);
+        CUDA_CHECK(cudaMemcpyAsync(r.data(), T.ptr, sizeof(double) * m, cudaMemcpyDeviceToHost,
+                                   a->st));
+        sync(a);
+        double mx = 0.0;
+        for (int j = 0; j < m; ++j) {
+            for (int c = 0; c < m; ++c) {
+                const double d = G[(size_t)j * m + c] - (j == c ? 1.0 : 0.0);
+                mx = std::max(mx, std::fabs(d));
+            }
+        }
+        double rs = 0.0;
+        for (double v : r) {
+            rs = std::fma(v, v, rs);
+        }
+        if (max_abs) {
+            *max_abs = mx;
+        }
+        if (rss) {
+            *rss = 1.0 - rs;
+        }
+    });
+}
+
+int mars_gpu_orthonormalize(size_t n, size_t m, size_t p, const float *B, size_t ldB,
+                            const float *x, const int *mask, const float *Bo, size_t ldBo,
+                            float *Bx, size_t ldBx, double *s_out, double tol, long *dgks)
+{
+    return guarded([&] {
+        verify(mars_gpu_device_count() > 0, "no CUDA device is visible", MARS_GPU_ECUDA);
+        verify(n >= 1 && p >= 1, "empty problem");
+        verify(ldB >= n && ldBx >= n && ldBo >= m, "leading dimension smaller than the data");
+        verify(p <= 262144, "too many candidate columns for one call");
+        int nbcols = 0;
+        for (size_t j = 0; j < p; ++j) {
+            verify(mask[j] >= 0, "negative basis index in mask");
+            nbcols = std::max(nbcols, mask[j] + 1);
+        }
+        cudaStream_t st;
+        CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        DevBuf dB, dx, dBo, dBx, dT, dTp, dpart, ds, dsn, dybx, dcand, dfired, dnf, dy, dsx;
+        long long launches = 0;
+        dB.ensure(sizeof(float) * n * nbcols);
+        CUDA_CHECK(cudaMemcpy2DAsync(dB.ptr, n * sizeof(float), B, ldB * sizeof(float),
+                                     n * sizeof(float), nbcols, cudaMemcpyHostToDevice, st));
+        dx.ensure(sizeof(float) * n);
+        CUDA_CHECK(cudaMemcpyAsync(dx.ptr, x, sizeof(float) * n, cudaMemcpyHostToDevice, st));
+        const size_t ldbo = std::max<size_t>(ldBo, 1);
+        dBo.ensure(sizeof(float) * n * ldbo);
+        CUDA_CHECK(cudaMemcpyAsync(dBo.ptr, Bo, sizeof(float) * n * ldbo, cudaMemcpyHostToDevice, st));
+        float one = 1.0f;
+        dsx.ensure(sizeof(float));
+        CUDA_CHECK(cudaMemcpyAsync(dsx.ptr, &one, sizeof(float), cudaMemcpyHostToDevice, st));
+        dcand.ensure(sizeof(int) * 2 * p);
+        std::vector<int> zeros(p, 0);
+        CUDA_CHECK(cudaMemcpyAsync(dcand.ptr, zeros.data(), sizeof(int) * p, cudaMemcpyHostToDevice, st));
+        CUDA_CHECK(cudaMemcpyAsync(dcand.as<int>() + p, mask, sizeof(int) * p,
+                                   cudaMemcpyHostToDevice, st));
+        dBx.ensure(sizeof(float) * n * p);
+        dT.ensure(sizeof(double) * std::max<size_t>(1, m * p));
+        dTp.ensure(sizeof(double) * std::max<size_t>(1, project_tpart_elems((int)n, (int)m, (int)p)));
+        dpart.ensure(sizeof(double) * std::max(project_part_elems((int)n, (int)p),
+                                               normalize_part_elems((int)n, (int)p)));
+        ds.ensure(sizeof(double) * p);
+        dsn.ensure(sizeof(double) * p);
+        dybx.ensure(sizeof(double) * p);
+        dfired.ensure(sizeof(int) * p);
+        dnf.ensure(sizeof(int));
+        dy.ensure(sizeof(float) * n);
+        CUDA_CHECK(cudaMemsetAsync(dy.ptr, 0, sizeof(float) * n, st));
+        ProjectScratch ws{dT.as<double>(), dTp.as<double>(), dpart.as<double>(),
+                          dpart.bytes / sizeof(double), dTp.bytes / sizeof(double)};
+        FillSrc src{dB.as<float>(), n, dx.as<float>(), n, dsx.as<float>(), dcand.as<int>(),
+                    dcand.as<int>() + p};
+        project_fp64(st, src, dBo.as<float>(), ldbo, (int)n, (int)m, (int)p, nullptr,
+                     dBx.as<float>(), n, ds.as<double>(), ws, &launches);
+        dgks_gate(st, dT.as<double>(), (int)m, (int)p, ds.as<double>(), tol, dfired.as<int>(),
+                  dnf.as<int>(), &launches);
+        int nf = 0;
+        CUDA_CHECK(cudaMemcpyAsync(&nf, dnf.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        if (nf > 0) {
+            StoredSrc s2{dBx.as<float>(), n, dfired.as<int>()};
+            project_fp64(st, s2, dBo.as<float>(), ldbo, (int)n, (int)m, nf, dfired.as<int>(),
+                         dBx.as<float>(), n, dsn.as<double>(), ws, &launches);
+            scatter_s(st, dfired.as<int>(), nf, dsn.as<double>(), ds.as<double>(), &launches);
+        }
+        std::vector<double> sh(p);
+        CUDA_CHECK(cudaMemcpyAsync(sh.data(), ds.ptr, sizeof(double) * p, cudaMemcpyDeviceToHost, st));
+        normalize_ybx(st, dBx.as<float>(), n, (int)n, (int)p, ds.as<double>(), tol, dy.as<float>(),
+                      true, dybx.as<double>(), dpart.as<double>(), &launches);
+        CUDA_CHECK(cudaMemcpy2DAsync(Bx, ldBx * sizeof(float), dBx.ptr, n * sizeof(float),
+                                     n * sizeof(float), p, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        cudaStreamDestroy(st);
+        if (s_out) {
+            std::memcpy(s_out, sh.data(), sizeof(double) * p);
+        }
+        if (dgks) {
+            *dgks += nf;
+        }
+    });
+}
+
+int mars_gpu_orthonormalize_col(size_t n, size_t m, double *v, const float *Bo, size_t ldBo,
+                                double tol, double *w_out, long *dgks)
+{
+    return guarded([&] {
+        verify(mars_gpu_device_count() > 0, "no CUDA device is visible", MARS_GPU_ECUDA);
+        verify(n >= 1, "empty problem");
+        cudaStream_t st;
+        CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        std::vector<float> colmajor(n * std::max<size_t>(m, 1));
+        for (size_t j = 0; j < m; ++j) {
+            for (size_t i = 0; i < n; ++i) {
+                colmajor[j * n + i] = Bo[i * ldBo + j];
+            }
+        }
+        DevBuf dBoC, dv, dpart, dcoef, dscal;
+        long long launches = 0;
+        const int nb = append_blocks((int)n);
+        dBoC.ensure(sizeof(float) * colmajor.size());
+        CUDA_CHECK(cudaMemcpyAsync(dBoC.ptr, colmajor.data(), sizeof(float) * colmajor.size(),
+                                   cudaMemcpyHostToDevice, st));
+        dv.ensure(sizeof(double) * n);
+        CUDA_CHECK(cudaMemcpyAsync(dv.ptr, v, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        dpart.ensure(sizeof(double) * 2 * nb);
+        dcoef.ensure(sizeof(double) * (m + 1));
+        dscal.ensure(sizeof(double) * 8);
+        AppendScratch ws{dv.as<double>(), dpart.as<double>(), dcoef.as<double>(),
+                         dscal.as<double>(), nb};
+        double scal[2];
+        mgs_pass(st, dBoC.as<float>(), (int)n, (int)m, ws, &launches);
+        CUDA_CHECK(cudaMemcpyAsync(scal, ws.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        double vn = scal[1];
+        if (vn > tol && vn * 9.0 < scal[0]) {
+            mgs_pass(st, dBoC.as<float>(), (int)n, (int)m, ws, &launches);
+            CUDA_CHECK(cudaMemcpyAsync(scal, ws.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            vn = scal[1];
+            if (dgks) {
+                *dgks += 1;
+            }
+        }
+        CUDA_CHECK(cudaMemcpyAsync(v, dv.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        cudaStreamDestroy(st);
+        const double w = std::sqrt(vn);
+        if (w * w > tol) {
+            for (size_t i = 0; i < n; ++i) {
+                v[i] /= w;
+            }
+        }
+        if (w_out) {
+            *w_out = w;
+        }
+    });
+}
+
+}  // extern "C"

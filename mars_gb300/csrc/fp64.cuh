@@ -1,0 +1,136 @@
+// FP64 forward-pass kernels: the plain FP64 GPU path and the FP64 re-decision
+// path of the mixed mode. Launch wrappers are host functions on a stream.
+#pragma once
+
+#include "common.cuh"
+
+namespace mgpu {
+
+// Candidate column source: Bx[i, j] = B[i, cand_b[j]] * (X[i, cand_x[j]] * s[cand_x[j]]),
+// both products in f32 (marsalgo.cc:436-441 and kernels.cc:298-312).
+struct FillSrc {
+    const float *B;
+    size_t ldB;
+    const float *X;
+    size_t ldX;
+    const float *s;
+    const int *cand_x;
+    const int *cand_b;
+    __device__ __forceinline__ float operator()(size_t i, int j) const
+    {
+        const int xc = cand_x[j];
+        return B[i + (size_t)cand_b[j] * ldB] * (X[i + (size_t)xc * ldX] * s[xc]);
+    }
+};
+
+// Candidate column source: an already-stored f32 column Bx[:, col[j]] (col may be null).
+struct StoredSrc {
+    const float *Bx;
+    size_t ldBx;
+    const int *col;
+    __device__ __forceinline__ float operator()(size_t i, int j) const
+    {
+        const int c = col ? col[j] : j;
+        return Bx[i + (size_t)c * ldBx];
+    }
+};
+
+// One block of the hinge sweep: up to 8 candidates that share an input column.
+struct SweepTask {
+    int xcol;
+    int cand0;
+    int count;
+};
+
+// Projection of P candidate columns onto the m columns of Bo (row-major, ldbo).
+//   T = Bo^T Bx               (FP64 accumulation, deterministic split-K)
+//   Bx <- f32(Bx - Bo T)      (FP64 arithmetic, one rounding)
+//   s  = ||Bx||^2             (FP64, of the rounded values)
+// `out_col` maps candidate j to its output column (null: identity).
+struct ProjectScratch {
+    double *T;      // [P][m]
+    double *Tpart;  // [splits][P][m]
+    double *part;   // [row blocks][P]
+    size_t part_elems;
+    size_t tpart_elems;
+};
+
+template <class Src>
+void project_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, int n, int m,
+                  int P, const int *out_col, float *Bx, size_t ldBx, double *s_out,
+                  const ProjectScratch &ws, long long *launches);
+
+// Workspace sizes (elements) for project_fp64 / normalize_ybx.
+size_t project_tpart_elems(int n, int m, int P);
+size_t project_part_elems(int n, int P);
+size_t normalize_part_elems(int n, int P);
+
+// T[j][c] = sum_i Bo[i,c] * src(i, j) only (FP64, deterministic split-K).
+template <class Src>
+void tgemm_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, int n, int m,
+                int P, double *T, double *Tpart, size_t tpart_elems, long long *launches);
+
+// s[fired[q]] = snew[q] for q < nf.
+void scatter_s(cudaStream_t st, const int *fired, int nf, const double *snew, double *s,
+               long long *launches);
+
+// DGKS gate (kernels.cc:384-395): fired = s > tol && 9 s < ||T_j||^2; the
+// fired candidate indexes are appended to `fired` (count in *nfired).
+void dgks_gate(cudaStream_t st, const double *T, int m, int P, const double *s, double tol,
+               int *fired, int *nfired, long long *launches);
+
+// Normalise (kernels.cc:401-416) and ybx = Bx^T y (kernels.cc:215-237):
+// scale = s > tol ? f32(1/sqrt(s+tol)) : 0; Bx *= scale (if store); ybx in FP64.
+void normalize_ybx(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const double *s,
+                   double tol, const float *y, bool store, double *ybx, double *part,
+                   long long *launches);
+
+// Hinge sweep in FP64 (marsalgo.cc:508-657), one warp per candidate.
+void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *perm,
+                const float *xsort, const float *y, const float *B, size_t ldB,
+                const int *cand_b, const float *Bx, size_t ldBx, const float *Bo, size_t ldbo,
+                const double *ybo, const double *ybx, int n, int m, int head, int tail,
+                int min_span, double tol, double *hsse, int *hrow, long long *launches);
+
+// Stable descending argsort of X columns (marsalgo.cc:33-39) and the scaled
+// sorted values xsort[i] = X[perm[i]] * s.
+void sort_columns(cudaStream_t st, const float *X, size_t ldX, const float *s, int n,
+                  const int *cols, int ncols, int *perm, float *xsort, DevBuf &keys,
+                  DevBuf &vals, DevBuf &tmp, long long *launches);
+
+// Scatter per-candidate results into the (rows, m) outputs.
+void assemble_outputs(cudaStream_t st, int P, const int *cand_x, const int *cand_b, int m,
+                      const double *ybx, const double *hsse, const int *hrow, const float *X,
+                      size_t ldX, bool linear_only, double *lin, double *hin, double *cut,
+                      long long *launches);
+void fill_outputs(cudaStream_t st, int rows, int m, double *lin, double *hin, double *cut,
+                  long long *launches);
+
+// --- append (marsalgo.cc:760-875 and kernels.cc:194-281) -------------------
+struct AppendScratch {
+    double *v;       // n
+    double *part;    // 2 * nblocks
+    double *coef;    // max_terms
+    double *scal;    // small result slots
+    int nblocks;
+};
+int append_blocks(int n);
+// Bm = s * B[:,bcol] * f(X[:,xcol]) into B[:, m]; v = (double)Bm; then
+// Bm /= f32(sqrt(sum v^2)). type: 'l', '+', '-'.
+void append_fill(cudaStream_t st, char type, const float *X, size_t ldX, const float *s,
+                 int xcol, float *B, size_t ldB, int bcol, int m, float h, int n,
+                 const AppendScratch &ws, long long *launches);
+// One modified Gram-Schmidt pass of v against BoC[:, 0:m] (column-major, ld n);
+// leaves sum(c^2) in scal[0] and ||v||^2 in scal[1].
+void mgs_pass(cudaStream_t st, const float *BoC, int n, int m, const AppendScratch &ws,
+              long long *launches);
+// v /= w; store f32(v) as column m of Bo (row-major) and BoC; ybo_m -> scal[2].
+void append_store(cudaStream_t st, double w, float *Bo, size_t ldbo, float *BoC, int n, int m,
+                  const float *y, const AppendScratch &ws, long long *launches);
+
+// Column sums of squares sum_i X[i,j]^2 in FP64 (for s = 1/rms).
+void column_sumsq(cudaStream_t st, const float *X, size_t ldX, int n, int p, double *out,
+                  double *part, long long *launches);
+
+
+}  // namespace mgpu

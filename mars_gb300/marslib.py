@@ -1,2 +1,244 @@
-"""placeholder"""
+"""``marslib`` surface over the GB300 C ABI (include/mars_gpu.h).
+
+Mirrors the reference pybind11 module (marslib.cc:152-179):
+``MarsAlgo(X, y, w, max_terms)`` with ``eval``, ``append``, ``nbasis``,
+``yvar`` and ``__version__``, raising ``RuntimeError`` with the reference's
+messages. Every call goes to ``lib/libmars_gpu.so``; there is no CPU path,
+so a missing library or GPU is an error, never a silent fallback.
+
+Extras over the reference: ``dsse()``, ``set_precision('fp64'|'mixed')``,
+``stats()`` and ``orth_error()`` (max |Q^T Q - I| and the FP64 RSS).
+"""
+import ctypes
+import os
+
+import numpy as np
+
 __version__ = "0.12"
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libmars_gpu.so")
+PREC_FP64, PREC_MIXED = 0, 1
+_lib = None
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("evals", ctypes.c_longlong),
+        ("candidates", ctypes.c_longlong),
+        ("knot_evals", ctypes.c_longlong),
+        ("dgks_fired", ctypes.c_longlong),
+        ("redecided", ctypes.c_longlong),
+        ("kernel_launches", ctypes.c_longlong),
+        ("ms_project", ctypes.c_double),
+        ("ms_dgks", ctypes.c_double),
+        ("ms_normalize", ctypes.c_double),
+        ("ms_sweep", ctypes.c_double),
+        ("ms_sort", ctypes.c_double),
+        ("ms_append", ctypes.c_double),
+        ("ms_redecide", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def load():
+    """Load libmars_gpu.so and bind its C ABI (raises if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.isfile(LIB_PATH):
+        raise RuntimeError(
+            "marslib: %s is not built; run mars_gb300.build.build() (nvcc, sm_103a)" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    vp, sz, i, d = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_double
+    fp = ctypes.POINTER(ctypes.c_float)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    lp = ctypes.POINTER(ctypes.c_long)
+    bp = ctypes.POINTER(ctypes.c_bool)
+    sig = {
+        "mars_gpu_last_error": (ctypes.c_char_p, []),
+        "mars_gpu_device_count": (i, []),
+        "mars_gpu_create": (i, [fp, fp, fp, sz, sz, sz, sz, ctypes.POINTER(vp)]),
+        "mars_gpu_destroy": (i, [vp]),
+        "mars_gpu_nbasis": (i, [vp, ip]),
+        "mars_gpu_yvar": (i, [vp, dp]),
+        "mars_gpu_dsse": (i, [vp, dp]),
+        "mars_gpu_set_precision": (i, [vp, i]),
+        "mars_gpu_eval": (i, [vp, bp, i, i, i, i, i, dp, dp, dp, dp]),
+        "mars_gpu_append": (i, [vp, ctypes.c_char, i, i, ctypes.c_float, dp]),
+        "mars_gpu_get_stats": (i, [vp, ctypes.POINTER(Stats)]),
+        "mars_gpu_orth_error": (i, [vp, dp, dp]),
+        "mars_gpu_orthonormalize": (i, [sz, sz, sz, fp, sz, fp, ip, fp, sz, fp, sz, dp, d, lp]),
+        "mars_gpu_orthonormalize_col": (i, [sz, sz, dp, fp, sz, d, dp, lp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != 0:
+        raise RuntimeError(load().mars_gpu_last_error().decode())
+
+
+def _p(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def _as_f32_vector(a, name):
+    if not isinstance(a, np.ndarray) or a.dtype != np.float32:
+        raise TypeError("MarsAlgo(): %s must be a float32 numpy array" % name)
+    return a
+
+
+class MarsAlgo:
+    """Device-resident forward-pass state (marsalgo.h:16-120)."""
+
+    def __init__(self, X, y, w, max_terms):
+        _as_f32_vector(X, "X")
+        _as_f32_vector(y, "y")
+        _as_f32_vector(w, "w")
+        if X.ndim != 2:
+            raise RuntimeError("expected 2D array for X")
+        if y.ndim != 1:
+            raise RuntimeError("expected 1D array for y")
+        if w.ndim != 1:
+            raise RuntimeError("expected 1D array for w")
+        if X.strides[0] != 4:
+            raise RuntimeError("X must be column-major")
+        if y.strides[0] != 4:
+            raise RuntimeError("y must be column-major")
+        if w.strides[0] != 4:
+            raise RuntimeError("w must be column-major")
+        if X.shape[0] != y.shape[0]:
+            raise RuntimeError("invalid dimension for y")
+        if X.shape[0] != w.shape[0]:
+            raise RuntimeError("invalid dimension for w")
+        L = load()
+        n, p = X.shape
+        ldx = X.strides[1] // 4 if p > 1 else n
+        h = ctypes.c_void_p()
+        check(L.mars_gpu_create(_p(X, ctypes.c_float), _p(y, ctypes.c_float),
+                                _p(w, ctypes.c_float), n, p, ldx, int(max_terms), ctypes.byref(h)))
+        self._h = h
+        self._L = L
+        self._p = p
+        mode = os.environ.get("MARS_GPU_PRECISION", "").strip().lower()
+        if mode:
+            self.set_precision(mode)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.mars_gpu_destroy(h)
+            self._h = None
+
+    def nbasis(self):
+        out = ctypes.c_int()
+        check(self._L.mars_gpu_nbasis(self._h, ctypes.byref(out)))
+        return out.value
+
+    def yvar(self):
+        out = ctypes.c_double()
+        check(self._L.mars_gpu_yvar(self._h, ctypes.byref(out)))
+        return out.value
+
+    def dsse(self):
+        out = ctypes.c_double()
+        check(self._L.mars_gpu_dsse(self._h, ctypes.byref(out)))
+        return out.value
+
+    def set_precision(self, mode):
+        modes = {"fp64": PREC_FP64, "mixed": PREC_MIXED}
+        if mode not in modes:
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        check(self._L.mars_gpu_set_precision(self._h, modes[mode]))
+
+    def eval(self, mask, min_span, endspan, linear_only, threads, cuda=False):
+        """(dsse, linear, hinge, cut) for every (input, parent) pair selected by
+        the (p, nbasis) row-major bool `mask` (marslib.cc:41-148). `threads`
+        and `cuda` are accepted for compatibility; the GPU evaluates all pairs."""
+        if not isinstance(mask, np.ndarray) or mask.dtype != np.bool_:
+            raise TypeError("eval(): mask must be a bool numpy array")
+        if mask.ndim != 2:
+            raise RuntimeError("expected 2D array for mask")
+        if mask.strides[1] != 1:
+            raise RuntimeError("mask must be row-major")
+        m = self.nbasis()
+        if mask.shape[1] != m:
+            raise RuntimeError("invalid dimension for mask")
+        if min_span < 1:
+            raise RuntimeError("min_span must be >= 1")
+        rows = mask.shape[0]
+        lin = np.empty((rows, m))
+        hin = np.empty((rows, m))
+        cut = np.empty((rows, m))
+        sse0 = ctypes.c_double()
+        stride = mask.strides[0] if rows > 0 else m
+        check(self._L.mars_gpu_eval(self._h, _p(mask, ctypes.c_bool), rows, stride,
+                                    int(min_span), int(endspan), int(bool(linear_only)),
+                                    ctypes.byref(sse0), _p(lin, ctypes.c_double),
+                                    _p(hin, ctypes.c_double), _p(cut, ctypes.c_double)))
+        return sse0.value, lin, hin, cut
+
+    def append(self, type, xcol, bcol, h):
+        """Add basis 'l', '+' or '-' (marsalgo.cc:760-875); returns the MSE or -1."""
+        t = type.encode() if isinstance(type, str) else bytes(type)
+        if len(t) != 1:
+            raise RuntimeError("invalid basis type")
+        mse = ctypes.c_double()
+        check(self._L.mars_gpu_append(self._h, t, int(xcol), int(bcol), float(h),
+                                      ctypes.byref(mse)))
+        return mse.value
+
+    def stats(self):
+        s = Stats()
+        check(self._L.mars_gpu_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def orth_error(self):
+        mx, rss = ctypes.c_double(), ctypes.c_double()
+        check(self._L.mars_gpu_orth_error(self._h, ctypes.byref(mx), ctypes.byref(rss)))
+        return mx.value, rss.value
+
+
+def device_count():
+    return load().mars_gpu_device_count()
+
+
+def orthonormalize(B, x, mask, Bo, m, tol):
+    """Kernel-level mars::orthonormalize on the GPU (kernels.h:52-62).
+    B (n, *) column-major f32, Bo (n, >= m) row-major f32. Returns (Bx, s, dgks)."""
+    L = load()
+    B = np.asfortranarray(B, dtype=np.float32)
+    Bo = np.ascontiguousarray(Bo, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    mask = np.ascontiguousarray(mask, dtype=np.int32)
+    n, p = B.shape[0], len(mask)
+    Bx = np.zeros((n, p), dtype=np.float32, order="F")
+    s = np.zeros(p)
+    c = ctypes.c_long(0)
+    check(L.mars_gpu_orthonormalize(n, m, p, _p(B, ctypes.c_float), n, _p(x, ctypes.c_float),
+                                    _p(mask, ctypes.c_int), _p(Bo, ctypes.c_float), Bo.shape[1],
+                                    _p(Bx, ctypes.c_float), n, _p(s, ctypes.c_double), tol,
+                                    ctypes.byref(c)))
+    return Bx, s, c.value
+
+
+def orthonormalize_col(v, Bo, m, tol):
+    """Kernel-level mars::orthonormalize_col on the GPU (kernels.h:91-96).
+    Returns (w, v_out, dgks)."""
+    L = load()
+    v = np.array(v, dtype=np.float64)
+    Bo = np.ascontiguousarray(Bo, dtype=np.float32)
+    w = ctypes.c_double()
+    c = ctypes.c_long(0)
+    check(L.mars_gpu_orthonormalize_col(len(v), m, _p(v, ctypes.c_double), _p(Bo, ctypes.c_float),
+                                        Bo.shape[1], tol, ctypes.byref(w), ctypes.byref(c)))
+    return w.value, v, c.value

@@ -1,0 +1,212 @@
+"""GPU parity: the CUDA path against the CPU oracle and the reference's goldens.
+
+All calls go through the C ABI (include/mars_gpu.h) via mars_gb300.marslib.
+Tolerances:
+  term path (type, parent, input, knot)   bit-exact vs the reference golden
+  r2 / r2_cv                               1e-6 absolute (f4 fields)
+  linear delta SSE                         1e-12 relative vs the oracle
+  hinge delta SSE                          1e-9 relative vs the oracle
+  knot (cut)                               bit-exact
+  append MSE                               1e-12 relative
+  orthonormalised columns                  1e-6 absolute (f32 storage, one ulp)
+"""
+import os
+
+import numpy as np
+import pytest
+
+from mars_gb300 import mars
+from tests import scenarios
+from tests.golden import cases
+from tests.test_oracle import assert_same_path, load_fit
+
+pytestmark = pytest.mark.gpu
+
+PRECISIONS = ["fp64"]
+
+
+@pytest.fixture(scope="module")
+def be_gpu(gpu):
+    return scenarios.GpuBackend(precision="fp64")
+
+
+@pytest.fixture(scope="module")
+def be_port(port):
+    return scenarios.OracleBackend("port")
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name", cases.FIT_CASES)
+def test_golden_term_path_gpu(name, precision, gpu, monkeypatch):
+    monkeypatch.setenv("MARS_GPU_PRECISION", precision)
+    g = load_fit(name)
+    X, y, w, kw = cases.fit_case(name)
+    model = mars.fit(X, y, w, **kw)
+    assert_same_path(model, g)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name", cases.EVAL_CASES)
+def test_eval_matches_oracle(name, precision, gpu, port):
+    import oracle
+
+    X, y, w, appends, evals = cases.eval_case(name)
+    a_gpu = gpu.MarsAlgo(X, y, w, cases.EVAL_MAX_TERMS)
+    a_gpu.set_precision(precision)
+    a_cpu = oracle.OracleAlgo(X, y, w, cases.EVAL_MAX_TERMS, kind="port")
+    assert a_gpu.yvar() == a_cpu.yvar()
+    for ap in appends:
+        mg, mc = a_gpu.append(*ap), a_cpu.append(*ap)
+        assert mg == pytest.approx(mc, rel=1e-12, abs=1e-300)
+    assert a_gpu.nbasis() == a_cpu.nbasis()
+    assert a_gpu.dsse() == pytest.approx(a_cpu.dsse(), rel=1e-14)
+    for i, (ms, es, lo) in enumerate(evals):
+        mask = cases.eval_mask(X.shape[1], a_cpu.nbasis(), i)
+        dg, lg, hg, cg = a_gpu.eval(mask, ms, es, lo, 1)
+        dc, lc, hc, cc = a_cpu.eval(mask, ms, es, lo, 1)
+        assert dg == pytest.approx(dc, rel=1e-14)
+        np.testing.assert_allclose(lg, lc, rtol=1e-12, atol=1e-300)
+        np.testing.assert_allclose(hg, hc, rtol=1e-9, atol=1e-300)
+        np.testing.assert_array_equal(cg, cc)
+    mx, rss = a_gpu.orth_error()
+    assert mx < 1e-5
+    assert rss == pytest.approx(1 - a_gpu.dsse(), rel=1e-6)
+
+
+def test_delta_sse_gpu(be_gpu):
+    scenarios.delta_sse(be_gpu, hinge_tol=1e-6)
+
+
+def test_weighted_ls_gpu(be_gpu):
+    scenarios.weighted_ls(be_gpu)
+
+
+def test_min_span_gpu(be_gpu):
+    scenarios.min_span(be_gpu)
+
+
+def test_orthonormalize_basic_gpu(be_gpu):
+    scenarios.orthonormalize_basic(be_gpu)
+
+
+def test_orthonormalize_col_gpu(be_gpu):
+    scenarios.orthonormalize_col_cases(be_gpu)
+
+
+def test_orthonormalize_stress_matches_oracle(be_gpu, be_port):
+    Bx_g, s_g, d_g = scenarios.orthonormalize_stress(be_gpu)
+    Bx_c, s_c, d_c = scenarios.orthonormalize_stress(be_port)
+    assert d_g == d_c
+    np.testing.assert_allclose(Bx_g, Bx_c, rtol=0, atol=1e-6)
+    np.testing.assert_allclose(s_g, s_c, rtol=1e-10, atol=1e-300)
+
+
+def test_orthonormalize_matches_oracle_random(be_gpu, be_port):
+    rng = np.random.default_rng(5)
+    n, m, p = 4096, 32, 12
+    Bo = scenarios.make_orthonormal_basis(n, m, rng, bad_col=3)
+    B = rng.uniform(-1, 1, (n, m)).astype(np.float32)
+    B[:, 7] = B[:, 6]
+    B[:, 10] = 0
+    x = (rng.uniform(-1, 1, n) * 4).astype(np.float32)
+    mask = np.sort(rng.permutation(m)[:p]).astype(np.int32)
+    r_g = be_gpu.orthonormalize(np.asfortranarray(B), x, mask, Bo, m, 1e-14)
+    r_c = be_port.orthonormalize(np.asfortranarray(B), x, mask, Bo, m, 1e-14)
+    np.testing.assert_allclose(r_g[0], r_c[0], rtol=0, atol=1e-6)
+    assert r_g[2] == r_c[2]
+
+
+def _rand_problem(n, p, seed):
+    rng = np.random.default_rng(seed)
+    X = np.asfortranarray(rng.standard_normal((n, p)).astype(np.float32))
+    y = (X[:, 0] - np.maximum(X[:, -1] - 0.3, 0) + 0.3 * rng.standard_normal(n)).astype(np.float32)
+    return X, y, np.ones(n, np.float32)
+
+
+def test_errors_match_reference_messages(gpu):
+    X, y, w = _rand_problem(200, 3, 0)
+    with pytest.raises(RuntimeError, match="target Y is all zero or NANs"):
+        gpu.MarsAlgo(X, np.zeros(200, np.float32), w, 5)
+    Xb = X.copy(order="F")
+    Xb[7, 2] = np.nan
+    with pytest.raises(RuntimeError, match="not all columns in X are finite"):
+        gpu.MarsAlgo(Xb, y, w, 5)
+    a = gpu.MarsAlgo(X, y, w, 2)
+    with pytest.raises(RuntimeError, match="invalid basis column number: 1"):
+        a.append("l", 0, 1, 0)
+    with pytest.raises(RuntimeError, match="invalid basis type"):
+        a.append("x", 0, 0, 0)
+    with pytest.raises(RuntimeError, match="invalid dimension for mask"):
+        a.eval(np.ones((3, 2), bool), 1, 0, False, 1)
+    with pytest.raises(RuntimeError, match="min_span must be >= 1"):
+        a.eval(np.ones((3, 1), bool), 0, 0, False, 1)
+    with pytest.raises(RuntimeError, match="invalid X column index"):
+        a.eval(np.ones((4, 1), bool), 1, 0, False, 1)
+    assert a.append("l", 0, 0, 0) >= 0
+    with pytest.raises(RuntimeError, match="basis matrix is full"):
+        a.append("l", 1, 0, 0)
+
+
+@pytest.mark.parametrize("end_span", [0, 1, 7, 199, 200, 5000])
+def test_edge_end_span(gpu, port, end_span):
+    import oracle
+
+    X, y, w = _rand_problem(200, 3, 1)
+    X[:, 1] = np.round(X[:, 1])  # ties
+    a_g = gpu.MarsAlgo(X, y, w, 6)
+    a_c = oracle.OracleAlgo(X, y, w, 6, kind="port")
+    for ap in [("l", 0, 0, 0), ("+", 2, 0, 0.1)]:
+        assert a_g.append(*ap) == pytest.approx(a_c.append(*ap), rel=1e-12)
+    mask = np.ones((3, a_c.nbasis()), bool)
+    mask[2, 1] = False
+    rg = a_g.eval(mask, 3, end_span, False, 1)
+    rc = a_c.eval(mask, 3, end_span, False, 1)
+    np.testing.assert_allclose(rg[1], rc[1], rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(rg[2], rc[2], rtol=1e-9, atol=1e-300)
+    np.testing.assert_array_equal(rg[3], rc[3])
+
+
+def test_edge_degenerate_columns(gpu, port):
+    import oracle
+
+    X, y, w = _rand_problem(300, 4, 2)
+    X[:, 1] = 0.0          # all-zero column
+    X[:, 2] = 1.5          # constant column (in the span of the intercept)
+    a_g = gpu.MarsAlgo(X, y, w, 8)
+    a_c = oracle.OracleAlgo(X, y, w, 8, kind="port")
+    for ap in [("l", 1, 0, 0), ("l", 2, 0, 0), ("l", 0, 0, 0), ("-", 3, 0, 0.0)]:
+        assert a_g.append(*ap) == pytest.approx(a_c.append(*ap), rel=1e-12)
+    assert a_g.nbasis() == a_c.nbasis()
+    mask = np.ones((4, a_c.nbasis()), bool)
+    mask[0, :] = False  # an input with no candidate
+    rg = a_g.eval(mask, 1, 0, False, 1)
+    rc = a_c.eval(mask, 1, 0, False, 1)
+    for k in (1, 2, 3):
+        np.testing.assert_allclose(rg[k], rc[k], rtol=1e-9, atol=1e-300)
+
+
+def test_small_n_and_single_column(gpu, port):
+    import oracle
+
+    for n in (2, 3, 17):
+        X, y, w = _rand_problem(n, 1, n)
+        a_g = gpu.MarsAlgo(X, y, w, 4)
+        a_c = oracle.OracleAlgo(X, y, w, 4, kind="port")
+        mask = np.ones((1, 1), bool)
+        rg = a_g.eval(mask, 1, 0, False, 1)
+        rc = a_c.eval(mask, 1, 0, False, 1)
+        for k in (1, 2, 3):
+            np.testing.assert_allclose(rg[k], rc[k], rtol=1e-9, atol=1e-300)
+
+
+def test_fit_with_weights_and_nan_target(gpu, port_lib):
+    rng = np.random.default_rng(3)
+    n = 3000
+    X = np.asfortranarray(rng.standard_normal((n, 4)).astype(np.float32))
+    y = (X[:, 0] * X[:, 1] + np.maximum(X[:, 2], 0) + 0.1 * rng.standard_normal(n)).astype(np.float32)
+    y[::37] = np.nan
+    w = (0.5 + rng.random(n)).astype(np.float32)
+    kw = dict(max_terms=11, min_span=3, tail_span=0.01)
+    m_g = mars.fit(X, y, w, **kw)
+    m_c = mars.forward_pass(port_lib, X, y, w, **kw)
+    assert [tuple(r)[:4] for r in m_g.tolist()] == [tuple(r)[:4] for r in m_c.tolist()]
