@@ -1,0 +1,432 @@
+#!/usr/bin/env python3
+"""Forward-pass benchmark on one GB300 (or N independent replicas).
+
+One step = one complete MARS forward pass (mars.fit) of the full hinge-search
+workload: X n=100,000 x p=20 iid N(0,1) float32, y = 6 random hinges + 3 hinge
+products + N(0, 0.5^2), max_terms=31, max_degree=2, tail_span=0 (synthetic,
+seeded; mars_gb300/workloads.py). Metric: knot evaluations per second (grid
+cuts scored by the hinge sweep, summed over every epoch and candidate), and
+the fit time.
+
+value        knot-evals/s over the device span of the fits (CUDA events on the
+             library's stream from the first eval to the last append; X, y
+             already resident in HBM), whole job (all ranks) / max rank time.
+e2e          the same metric through mars.fit with host arrays: host->device
+             upload of X, y, w and every eval's result download inside the
+             timed region (wall clock with the device synchronised).
+roofline     the dominant kernel of the timed region against the measured
+             peaks in MEASURED_PEAKS.json (HBM GB/s or tensor TFLOP/s).
+cpu_baseline the CPU oracle (the C restatement of the reference CPU path) on
+             the host cores, one fit of the same workload.
+
+--impl reference times that CPU implementation alone on the same workload.
+Under torchrun (N > 1) every rank runs its own replica on its own GPU (the
+fit does not exchange data between GPUs); timing is max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORLD = int(os.environ.get("WORLD_SIZE", "1"))
+RANK = int(os.environ.get("RANK", "0"))
+LOCAL_RANK = int(os.environ.get("LOCAL_RANK", "0"))
+if WORLD > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
+    os.environ["CUDA_VISIBLE_DEVICES"] = str(LOCAL_RANK)
+
+import numpy as np  # noqa: E402
+
+METRIC = "knot-evals/sec & fit time: mixed-prec batched vs FP64 GPU, same term path"
+UNIT = "knot-evals/s"
+WORKLOADS = {
+    "hinge_search": "hinge_search n=100000 p=20 iid N(0,1), 6 hinges + 3 hinge products, "
+                    "max_terms=31 max_degree=2 tail_span=0 (config 2)",
+    "precision_stress": "precision_stress n=1000000 p=100 AR(1) rho=0.9 + 5 near-duplicates, "
+                        "max_terms=63 tail_span=0 (config 3)",
+    "plain_fit": "plain_fit n=10000 p=2 linear_only max_terms=17 (config 1)",
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default=os.environ.get("MARS_BENCH_PRECISION", "fp64"),
+                    choices=["mixed", "fp64"])
+    ap.add_argument("--workload", default="hinge_search", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the FP64 comparator fits when timing the mixed path")
+    return ap.parse_args()
+
+
+def workload(name):
+    from mars_gb300 import workloads
+
+    if name == "hinge_search":
+        return workloads.hinge_search()
+    if name == "precision_stress":
+        return workloads.precision_stress()
+    return workloads.plain_fit()
+
+
+class Counting:
+    """A marslib-like module that counts knot evaluations and keeps the algo."""
+
+    def __init__(self, factory):
+        self.__version__ = "0.12"
+        self._factory = factory
+        self.algo = None
+        self.knot_evals = 0
+        self.candidates = 0
+
+    def MarsAlgo(self, X, y, w, max_terms):
+        from mars_gb300 import workloads
+
+        inner = self._factory(X, y, w, max_terms)
+        outer = self
+        n = X.shape[0]
+
+        class Wrapped:
+            def __getattr__(self, k):
+                return getattr(inner, k)
+
+            def eval(self, mask, min_span, endspan, linear_only, threads, cuda=False):
+                res = inner.eval(mask, min_span, endspan, linear_only, threads, cuda)
+                c = int(mask.sum())
+                outer.candidates += c
+                if not linear_only:
+                    outer.knot_evals += c * workloads.knot_evals(n, endspan, min_span)
+                return res
+
+        self.algo = inner
+        return Wrapped()
+
+
+def path_of(model):
+    return [(r["type"].decode(), int(r["basis"]), int(r["input"]),
+             None if np.isnan(r["hinge"]) else float(r["hinge"])) for r in model]
+
+
+def gpu_fit(X, y, kw, precision):
+    from mars_gb300 import marslib
+    from mars_gb300.mars import forward_pass
+
+    def factory(X_, y_, w_, mt):
+        a = marslib.MarsAlgo(X_, y_, w_, mt)
+        a.set_precision(precision)
+        return a
+
+    lib = Counting(factory)
+    t0 = time.perf_counter()
+    model = forward_pass(lib, X, y, None, **kw)
+    wall = time.perf_counter() - t0
+    st = lib.algo.stats()
+    return model, wall, st, lib.knot_evals
+
+
+class L2Flush:
+    """Writes a buffer larger than the 129 MB L2 between timed steps."""
+
+    def __init__(self):
+        try:
+            import torch
+
+            self.torch = torch
+            self.buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        except Exception:  # noqa: BLE001 - torch is optional plumbing here
+            self.torch = None
+
+    def __call__(self):
+        if self.torch is not None:
+            self.buf.zero_()
+            self.torch.cuda.synchronize()
+
+    @property
+    def ok(self):
+        return self.torch is not None
+
+
+class Clocks:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-f", self.path], stdout=subprocess.DEVNULL,
+                stderr=subprocess.DEVNULL)
+        except Exception:  # noqa: BLE001
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9 or (dev.isdigit() and f[0] != dev):
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for k, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(k)
+        finally:
+            os.unlink(self.path)
+        if not sm:
+            return None
+        top = max(sm)
+        loaded = [s for s in sm if s >= 0.5 * top] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(mx),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], p["bf16_tflops"], "measured"
+    except Exception:  # noqa: BLE001
+        return 6800.0, 1900.0, "fallback"
+
+
+def traffic_for(workload_name, kernel):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            t = json.load(f)
+        return t.get(workload_name, {}).get(kernel)
+    except Exception:  # noqa: BLE001
+        return None
+
+
+def roofline(st, workload_name):
+    hbm, bf16, src = peaks()
+    phases = {"sweep": st["ms_sweep"], "project": st["ms_project"]}
+    dom = max(phases, key=phases.get)
+    if dom == "sweep" and st["ms_sweep"] > 0:
+        ach = st["sweep_bytes"] / (st["ms_sweep"] * 1e-3) / 1e9
+        return {"kernel": "hinge sweep", "bound": "hbm", "achieved": ach, "peak": hbm,
+                "unit": "GB/s", "frac": ach / hbm, "peak_source": src,
+                "traffic": traffic_for(workload_name, "sweep")}
+    ms = max(st["ms_project"], 1e-9)
+    ach = st["project_flops"] / (ms * 1e-3) / 1e12
+    return {"kernel": "projection", "bound": "tensor", "achieved": ach, "peak": bf16,
+            "unit": "TFLOP/s", "frac": ach / bf16, "peak_source": src,
+            "traffic": traffic_for(workload_name, "project")}
+
+
+def cpu_threads():
+    return os.cpu_count() or 1
+
+
+def cpu_fit(X, y, kw, threads):
+    import oracle
+    from mars_gb300.mars import forward_pass
+
+    if not oracle.available("port"):
+        oracle.build(with_reference=False)
+
+    def factory(X_, y_, w_, mt):
+        return oracle.OracleAlgo(X_, y_, w_, mt, kind="port")
+
+    lib = Counting(factory)
+    t0 = time.perf_counter()
+    model = forward_pass(lib, X, y, None, threads=threads, **kw)
+    return model, time.perf_counter() - t0, lib.knot_evals
+
+
+def dist():
+    if WORLD <= 1:
+        return None
+    import torch.distributed as tdist
+
+    tdist.init_process_group("gloo")
+    return tdist
+
+
+def allmax(tdist, v):
+    if tdist is None:
+        return v
+    import torch
+
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(tdist, v):
+    if tdist is None:
+        return v
+    import torch
+
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    tdist.all_reduce(t, op=tdist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def run_reference(args):
+    if RANK != 0:
+        return 0
+    X, y, kw = workload(args.workload)
+    threads = cpu_threads()
+    for _ in range(args.warmup):
+        cpu_fit(X, y, kw, threads)
+    total_k, total_t = 0, 0.0
+    for _ in range(args.steps):
+        _, dt, k = cpu_fit(X, y, kw, threads)
+        total_k += k
+        total_t += dt
+    value = total_k / total_t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "full fit per step, OpenMP over input columns"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    tdist = dist()
+    from mars_gb300 import marslib
+
+    marslib.load()
+    X, y, kw = workload(args.workload)
+    flush = L2Flush()
+
+    for _ in range(max(args.warmup, 0)):
+        flush()
+        gpu_fit(X, y, kw, args.precision)
+
+    clocks = Clocks() if RANK == 0 else None
+    if tdist is not None:
+        tdist.barrier()
+    if clocks:
+        clocks.start()
+    spans, walls, knots, launches, h2d, d2h = [], [], [], [], [], []
+    agg = None
+    model = None
+    for _ in range(args.steps):
+        flush()
+        model, wall, st, k = gpu_fit(X, y, kw, args.precision)
+        spans.append(st["ms_span"] * 1e-3)
+        walls.append(wall)
+        knots.append(k)
+        launches.append(st["kernel_launches"])
+        h2d.append(st["h2d_bytes"])
+        d2h.append(st["d2h_bytes"])
+        if agg is None:
+            agg = dict(st)
+        else:
+            for key in ("ms_project", "ms_sweep", "ms_dgks", "ms_normalize", "ms_append",
+                        "ms_sort", "project_flops", "sweep_bytes"):
+                agg[key] += st[key]
+    if tdist is not None:
+        tdist.barrier()
+    clk = clocks.stop() if clocks else None
+
+    t_dev = allmax(tdist, sum(spans))
+    t_wall = allmax(tdist, sum(walls))
+    k_all = allsum(tdist, sum(knots))
+    line = {
+        "metric": METRIC,
+        "value": k_all / t_dev,
+        "unit": UNIT,
+        "n_gpus": WORLD,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_dev / args.steps,
+        "fit_time_s": t_dev / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+tf32/bf16 with f64 carries",
+        "precision": args.precision,
+        "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload], "l2": "flushed between steps"
+                   if flush.ok else "not flushed (torch unavailable)",
+                   "parallelism": "replicas" if WORLD > 1 else "single GPU"},
+        "e2e": {"value": k_all / t_wall, "unit": UNIT,
+                "h2d_bytes_per_step": int(statistics.mean(h2d)),
+                "d2h_bytes_per_step": int(statistics.mean(d2h)),
+                "fit_time_s": t_wall / args.steps},
+        "gpu_launches": int(sum(launches)),
+        "knot_evals_per_step": int(statistics.mean(knots)),
+        "terms": len(model),
+        "roofline": roofline(agg, args.workload),
+        "phase_ms_per_step": {k[3:]: agg[k] / args.steps for k in
+                              ("ms_project", "ms_dgks", "ms_normalize", "ms_sweep",
+                               "ms_append", "ms_sort")},
+        "clocks": clk,
+    }
+    if args.precision == "mixed" and not args.no_compare:
+        fp_spans, fp_model = [], None
+        for _ in range(max(1, min(args.steps, 2))):
+            flush()
+            fp_model, _, st, _ = gpu_fit(X, y, kw, "fp64")
+            fp_spans.append(st["ms_span"] * 1e-3)
+        line["fp64"] = {"fit_time_s": statistics.mean(fp_spans),
+                        "value": line["knot_evals_per_step"] / statistics.mean(fp_spans),
+                        "speedup": statistics.mean(fp_spans) / (t_dev / args.steps)}
+        line["term_path_identical_to_fp64"] = path_of(model) == path_of(fp_model)
+    golden = os.path.join(ROOT, "tests", "golden", args.workload + ".json")
+    if os.path.isfile(golden):
+        with open(golden) as f:
+            g = json.load(f)
+        want = [(r["type"], r["basis"], r["input"], r["hinge"]) for r in g["model"]]
+        line["term_path_identical_to_reference"] = path_of(model) == want
+    if RANK == 0 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        _, dt, k = cpu_fit(X, y, kw, threads)
+        line["cpu_baseline"] = {"value": k / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "one full fit of the same workload",
+                                "fit_time_s": dt}
+    if RANK == 0:
+        print(json.dumps(line))
+    if tdist is not None:
+        tdist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

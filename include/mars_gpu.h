@@ -63,7 +63,12 @@ typedef struct {
     long long knot_evals;       /* grid cuts scored by the hinge sweep */
     long long dgks_fired;       /* candidate columns re-orthogonalised */
     long long redecided;        /* candidates re-evaluated in FP64 (mixed mode) */
-    long long kernel_launches;  /* kernels launched by this handle */
+    long long kernel_launches;  /* kernels of this library launched by this handle */
+    long long h2d_bytes;        /* host-to-device bytes copied by this handle */
+    long long d2h_bytes;        /* device-to-host bytes copied by this handle */
+    double project_flops;       /* algorithmic projection FLOPs: 4 n m per candidate */
+    double sweep_bytes;         /* algorithmic sweep bytes: n (12 + 4 m + 8 P_x) per input */
+    double ms_span;             /* device time from the first eval to the last call */
     double ms_project;          /* device time per phase, summed (CUDA events) */
     double ms_dgks;
     double ms_normalize;

@@ -103,21 +103,29 @@ struct mars_gpu_algo {
     cudaStream_t st = nullptr;
     PhaseTimer timer;
     double phase_ms[PH_N] = {0};
+    cudaEvent_t span_begin = nullptr, span_end = nullptr;
+    bool span_started = false;
     mars_gpu_stats stats;
 
     // Resident state.
     DevBuf X, s, y, B, Bo, BoC, ybo_d, perm, xsort;
     std::vector<char> sorted;
     // Per-eval scratch (grow-only).
-    DevBuf Bx, T, Tpart, part, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks;
+    DevBuf Bx, T, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks;
     DevBuf sort_keys, sort_vals, sort_tmp;
-    DevBuf ap_v, ap_part, ap_coef, ap_scal;
+    DevBuf ap_v, ap_coef, ap_scal;
 
     ~mars_gpu_algo()
     {
         if (st) {
             cudaStreamSynchronize(st);
             cudaStreamDestroy(st);
+        }
+        if (span_begin) {
+            cudaEventDestroy(span_begin);
+        }
+        if (span_end) {
+            cudaEventDestroy(span_end);
         }
     }
 };
@@ -126,19 +134,32 @@ namespace {
 
 void sync(mars_gpu_algo *a) { CUDA_CHECK(cudaStreamSynchronize(a->st)); }
 
+// The device-time span of a fit: from the start of its first eval to the end
+// of its latest eval or append, on the handle's stream.
+void span_mark_begin(mars_gpu_algo *a)
+{
+    if (!a->span_started) {
+        CUDA_CHECK(cudaEventRecord(a->span_begin, a->st));
+        a->span_started = true;
+    }
+}
+
+void span_mark_end(mars_gpu_algo *a)
+{
+    if (a->span_started) {
+        CUDA_CHECK(cudaEventRecord(a->span_end, a->st));
+    }
+}
+
 AppendScratch append_scratch(mars_gpu_algo *a)
 {
-    const int nb = append_blocks((int)a->n);
     a->ap_v.ensure(sizeof(double) * a->n);
-    a->ap_part.ensure(sizeof(double) * 2 * nb);
     a->ap_coef.ensure(sizeof(double) * (a->max_terms + 1));
     a->ap_scal.ensure(sizeof(double) * 8);
     AppendScratch ws;
     ws.v = a->ap_v.as<double>();
-    ws.part = a->ap_part.as<double>();
     ws.coef = a->ap_coef.as<double>();
     ws.scal = a->ap_scal.as<double>();
-    ws.nblocks = nb;
     return ws;
 }
 
@@ -167,6 +188,8 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     a->tol = ((double)n * 0.02) * DBL_EPSILON;
     std::memset(&a->stats, 0, sizeof(a->stats));
     CUDA_CHECK(cudaStreamCreateWithFlags(&a->st, cudaStreamNonBlocking));
+    CUDA_CHECK(cudaEventCreate(&a->span_begin));
+    CUDA_CHECK(cudaEventCreate(&a->span_end));
     a->timer.st = a->st;
 
     // Weighted, normalised target (marsalgo.cc:278-352), in the reference's
@@ -213,6 +236,7 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     a->yvar = vsum / (double)n;
 
     // Device-resident state.
+    a->stats.h2d_bytes += (long long)(sizeof(float) * (n * p + 3 * n));
     a->X.ensure(sizeof(float) * std::max<size_t>(1, n * p));
     if (n * p) {
         CUDA_CHECK(cudaMemcpy2DAsync(a->X.ptr, n * sizeof(float), X, ldx * sizeof(float),
@@ -239,12 +263,10 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     // Column scales s = 1/rms (marsalgo.cc:359-369).
     a->s.ensure(sizeof(float) * std::max<size_t>(1, p));
     if (p) {
-        const int nb = append_blocks((int)n);
-        DevBuf part, sums;
-        part.ensure(sizeof(double) * nb * p);
+        DevBuf sums;
         sums.ensure(sizeof(double) * p);
         column_sumsq(a->st, a->X.as<float>(), n, (int)n, (int)p, sums.as<double>(),
-                     part.as<double>(), &a->stats.kernel_launches);
+                     &a->stats.kernel_launches);
         std::vector<double> sq(p);
         CUDA_CHECK(cudaMemcpyAsync(sq.data(), sums.ptr, sizeof(double) * p, cudaMemcpyDeviceToHost,
                                    a->st));
@@ -321,12 +343,9 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
     float *Bx = a->Bx.as<float>();
     ProjectScratch ws;
     ws.T = a->T.as<double>();
-    ws.Tpart = a->Tpart.as<double>();
-    ws.part = a->part.as<double>();
-    ws.part_elems = a->part.bytes / sizeof(double);
-    ws.tpart_elems = a->Tpart.bytes / sizeof(double);
     double *s = a->svec.as<double>();
 
+    a->stats.project_flops += 4.0 * (double)n * (double)m * (double)Pc;
     cudaEvent_t t0 = a->timer.begin();
     FillSrc src{a->B.as<float>(), a->n, a->X.as<float>(), a->n, a->s.as<float>(), cx_d, cb_d};
     project_fp64(a->st, src, a->Bo.as<float>(), a->ldbo, n, m, Pc, nullptr, Bx, a->n, s, ws,
@@ -351,20 +370,22 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
 
     t0 = a->timer.begin();
     normalize_ybx(a->st, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), !linear_only,
-                  a->ybx.as<double>(), a->part.as<double>(), &a->stats.kernel_launches);
+                  a->ybx.as<double>(), &a->stats.kernel_launches);
     a->timer.end(PH_NORMALIZE, t0);
 
     if (linear_only) {
         return;
     }
     std::vector<SweepTask> tasks;
+    const int warps = sweep_warps(m);
     for (int b = 0; b < Pc;) {
         int e = b;
         while (e < Pc && cx_h[c0 + e] == cx_h[c0 + b]) {
             ++e;
         }
-        for (int t = b; t < e; t += 8) {
-            tasks.push_back({cx_h[c0 + b], t, std::min(8, e - t)});
+        a->stats.sweep_bytes += (double)tail * (12.0 + 4.0 * m + 8.0 * (e - b));
+        for (int t = b; t < e; t += warps) {
+            tasks.push_back({cx_h[c0 + b], t, std::min(warps, e - t)});
         }
         b = e;
     }
@@ -392,6 +413,7 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
     const int m = (int)a->m, n = (int)a->n;
     verify(mask_stride >= m || rows <= 1, "mask row stride smaller than nbasis");
     a->stats.evals += 1;
+    span_mark_begin(a);
 
     std::vector<int> cx, cb, cols;
     for (int i = 0; i < rows; ++i) {
@@ -432,9 +454,6 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         }
         a->Bx.ensure(sizeof(float) * a->n * maxPc);
         a->T.ensure(sizeof(double) * std::max<size_t>(1, (size_t)m * maxPc));
-        a->Tpart.ensure(sizeof(double) * std::max<size_t>(1, project_tpart_elems(n, m, (int)maxPc)));
-        a->part.ensure(sizeof(double) * std::max(project_part_elems(n, (int)maxPc),
-                                                 normalize_part_elems(n, (int)maxPc)));
         a->svec.ensure(sizeof(double) * maxPc);
         a->snew.ensure(sizeof(double) * maxPc);
         a->ybx.ensure(sizeof(double) * maxPc);
@@ -443,6 +462,7 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         a->fired.ensure(sizeof(int) * maxPc);
         a->nfired.ensure(sizeof(int) * 4);
         a->cand.ensure(sizeof(int) * 2 * (size_t)P);
+        a->stats.h2d_bytes += (long long)(sizeof(int) * 2 * (size_t)P);
         int *cx_all = a->cand.as<int>(), *cb_all = cx_all + P;
         CUDA_CHECK(cudaMemcpyAsync(cx_all, cx.data(), sizeof(int) * P, cudaMemcpyHostToDevice,
                                    a->st));
@@ -462,6 +482,8 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         CUDA_CHECK(cudaMemcpyAsync(hin, o_hin, sizeof(double) * cnt, cudaMemcpyDeviceToHost, a->st));
         CUDA_CHECK(cudaMemcpyAsync(cut, o_cut, sizeof(double) * cnt, cudaMemcpyDeviceToHost, a->st));
     }
+    a->stats.d2h_bytes += (long long)(3 * sizeof(double) * cnt);
+    span_mark_end(a);
     sync(a);
     a->timer.resolve(a->phase_ms);
     if (sse0) {
@@ -523,6 +545,7 @@ double append_impl(mars_gpu_algo *a, char type, int xcol, int bcol, float h)
         }
     }
     a->timer.end(PH_APPEND, t0);
+    span_mark_end(a);
     sync(a);
     a->timer.resolve(a->phase_ms);
     return result;
@@ -655,6 +678,15 @@ int mars_gpu_get_stats(const mars_gpu_algo *a, mars_gpu_stats *out)
     out->ms_sort = a->phase_ms[PH_SORT];
     out->ms_append = a->phase_ms[PH_APPEND];
     out->ms_redecide = a->phase_ms[PH_REDECIDE];
+    out->ms_span = 0.0;
+    if (a->span_started) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, a->span_begin, a->span_end) == cudaSuccess) {
+            out->ms_span = t;
+        } else {
+            cudaGetLastError();
+        }
+    }
     return MARS_GPU_OK;
 }
 
@@ -663,18 +695,17 @@ int mars_gpu_orth_error(mars_gpu_algo *a, double *max_abs, double *rss)
     return guarded([&] {
         verify(a != nullptr, "null handle");
         const int n = (int)a->n, m = (int)a->m;
-        DevBuf T, Tpart;
+        DevBuf T;
         T.ensure(sizeof(double) * (size_t)m * (m + 1));
-        Tpart.ensure(sizeof(double) * std::max<size_t>(1, project_tpart_elems(n, m, m)));
         StoredSrc q{a->BoC.as<float>(), a->n, nullptr};
         tgemm_fp64(a->st, q, a->Bo.as<float>(), a->ldbo, n, m, m, T.as<double>(),
-                   Tpart.as<double>(), Tpart.bytes / sizeof(double), &a->stats.kernel_launches);
+                   &a->stats.kernel_launches);
         std::vector<double> G((size_t)m * m);
         CUDA_CHECK(cudaMemcpyAsync(G.data(), T.ptr, sizeof(double) * m * m,
                                    cudaMemcpyDeviceToHost, a->st));
         StoredSrc yy{a->y.as<float>(), a->n, nullptr};
         tgemm_fp64(a->st, yy, a->Bo.as<float>(), a->ldbo, n, m, 1, T.as<double>(),
-                   Tpart.as<double>(), Tpart.bytes / sizeof(double), &a->stats.kernel_launches);
+                   &a->stats.kernel_launches);
         std::vector<double> r(m);
         CUDA_CHECK(cudaMemcpyAsync(r.data(), T.ptr, sizeof(double) * m, cudaMemcpyDeviceToHost,
                                    a->st));
@@ -715,7 +746,7 @@ int mars_gpu_orthonormalize(size_t n, size_t m, size_t p, const float *B, size_t
         }
         cudaStream_t st;
         CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-        DevBuf dB, dx, dBo, dBx, dT, dTp, dpart, ds, dsn, dybx, dcand, dfired, dnf, dy, dsx;
+        DevBuf dB, dx, dBo, dBx, dT, ds, dsn, dybx, dcand, dfired, dnf, dy, dsx;
         long long launches = 0;
         dB.ensure(sizeof(float) * n * nbcols);
         CUDA_CHECK(cudaMemcpy2DAsync(dB.ptr, n * sizeof(float), B, ldB * sizeof(float),
@@ -735,9 +766,6 @@ int mars_gpu_orthonormalize(size_t n, size_t m, size_t p, const float *B, size_t
                                    cudaMemcpyHostToDevice, st));
         dBx.ensure(sizeof(float) * n * p);
         dT.ensure(sizeof(double) * std::max<size_t>(1, m * p));
-        dTp.ensure(sizeof(double) * std::max<size_t>(1, project_tpart_elems((int)n, (int)m, (int)p)));
-        dpart.ensure(sizeof(double) * std::max(project_part_elems((int)n, (int)p),
-                                               normalize_part_elems((int)n, (int)p)));
         ds.ensure(sizeof(double) * p);
         dsn.ensure(sizeof(double) * p);
         dybx.ensure(sizeof(double) * p);
@@ -745,8 +773,7 @@ int mars_gpu_orthonormalize(size_t n, size_t m, size_t p, const float *B, size_t
         dnf.ensure(sizeof(int));
         dy.ensure(sizeof(float) * n);
         CUDA_CHECK(cudaMemsetAsync(dy.ptr, 0, sizeof(float) * n, st));
-        ProjectScratch ws{dT.as<double>(), dTp.as<double>(), dpart.as<double>(),
-                          dpart.bytes / sizeof(double), dTp.bytes / sizeof(double)};
+        ProjectScratch ws{dT.as<double>()};
         FillSrc src{dB.as<float>(), n, dx.as<float>(), n, dsx.as<float>(), dcand.as<int>(),
                     dcand.as<int>() + p};
         project_fp64(st, src, dBo.as<float>(), ldbo, (int)n, (int)m, (int)p, nullptr,
@@ -765,7 +792,7 @@ int mars_gpu_orthonormalize(size_t n, size_t m, size_t p, const float *B, size_t
         std::vector<double> sh(p);
         CUDA_CHECK(cudaMemcpyAsync(sh.data(), ds.ptr, sizeof(double) * p, cudaMemcpyDeviceToHost, st));
         normalize_ybx(st, dBx.as<float>(), n, (int)n, (int)p, ds.as<double>(), tol, dy.as<float>(),
-                      true, dybx.as<double>(), dpart.as<double>(), &launches);
+                      true, dybx.as<double>(), &launches);
         CUDA_CHECK(cudaMemcpy2DAsync(Bx, ldBx * sizeof(float), dBx.ptr, n * sizeof(float),
                                      n * sizeof(float), p, cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaStreamSynchronize(st));
@@ -793,19 +820,16 @@ int mars_gpu_orthonormalize_col(size_t n, size_t m, double *v, const float *Bo, 
                 colmajor[j * n + i] = Bo[i * ldBo + j];
             }
         }
-        DevBuf dBoC, dv, dpart, dcoef, dscal;
+        DevBuf dBoC, dv, dcoef, dscal;
         long long launches = 0;
-        const int nb = append_blocks((int)n);
         dBoC.ensure(sizeof(float) * colmajor.size());
         CUDA_CHECK(cudaMemcpyAsync(dBoC.ptr, colmajor.data(), sizeof(float) * colmajor.size(),
                                    cudaMemcpyHostToDevice, st));
         dv.ensure(sizeof(double) * n);
         CUDA_CHECK(cudaMemcpyAsync(dv.ptr, v, sizeof(double) * n, cudaMemcpyHostToDevice, st));
-        dpart.ensure(sizeof(double) * 2 * nb);
         dcoef.ensure(sizeof(double) * (m + 1));
         dscal.ensure(sizeof(double) * 8);
-        AppendScratch ws{dv.as<double>(), dpart.as<double>(), dcoef.as<double>(),
-                         dscal.as<double>(), nb};
+        AppendScratch ws{dv.as<double>(), dcoef.as<double>(), dscal.as<double>()};
         double scal[2];
         mgs_pass(st, dBoC.as<float>(), (int)n, (int)m, ws, &launches);
         CUDA_CHECK(cudaMemcpyAsync(scal, ws.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -15,96 +15,76 @@ namespace mgpu {
 namespace {
 
 // ---------------------------------------------------------------------------
-// T = Bo^T Bx, split over rows (K). Block tile: 64 components x 32 columns,
-// 32 rows per stage. Each thread owns one component and 8 columns.
+// T = Bo^T Bx with every entry accumulated over the rows in order
+// i = 0..n-1 by one fused-multiply-add chain, which is the reference's order
+// (kernels.cc:327-335: tc[k] += bo_row[k] * bx[i], rows outermost). The block
+// tile is KT components x (128 / KT) columns, one accumulator per thread; the
+// rows are staged 32 at a time in shared memory.
 // ---------------------------------------------------------------------------
-constexpr int TG_ROWS = 32, TG_COMPS = 64, TG_COLS = 32, TG_THREADS = 256;
+constexpr int TG_ROWS = 32, TG_THREADS = 128;
 
-template <class Src>
+template <class Src, int KT>
 __global__ void __launch_bounds__(TG_THREADS)
     k_tgemm(Src src, const float *__restrict__ Bo, size_t ldbo, int n, int m, int P,
-            int rows_per_split, double *__restrict__ Tpart)
+            double *__restrict__ T)
 {
-    __shared__ float sBo[TG_ROWS][TG_COMPS + 1];
-    __shared__ float sV[TG_ROWS][TG_COLS + 1];
-    const int t = threadIdx.x, cl = t & (TG_COMPS - 1), jg = t / TG_COMPS;
-    const int col0 = blockIdx.x * TG_COLS, split = blockIdx.y, c0 = blockIdx.z * TG_COMPS;
-    const size_t rb = (size_t)split * rows_per_split;
-    const size_t re = min((size_t)n, rb + (size_t)rows_per_split);
-    double acc[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        acc[q] = 0.0;
-    }
-    for (size_t r0 = rb; r0 < re; r0 += TG_ROWS) {
-        for (int e = t; e < TG_ROWS * TG_COMPS; e += TG_THREADS) {
-            const int rr = e / TG_COMPS, cc = e % TG_COMPS;
-            const size_t i = r0 + rr;
-            const int c = c0 + cc;
-            sBo[rr][cc] = (i < re && c < m) ? Bo[i * ldbo + c] : 0.f;
+    constexpr int JT = TG_THREADS / KT;
+    __shared__ float sBo[TG_ROWS][KT + 1];
+    __shared__ float sV[TG_ROWS][JT + 1];
+    const int t = threadIdx.x, kk = t % KT, jj = t / KT;
+    const int k0 = blockIdx.x * KT, j0 = blockIdx.y * JT;
+    double acc = 0.0;
+    for (int r0 = 0; r0 < n; r0 += TG_ROWS) {
+        const int rows = min(TG_ROWS, n - r0);
+        for (int e = t; e < TG_ROWS * KT; e += TG_THREADS) {
+            const int rr = e / KT, cc = e % KT;
+            sBo[rr][cc] = (rr < rows && k0 + cc < m) ? Bo[(size_t)(r0 + rr) * ldbo + k0 + cc] : 0.f;
         }
-        for (int e = t; e < TG_ROWS * TG_COLS; e += TG_THREADS) {
-            const int rr = e % TG_ROWS, jj = e / TG_ROWS;
-            const size_t i = r0 + rr;
-            const int col = col0 + jj;
-            sV[rr][jj] = (i < re && col < P) ? src(i, col) : 0.f;
+        for (int e = t; e < TG_ROWS * JT; e += TG_THREADS) {
+            const int rr = e % TG_ROWS, cj = e / TG_ROWS;
+            sV[rr][cj] = (rr < rows && j0 + cj < P) ? src((size_t)(r0 + rr), j0 + cj) : 0.f;
         }
         __syncthreads();
-#pragma unroll 4
-        for (int rr = 0; rr < TG_ROWS; ++rr) {
-            const double bo = (double)sBo[rr][cl];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                acc[q] = fma(bo, (double)sV[rr][jg * 8 + q], acc[q]);
-            }
+        for (int rr = 0; rr < rows; ++rr) {
+            acc = fma((double)sBo[rr][kk], (double)sV[rr][jj], acc);
         }
         __syncthreads();
     }
-    const int c = c0 + cl;
-    if (c < m) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int col = col0 + jg * 8 + q;
-            if (col < P) {
-                Tpart[((size_t)split * P + col) * m + c] = acc[q];
-            }
-        }
+    if (k0 + kk < m && j0 + jj < P) {
+        T[(size_t)(j0 + jj) * m + k0 + kk] = acc;
     }
 }
 
-__global__ void k_reduce_splits(const double *__restrict__ part, int splits, size_t count,
-                                double *__restrict__ out)
-{
-    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= count) {
-        return;
+// out[j] = fused chain over i = 0..n-1 (in order) of a*b for the pairs the
+// functor yields: the reference's sequential f64 accumulations
+// (kernels.cc:361-366 norm of the stored column; kernels.cc:215-237 dot_widen).
+struct SqChain {  // sum of squares of the stored f32 column Bx[:, col[j]]
+    const float *Bx;
+    size_t ld;
+    const int *col;
+    __device__ __forceinline__ double operator()(size_t i, int j, double acc) const
+    {
+        const double v = (double)Bx[i + (size_t)(col ? col[j] : j) * ld];
+        return fma(v, v, acc);
     }
-    double s = part[idx];
-    for (int sp = 1; sp < splits; ++sp) {
-        s += part[(size_t)sp * count + idx];
-    }
-    out[idx] = s;
-}
-
-// out[j] = sum_b part[b*P + j] in block order.
-__global__ void k_reduce_cols(const double *__restrict__ part, int nb, int P,
-                              double *__restrict__ out)
+};
+template <class Op>
+__global__ void __launch_bounds__(64) k_colchain(Op op, int n, int P, double *__restrict__ out)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= P) {
         return;
     }
-    double s = 0.0;
-    for (int b = 0; b < nb; ++b) {
-        s += part[(size_t)b * P + j];
+    double acc = 0.0;
+    for (int i = 0; i < n; ++i) {
+        acc = op((size_t)i, j, acc);
     }
-    out[j] = s;
+    out[j] = acc;
 }
 
 // ---------------------------------------------------------------------------
-// Bx <- f32(Bx - Bo T) per row and candidate; per-block partial ||Bx||^2.
-// The projection is the reference's sequential fused chain over k
-// (kernels.cc:56-78, 86-118 scalar branches).
+// Bx <- f32(Bx - Bo T), one element per thread; the projection is the
+// reference's fused chain over k from 0 (kernels.cc:56-118 scalar branches).
 // ---------------------------------------------------------------------------
 constexpr int PJ_THREADS = 128, PJ_COLS = 8;
 
@@ -112,10 +92,9 @@ template <class Src>
 __global__ void __launch_bounds__(PJ_THREADS)
     k_project(Src src, const float *__restrict__ Bo, size_t ldbo, int n, int m, int P,
               const double *__restrict__ T, const int *__restrict__ out_col,
-              float *__restrict__ Bx, size_t ldBx, double *__restrict__ part)
+              float *__restrict__ Bx, size_t ldBx)
 {
     extern __shared__ double sT[];  // PJ_COLS * m
-    __shared__ double red[32];
     const int t = threadIdx.x, j0 = blockIdx.y * PJ_COLS;
     for (int e = t; e < PJ_COLS * m; e += PJ_THREADS) {
         const int q = e / m, k = e % m, j = j0 + q;
@@ -123,29 +102,23 @@ __global__ void __launch_bounds__(PJ_THREADS)
     }
     __syncthreads();
     const size_t i = (size_t)blockIdx.x * PJ_THREADS + t;
-    const float *bo = Bo + (i < (size_t)n ? i : 0) * ldbo;
+    if (i >= (size_t)n) {
+        return;
+    }
+    const float *bo = Bo + i * ldbo;
     for (int q = 0; q < PJ_COLS; ++q) {
         const int j = j0 + q;
         if (j >= P) {
-            break;  // uniform over the block
+            break;
         }
-        double sq = 0.0;
-        if (i < (size_t)n) {
-            double proj = 0.0;
-            const double *tj = sT + q * m;
-            for (int k = 0; k < m; ++k) {
-                proj = fma((double)bo[k], tj[k], proj);
-            }
-            const double v = (double)src(i, j) - proj;
-            const float vf = (float)v;
-            const int oc = out_col ? out_col[j] : j;
-            Bx[i + (size_t)oc * ldBx] = vf;
-            sq = (double)vf * (double)vf;
+        double proj = 0.0;
+        const double *tj = sT + q * m;
+        for (int k = 0; k < m; ++k) {
+            proj = fma((double)bo[k], tj[k], proj);
         }
-        const double bs = block_sum<PJ_THREADS>(sq, red);
-        if (t == 0) {
-            part[(size_t)blockIdx.x * P + j] = bs;
-        }
+        const double v = (double)src(i, j) - proj;
+        const int oc = out_col ? out_col[j] : j;
+        Bx[i + (size_t)oc * ldBx] = (float)v;
     }
 }
 
@@ -178,54 +151,69 @@ __global__ void k_scatter_s(const int *__restrict__ fired, int nf, const double 
     }
 }
 
+__device__ __forceinline__ float norm_scale(double s, double tol)
+{
+    return (s > tol) ? (float)(1.0 / sqrt(s + tol)) : 0.0f;
+}
+
+// ybx[j] = fused chain over i of f32(Bx[i,j] * scale_j) * y[i] (dot_widen of the
+// normalised column, kernels.cc:215-237 after kernels.cc:401-416).
+struct NormDotChain {
+    const float *Bx;
+    size_t ld;
+    const float *y;
+    const double *s;
+    double tol;
+    __device__ __forceinline__ double operator()(size_t i, int j, double acc) const
+    {
+        const float v = Bx[i + (size_t)j * ld] * norm_scale(s[j], tol);
+        return fma((double)v, (double)y[i], acc);
+    }
+};
+
 constexpr int NM_THREADS = 256, NM_COLS = 8;
 
 __global__ void __launch_bounds__(NM_THREADS)
-    k_normalize(float *__restrict__ Bx, size_t ldBx, int n, int P, const double *__restrict__ s,
-                double tol, const float *__restrict__ y, bool store, double *__restrict__ part)
+    k_scale(float *__restrict__ Bx, size_t ldBx, int n, int P, const double *__restrict__ s,
+            double tol)
 {
     __shared__ float sc[NM_COLS];
-    __shared__ double red[32];
     const int t = threadIdx.x, j0 = blockIdx.y * NM_COLS;
     if (t < NM_COLS) {
         const int j = j0 + t;
-        const double sj = j < P ? s[j] : 0.0;
-        sc[t] = (sj > tol) ? (float)(1.0 / sqrt(sj + tol)) : 0.0f;
+        sc[t] = j < P ? norm_scale(s[j], tol) : 0.0f;
     }
     __syncthreads();
     const size_t i = (size_t)blockIdx.x * NM_THREADS + t;
-    const float yi = i < (size_t)n ? y[i] : 0.f;
-    for (int q = 0; q < NM_COLS; ++q) {
-        const int j = j0 + q;
-        if (j >= P) {
-            break;
-        }
-        double prod = 0.0;
-        if (i < (size_t)n) {
-            const float v = Bx[i + (size_t)j * ldBx] * sc[q];
-            if (store) {
-                Bx[i + (size_t)j * ldBx] = v;
-            }
-            prod = (double)v * (double)yi;
-        }
-        const double bs = block_sum<NM_THREADS>(prod, red);
-        if (t == 0) {
-            part[(size_t)blockIdx.x * P + j] = bs;
-        }
+    if (i >= (size_t)n) {
+        return;
+    }
+    for (int q = 0; q < NM_COLS && j0 + q < P; ++q) {
+        Bx[i + (size_t)(j0 + q) * ldBx] *= sc[q];
     }
 }
 
 // ---------------------------------------------------------------------------
 // FP64 hinge sweep (marsalgo.cc:576-649 with covariates_impl :91-151).
-// One warp per candidate; lanes own components c = lane + 32 q of f and g
-// (component m is the candidate column Bx itself). The sorted rows are staged
-// 32 at a time: permutation, deltas, y, the gathered Bo rows (shared by all
-// candidates of the block's input column), and per warp B and Bx.
+// One warp per candidate; lane l owns components c = l + 32 q of f and g
+// (component m is the candidate column Bx itself). Sorted rows are staged 32
+// at a time: permutation, deltas, y and the gathered Bo rows (shared by all
+// candidates of the block's input column), and per warp B and Bx. At a grid
+// row the warp saves f into a snapshot slot; once SNAP slots are full each
+// lane scores one of them with the reference's sequential fused chains
+// ff = sum_c f_c^2, fy = sum_c f_c y_c (c = 0..m), so the scores match the
+// reference bit for bit while the chains run side by side.
 // ---------------------------------------------------------------------------
-constexpr int SW_ROWS = 32, SW_WARPS = 8, SW_THREADS = SW_WARPS * 32;
+constexpr int SW_ROWS = 32, SW_SNAP = 16;
+
+struct SweepWarp {
+    double k01[SW_SNAP];
+    double w[SW_SNAP];
+    int row[SW_SNAP];
+};
 
 template <int CPL>
-__global__ void __launch_bounds__(SW_THREADS)
+__global__ void __launch_bounds__(256)
     k_sweep(const SweepTask *__restrict__ tasks, const int *__restrict__ perm,
             const float *__restrict__ xsort, const float *__restrict__ y,
             const float *__restrict__ B, size_t ldB, const int *__restrict__ cand_b,
@@ -234,11 +222,18 @@ __global__ void __launch_bounds__(SW_THREADS)
             int m, int head, int tail, int min_span, double tol, double *__restrict__ hsse,
             int *__restrict__ hrow)
 {
-    extern __shared__ float sBo[];  // SW_ROWS * ldS
+    extern __shared__ double dyn[];
+    const int nwarps = blockDim.x >> 5;
+    const int ldF = m + 1;
+    double *snap_all = dyn;                                  // nwarps * SW_SNAP * ldF
+    double *sY = snap_all + (size_t)nwarps * SW_SNAP * ldF;  // m (ybo)
+    float *sBo = (float *)(sY + m + 1);                      // SW_ROWS * ldS
+    const int ldS = m | 1;
     __shared__ int sk[SW_ROWS];
     __shared__ float sd[SW_ROWS], sy[SW_ROWS];
-    __shared__ float sb[SW_WARPS][SW_ROWS], sbx[SW_WARPS][SW_ROWS];
-    const int ldS = m | 1;
+    __shared__ float sb[8][SW_ROWS], sbx[8][SW_ROWS];
+    __shared__ SweepWarp meta[8];
+
     const SweepTask task = tasks[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool active = warp < task.count;
@@ -247,19 +242,60 @@ __global__ void __launch_bounds__(SW_THREADS)
     const float *xs = xsort + (size_t)task.xcol * n;
     const float *bcol = B + (size_t)cand_b[cand] * ldB;
     const float *bxcol = Bx + (size_t)cand * ldBx;
+    double *snap = snap_all + (size_t)warp * SW_SNAP * ldF;
+    SweepWarp &mw = meta[warp];
+    const double ybx_c = ybx[cand];
 
-    double f[CPL], g[CPL], yc[CPL];
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+        sY[c] = ybo[c];
+    }
+    double f[CPL], g[CPL];
 #pragma unroll
     for (int q = 0; q < CPL; ++q) {
-        const int c = lane + 32 * q;
         f[q] = 0.0;
         g[q] = 0.0;
-        yc[q] = c < m ? ybo[c] : (c == m ? ybx[cand] : 0.0);
     }
     double k0 = 0, k1 = 0, w = 0, bd = 0, vb = 0, b2 = 0;
     double best = 0.0;
-    int besti = -1;
+    int besti = -1, nsnap = 0;
     long next_grid = (long)head + 1;
+
+    // Score the saved grid rows: lane l takes slot l (in row order).
+    auto flush = [&]() {
+        __syncwarp();
+        double sse = -1.0;
+        int row = 0x7fffffff;
+        if (lane < nsnap) {
+            const double *fs = snap + (size_t)lane * ldF;
+            double ff = 0.0, fy = 0.0;
+            for (int c = 0; c < m; ++c) {
+                ff = fma(fs[c], fs[c], ff);
+                fy = fma(fs[c], sY[c], fy);
+            }
+            ff = fma(fs[m], fs[m], ff);
+            fy = fma(fs[m], ybx_c, fy);
+            const double uw = fy - mw.w[lane];
+            const double den = mw.k01[lane] - ff;
+            sse = den > tol ? (uw * uw) / (den + tol) : 0.0;
+            row = mw.row[lane];
+        }
+        // first maximum in row order (the reference's strict '>' scan)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double s2 = __shfl_xor_sync(0xffffffffu, sse, o);
+            const int r2 = __shfl_xor_sync(0xffffffffu, row, o);
+            if (s2 > sse || (s2 == sse && r2 < row)) {
+                sse = s2;
+                row = r2;
+            }
+        }
+        if (sse > best) {
+            best = sse;
+            besti = row;
+        }
+        nsnap = 0;
+        __syncwarp();
+    };
 
     for (int i0 = 0; i0 < tail; i0 += SW_ROWS) {
         const int rows = min(SW_ROWS, tail - i0);
@@ -271,7 +307,7 @@ __global__ void __launch_bounds__(SW_THREADS)
             sd[r] = i > 0 ? xs[i - 1] - xs[i] : 0.f;
         }
         __syncthreads();
-        for (int e = threadIdx.x; e < rows * m; e += SW_THREADS) {
+        for (int e = threadIdx.x; e < rows * m; e += blockDim.x) {
             const int r = e / m, c = e % m;
             sBo[r * ldS + c] = Bo[(size_t)sk[r] * ldbo + c];
         }
@@ -284,13 +320,13 @@ __global__ void __launch_bounds__(SW_THREADS)
             for (int r = 0; r < rows; ++r) {
                 const int i = i0 + r;
                 const double bk = sb[warp][r], bxk = sbx[warp][r], yk = sy[r];
-                const float *row = sBo + r * ldS;
+                const float *rowp = sBo + r * ldS;
                 if (i == 0) {
-                    // covariates_impl<false>(.., k0 = 0, k1 = b_k): g = b_k * row.
+                    // covariates_impl<false>(.., k0 = 0, k1 = b_k): g = b_k * row
 #pragma unroll
                     for (int q = 0; q < CPL; ++q) {
                         const int c = lane + 32 * q;
-                        const double xv = c < m ? (double)row[c] : (c == m ? bxk : 0.0);
+                        const double xv = c < m ? (double)rowp[c] : (c == m ? bxk : 0.0);
                         f[q] = fma(0.0, g[q], f[q]);
                         g[q] = fma(bk, xv, g[q]);
                     }
@@ -303,17 +339,12 @@ __global__ void __launch_bounds__(SW_THREADS)
                 if (on_grid) {
                     next_grid += min_span;
                 }
-                double pf = 0.0, py = 0.0;
 #pragma unroll
                 for (int q = 0; q < CPL; ++q) {
                     const int c = lane + 32 * q;
-                    const double xv = c < m ? (double)row[c] : (c == m ? bxk : 0.0);
+                    const double xv = c < m ? (double)rowp[c] : (c == m ? bxk : 0.0);
                     f[q] = fma(di, g[q], f[q]);
                     g[q] = fma(bk, xv, g[q]);
-                    if (on_grid) {
-                        pf = fma(f[q], f[q], pf);
-                        py = fma(f[q], yc[q], py);
-                    }
                 }
                 k0 = fma(di * di, b2, k0);
                 k1 = fma(di * 2, bd, k1);
@@ -322,23 +353,36 @@ __global__ void __launch_bounds__(SW_THREADS)
                 b2 = fma(bk, bk, b2);
                 vb = fma(yk, bk, vb);
                 if (on_grid) {
-                    const double ff = warp_sum(pf);
-                    const double fy = warp_sum(py);
-                    const double uw = fy - w;
-                    const double den = (k0 + k1) - ff;
-                    const double sse = den > tol ? (uw * uw) / (den + tol) : 0.0;
-                    if (sse > best) {
-                        best = sse;
-                        besti = i;
+                    double *fs = snap + (size_t)nsnap * ldF;
+#pragma unroll
+                    for (int q = 0; q < CPL; ++q) {
+                        const int c = lane + 32 * q;
+                        if (c <= m) {
+                            fs[c] = f[q];
+                        }
+                    }
+                    if (lane == 0) {
+                        mw.k01[nsnap] = k0 + k1;
+                        mw.w[nsnap] = w;
+                        mw.row[nsnap] = i;
+                    }
+                    ++nsnap;
+                    if (nsnap == SW_SNAP) {
+                        flush();
                     }
                 }
             }
         }
         __syncthreads();
     }
-    if (active && lane == 0) {
-        hsse[cand] = best;
-        hrow[cand] = besti >= 0 ? pk[besti] : -1;
+    if (active) {
+        if (nsnap > 0) {
+            flush();
+        }
+        if (lane == 0) {
+            hsse[cand] = best;
+            hrow[cand] = besti >= 0 ? pk[besti] : -1;
+        }
     }
 }
 
@@ -397,33 +441,151 @@ __global__ void k_assemble(int P, const int *__restrict__ cx, const int *__restr
 // ---------------------------------------------------------------------------
 constexpr int AP_THREADS = 256;
 
-__device__ __forceinline__ void block_rows(int n, int nb, int b, int &lo, int &hi)
+
+// ---------------------------------------------------------------------------
+// Serial chains of the append, in the reference's row order
+// (kernels.cc:194-281, marsalgo.cc:829-861). One block: thread 0 runs the
+// fused-multiply-add chain out of shared memory while the other threads stage
+// the next chunk of rows and write the previous chunk's updated v back.
+// ---------------------------------------------------------------------------
+constexpr int SER_THREADS = 256, SER_CH = 1024;
+
+// Modified Gram-Schmidt pass j = 0..m: v <- v - c_{j-1} Bo[:, j-1] (fused),
+// then c_j = sum_i Bo[i,j] v[i] (j < m) or ||v||^2 (j == m), rows in order.
+// Leaves c_j in coef, sum_j c_j^2 in scal[0] and ||v||^2 in scal[1].
+__global__ void __launch_bounds__(SER_THREADS)
+    k_mgs_serial(const float *__restrict__ BoC, int n, int m, double *__restrict__ v,
+                 double *__restrict__ coef, double *__restrict__ scal)
 {
-    const int per = (n + nb - 1) / nb;
-    lo = min(n, b * per);
-    hi = min(n, lo + per);
+    __shared__ double sv[2][SER_CH];
+    __shared__ float sp[2][SER_CH], sc[2][SER_CH];
+    __shared__ double s_coef;
+    const int t = threadIdx.x;
+    const int nch = (n + SER_CH - 1) / SER_CH;
+    double proj = 0.0;
+    for (int j = 0; j <= m; ++j) {
+        const float *prev = BoC + (size_t)(j > 0 ? j - 1 : 0) * n;
+        const float *cur = BoC + (size_t)(j < m ? j : 0) * n;
+        const double cprev = (j > 0) ? s_coef : 0.0;
+        auto load = [&](int ch, int b) {
+            const int base = ch * SER_CH, cnt = min(SER_CH, n - base);
+            for (int e = t - 1; e < cnt; e += SER_THREADS - 1) {
+                sv[b][e] = v[base + e];
+                sp[b][e] = prev[base + e];
+                sc[b][e] = cur[base + e];
+            }
+        };
+        auto store = [&](int ch, int b) {
+            const int base = ch * SER_CH, cnt = min(SER_CH, n - base);
+            for (int e = t - 1; e < cnt; e += SER_THREADS - 1) {
+                v[base + e] = sv[b][e];
+            }
+        };
+        if (t > 0) {
+            load(0, 0);
+        }
+        __syncthreads();
+        double acc = 0.0;
+        for (int ch = 0; ch < nch; ++ch) {
+            const int b = ch & 1;
+            if (t == 0) {
+                const int cnt = min(SER_CH, n - ch * SER_CH);
+                for (int e = 0; e < cnt; ++e) {
+                    double vi = sv[b][e];
+                    if (j > 0) {
+                        vi = fma(-cprev, (double)sp[b][e], vi);
+                        sv[b][e] = vi;
+                    }
+                    acc = (j < m) ? fma((double)sc[b][e], vi, acc) : fma(vi, vi, acc);
+                }
+            } else {
+                if (ch > 0 && j > 0) {
+                    store(ch - 1, b ^ 1);
+                }
+                if (ch + 1 < nch) {
+                    load(ch + 1, b ^ 1);
+                }
+            }
+            __syncthreads();
+        }
+        if (t > 0 && j > 0) {
+            store(nch - 1, (nch - 1) & 1);
+        }
+        if (t == 0) {
+            if (j < m) {
+                coef[j] = acc;
+                s_coef = acc;
+                proj = fma(acc, acc, proj);
+            } else {
+                scal[0] = proj;
+                scal[1] = acc;
+            }
+        }
+        __syncthreads();
+    }
 }
 
-__device__ __forceinline__ double sum_parts(const double *part, int nb)
-{
-    double s = 0.0;
-    for (int b = 0; b < nb; ++b) {
-        s += part[b];
+// out = sum_i a_i b_i as one fused chain over the rows in order.
+struct VSq {  // (v, v)
+    const double *v;
+    __device__ __forceinline__ void operator()(int i, double &a, double &b) const
+    {
+        a = v[i];
+        b = v[i];
     }
-    return s;
+};
+struct ColDotY {  // ((double)Q[i], (double)y[i])
+    const float *q;
+    const float *y;
+    __device__ __forceinline__ void operator()(int i, double &a, double &b) const
+    {
+        a = (double)q[i];
+        b = (double)y[i];
+    }
+};
+
+template <class Op>
+__global__ void __launch_bounds__(SER_THREADS)
+    k_serial_dot(Op op, int n, double *__restrict__ out)
+{
+    __shared__ double sa[2][SER_CH], sb[2][SER_CH];
+    const int t = threadIdx.x;
+    const int nch = (n + SER_CH - 1) / SER_CH;
+    auto load = [&](int ch, int b) {
+        const int base = ch * SER_CH, cnt = min(SER_CH, n - base);
+        for (int e = t - 1; e < cnt; e += SER_THREADS - 1) {
+            op(base + e, sa[b][e], sb[b][e]);
+        }
+    };
+    if (t > 0) {
+        load(0, 0);
+    }
+    __syncthreads();
+    double acc = 0.0;
+    for (int ch = 0; ch < nch; ++ch) {
+        const int b = ch & 1;
+        if (t == 0) {
+            const int cnt = min(SER_CH, n - ch * SER_CH);
+            for (int e = 0; e < cnt; ++e) {
+                acc = fma(sa[b][e], sb[b][e], acc);
+            }
+        } else if (ch + 1 < nch) {
+            load(ch + 1, b ^ 1);
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        *out = acc;
+    }
 }
 
 __global__ void __launch_bounds__(AP_THREADS)
     k_append_fill(char type, const float *__restrict__ X, size_t ldX, const float *__restrict__ s,
                   int xcol, float *__restrict__ B, size_t ldB, int bcol, int m, float h, int n,
-                  double *__restrict__ v, double *__restrict__ part)
+                  double *__restrict__ v)
 {
-    __shared__ double red[32];
-    int lo, hi;
-    block_rows(n, gridDim.x, blockIdx.x, lo, hi);
     const float sx = s[xcol];
-    double acc = 0.0;
-    for (int i = lo + threadIdx.x; i < hi; i += AP_THREADS) {
+    for (int i = blockIdx.x * AP_THREADS + threadIdx.x; i < n; i += gridDim.x * AP_THREADS) {
         const float xp = X[(size_t)i + (size_t)xcol * ldX];
         const float bp = B[(size_t)i + (size_t)bcol * ldB];
         float val;
@@ -434,185 +596,85 @@ __global__ void __launch_bounds__(AP_THREADS)
             val = sx * bp * ((t < 0.0f) ? 0.0f : t);  // std::max(t, 0.0f)
         }
         B[(size_t)i + (size_t)m * ldB] = val;
-        const double vd = (double)val;
-        v[i] = vd;
-        acc = fma(vd, vd, acc);
-    }
-    const double bs = block_sum<AP_THREADS>(acc, red);
-    if (threadIdx.x == 0) {
-        part[blockIdx.x] = bs;
+        v[i] = (double)val;
     }
 }
 
+// B[:, m] /= f32(sqrt(raw2)) (marsalgo.cc:829-836).
 __global__ void __launch_bounds__(AP_THREADS)
-    k_append_scale(float *__restrict__ B, size_t ldB, int m, int n, const double *__restrict__ part,
-                   int nb)
+    k_append_scale(float *__restrict__ B, size_t ldB, int m, int n, const double *__restrict__ raw2)
 {
-    int lo, hi;
-    block_rows(n, gridDim.x, blockIdx.x, lo, hi);
-    const float raw = (float)sqrt(sum_parts(part, nb));
-    for (int i = lo + threadIdx.x; i < hi; i += AP_THREADS) {
+    const float raw = (float)sqrt(*raw2);
+    for (int i = blockIdx.x * AP_THREADS + threadIdx.x; i < n; i += gridDim.x * AP_THREADS) {
         B[(size_t)i + (size_t)m * ldB] /= raw;
     }
 }
 
-// Step j of modified Gram-Schmidt: apply coefficient j-1 (reduced from the
-// previous step's partials), then the partial dot of column j with v
-// (or of v with itself when j == m).
-__global__ void __launch_bounds__(AP_THREADS)
-    k_mgs_step(const float *__restrict__ BoC, int n, int m, int j, double *__restrict__ v,
-               double *__restrict__ part, int nb, double *__restrict__ coef)
-{
-    __shared__ double red[32];
-    int lo, hi;
-    block_rows(n, gridDim.x, blockIdx.x, lo, hi);
-    double c = 0.0;
-    if (j > 0) {
-        c = sum_parts(part + ((j - 1) & 1) * nb, nb);
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            coef[j - 1] = c;
-        }
-    }
-    const float *prev = BoC + (size_t)(j > 0 ? j - 1 : 0) * n;
-    const float *cur = BoC + (size_t)(j < m ? j : 0) * n;
-    double acc = 0.0;
-    for (int i = lo + threadIdx.x; i < hi; i += AP_THREADS) {
-        double vi = v[i];
-        if (j > 0) {
-            vi = fma(-c, (double)prev[i], vi);
-            v[i] = vi;
-        }
-        if (j < m) {
-            acc = fma((double)cur[i], vi, acc);
-        } else {
-            acc = fma(vi, vi, acc);
-        }
-    }
-    const double bs = block_sum<AP_THREADS>(acc, red);
-    if (threadIdx.x == 0) {
-        part[(j & 1) * nb + blockIdx.x] = bs;
-    }
-}
-
-// scal[0] = sum_j c_j^2 (sequential fused chain), scal[1] = ||v||^2.
-__global__ void k_mgs_finish(const double *__restrict__ part, int nb, int m,
-                             const double *__restrict__ coef, double *__restrict__ scal)
-{
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double pn = 0.0;
-        for (int j = 0; j < m; ++j) {
-            pn = fma(coef[j], coef[j], pn);
-        }
-        scal[0] = pn;
-        scal[1] = sum_parts(part + (m & 1) * nb, nb);
-    }
-}
-
+// v /= w; column m of Bo (row-major) and BoC = f32(v) (kernels.cc:274-279,
+// marsalgo.cc:846-850).
 __global__ void __launch_bounds__(AP_THREADS)
     k_append_store(double w, double *__restrict__ v, float *__restrict__ Bo, size_t ldbo,
-                   float *__restrict__ BoC, int n, int m, const float *__restrict__ y,
-                   double *__restrict__ part)
+                   float *__restrict__ BoC, int n, int m)
 {
-    __shared__ double red[32];
-    int lo, hi;
-    block_rows(n, gridDim.x, blockIdx.x, lo, hi);
-    double acc = 0.0;
-    for (int i = lo + threadIdx.x; i < hi; i += AP_THREADS) {
+    for (int i = blockIdx.x * AP_THREADS + threadIdx.x; i < n; i += gridDim.x * AP_THREADS) {
         const double vi = v[i] / w;
         v[i] = vi;
         const float vf = (float)vi;
         Bo[(size_t)i * ldbo + m] = vf;
         BoC[(size_t)m * n + i] = vf;
-        acc = fma((double)vf, (double)y[i], acc);
-    }
-    const double bs = block_sum<AP_THREADS>(acc, red);
-    if (threadIdx.x == 0) {
-        part[blockIdx.x] = bs;
     }
 }
 
-__global__ void k_sum_into(const double *__restrict__ part, int nb, double *__restrict__ out)
-{
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        *out = sum_parts(part, nb);
-    }
-}
-
-constexpr int CS_THREADS = 256;
-__global__ void __launch_bounds__(CS_THREADS)
-    k_colsumsq(const float *__restrict__ X, size_t ldX, int n, int p, double *__restrict__ part)
-{
-    __shared__ double red[32];
-    const int j = blockIdx.y;
-    int lo, hi;
-    block_rows(n, gridDim.x, blockIdx.x, lo, hi);
-    double acc = 0.0;
-    for (int i = lo + threadIdx.x; i < hi; i += CS_THREADS) {
-        const double x = (double)X[(size_t)i + (size_t)j * ldX];
-        acc = fma(x, x, acc);
-    }
-    const double bs = block_sum<CS_THREADS>(acc, red);
-    if (threadIdx.x == 0) {
-        part[(size_t)blockIdx.x * p + j] = bs;
-    }
-}
-
-int tgemm_splits(int n, int col_tiles, int comp_tiles, int *rows_per_split)
-{
-    const int target = 152 * 4;
-    int splits = (int)ceil_div((size_t)target, (size_t)col_tiles * comp_tiles);
-    const int max_splits = (int)ceil_div((size_t)n, 256);
-    splits = std::max(1, std::min(splits, max_splits));
-    *rows_per_split = (int)round_up(ceil_div((size_t)n, (size_t)splits), TG_ROWS);
-    splits = (int)ceil_div((size_t)n, (size_t)*rows_per_split);
-    return std::max(splits, 1);
-}
 
 }  // namespace
 
 int append_blocks(int n) { return (int)std::max<size_t>(1, std::min<size_t>(608, ceil_div(n, 2048))); }
 
-// Largest split-K workspace any column count in [1, P] needs (fewer columns
-// mean more splits, so the maximum is not always at P itself).
-size_t project_tpart_elems(int n, int m, int P)
-{
-    size_t best = 0;
-    const int comp_tiles = (int)ceil_div(std::max(m, 1), TG_COMPS);
-    for (int ct = 1; ct <= (int)ceil_div(std::max(P, 1), TG_COLS); ++ct) {
-        const int cols = std::min(ct * TG_COLS, std::max(P, 1));
-        int rps;
-        const int splits = tgemm_splits(n, ct, comp_tiles, &rps);
-        best = std::max(best, (size_t)splits * cols * std::max(m, 1));
-    }
-    return best;
-}
-
-size_t project_part_elems(int n, int P) { return ceil_div(n, PJ_THREADS) * (size_t)P; }
-
 template <class Src>
 void tgemm_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, int n, int m,
-                int P, double *T, double *Tpart, size_t tpart_elems, long long *launches)
+                int P, double *T, long long *launches)
 {
     if (P <= 0 || m <= 0) {
         return;
     }
-    int rps;
-    const int col_tiles = (int)ceil_div(P, TG_COLS), comp_tiles = (int)ceil_div(m, TG_COMPS);
-    const int splits = tgemm_splits(n, col_tiles, comp_tiles, &rps);
-    verify((size_t)splits * P * m <= tpart_elems, "internal: T workspace too small", 2);
-    k_tgemm<Src><<<dim3(col_tiles, splits, comp_tiles), TG_THREADS, 0, st>>>(src, Bo, ldbo, n, m,
-                                                                           P, rps, Tpart);
+    int kt = 1;
+    while (kt < m && kt < 32) {
+        kt *= 2;
+    }
+    const unsigned gx = (unsigned)ceil_div(m, kt), gy = (unsigned)ceil_div(P, TG_THREADS / kt);
+    verify(gy <= 65535, "too many candidate columns for one launch", 2);
+#define TG_CASE(K)                                                                    \
+    case K:                                                                           \
+        k_tgemm<Src, K><<<dim3(gx, gy), TG_THREADS, 0, st>>>(src, Bo, ldbo, n, m, P, T); \
+        break;
+    switch (kt) {
+        TG_CASE(1)
+        TG_CASE(2)
+        TG_CASE(4)
+        TG_CASE(8)
+        TG_CASE(16)
+        TG_CASE(32)
+    }
+#undef TG_CASE
     LAUNCH_CHECK();
-    const size_t cnt = (size_t)P * m;
-    k_reduce_splits<<<(unsigned)ceil_div(cnt, 256), 256, 0, st>>>(Tpart, splits, cnt, T);
-    LAUNCH_CHECK();
-    *launches += 2;
+    *launches += 1;
 }
 
 template void tgemm_fp64<FillSrc>(cudaStream_t, const FillSrc &, const float *, size_t, int, int,
-                                  int, double *, double *, size_t, long long *);
+                                  int, double *, long long *);
 template void tgemm_fp64<StoredSrc>(cudaStream_t, const StoredSrc &, const float *, size_t, int,
-                                    int, int, double *, double *, size_t, long long *);
+                                    int, int, double *, long long *);
+
+template <class Op>
+void colchain(cudaStream_t st, const Op &op, int n, int P, double *out, long long *launches)
+{
+    if (P <= 0) {
+        return;
+    }
+    k_colchain<Op><<<(unsigned)ceil_div(P, 64), 64, 0, st>>>(op, n, P, out);
+    LAUNCH_CHECK();
+    *launches += 1;
+}
 
 template <class Src>
 void project_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, int n, int m,
@@ -622,20 +684,19 @@ void project_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo,
     if (P <= 0) {
         return;
     }
-    tgemm_fp64(st, src, Bo, ldbo, n, m, P, ws.T, ws.Tpart, ws.tpart_elems, launches);
+    tgemm_fp64(st, src, Bo, ldbo, n, m, P, ws.T, launches);
     const int rb = (int)ceil_div(n, PJ_THREADS);
-    verify((size_t)rb * P <= ws.part_elems, "internal: partial workspace too small", 2);
     const size_t smem = sizeof(double) * PJ_COLS * std::max(m, 1);
     if (smem > 48 * 1024) {
         CUDA_CHECK(cudaFuncSetAttribute(k_project<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
     }
+    verify(ceil_div(P, PJ_COLS) <= 65535, "too many candidate columns for one launch", 2);
     k_project<Src><<<dim3(rb, (unsigned)ceil_div(P, PJ_COLS)), PJ_THREADS, smem, st>>>(
-        src, Bo, ldbo, n, m, P, ws.T, out_col, Bx, ldBx, ws.part);
+        src, Bo, ldbo, n, m, P, ws.T, out_col, Bx, ldBx);
     LAUNCH_CHECK();
-    k_reduce_cols<<<(unsigned)ceil_div(P, 128), 128, 0, st>>>(ws.part, rb, P, s_out);
-    LAUNCH_CHECK();
-    *launches += 2;
+    *launches += 1;
+    colchain(st, SqChain{Bx, ldBx, out_col}, n, P, s_out, launches);
 }
 
 template void project_fp64<FillSrc>(cudaStream_t, const FillSrc &, const float *, size_t, int,
@@ -663,19 +724,33 @@ void scatter_s(cudaStream_t st, const int *fired, int nf, const double *snew, do
 }
 
 void normalize_ybx(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const double *s,
-                   double tol, const float *y, bool store, double *ybx, double *part,
-                   long long *launches)
+                   double tol, const float *y, bool store, double *ybx, long long *launches)
 {
-    const int rb = (int)ceil_div(n, NM_THREADS);
-    k_normalize<<<dim3(rb, (unsigned)ceil_div(P, NM_COLS)), NM_THREADS, 0, st>>>(
-        Bx, ldBx, n, P, s, tol, y, store, part);
-    LAUNCH_CHECK();
-    k_reduce_cols<<<(unsigned)ceil_div(P, 128), 128, 0, st>>>(part, rb, P, ybx);
-    LAUNCH_CHECK();
-    *launches += 2;
+    if (P <= 0) {
+        return;
+    }
+    colchain(st, NormDotChain{Bx, ldBx, y, s, tol}, n, P, ybx, launches);
+    if (store) {
+        verify(ceil_div(P, NM_COLS) <= 65535, "too many candidate columns for one launch", 2);
+        k_scale<<<dim3((unsigned)ceil_div(n, NM_THREADS), (unsigned)ceil_div(P, NM_COLS)),
+                  NM_THREADS, 0, st>>>(Bx, ldBx, n, P, s, tol);
+        LAUNCH_CHECK();
+        *launches += 1;
+    }
 }
 
-size_t normalize_part_elems(int n, int P) { return ceil_div(n, NM_THREADS) * (size_t)P; }
+// Warps per sweep block: the snapshot buffers take SW_SNAP * (m+1) doubles
+// per warp; keep the block's shared memory near 200 KB.
+int sweep_warps(int m)
+{
+    const size_t per_warp = sizeof(double) * SW_SNAP * (size_t)(m + 1);
+    const size_t fixed = sizeof(double) * (m + 1) + sizeof(float) * SW_ROWS * (size_t)(m | 1);
+    int w = 8;
+    while (w > 1 && fixed + per_warp * w > 200 * 1024) {
+        --w;
+    }
+    return w;
+}
 
 void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *perm,
                 const float *xsort, const float *y, const float *B, size_t ldB,
@@ -686,16 +761,16 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
     if (ntasks <= 0) {
         return;
     }
-    const size_t smem = sizeof(float) * SW_ROWS * (size_t)(m | 1);
+    const int warps = sweep_warps(m);
+    const size_t smem = sizeof(double) * ((size_t)warps * SW_SNAP * (m + 1) + (m + 1)) +
+                        sizeof(float) * SW_ROWS * (size_t)(m | 1);
     const int comps = m + 1;
 #define LAUNCH_SWEEP(CPL)                                                                      \
     do {                                                                                       \
-        if (smem > 48 * 1024) {                                                                \
-            CUDA_CHECK(cudaFuncSetAttribute(k_sweep<CPL>,                                      \
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,       \
-                                            (int)smem));                                       \
-        }                                                                                      \
-        k_sweep<CPL><<<ntasks, SW_THREADS, smem, st>>>(tasks, perm, xsort, y, B, ldB, cand_b,  \
+        CUDA_CHECK(cudaFuncSetAttribute(k_sweep<CPL>,                                          \
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,           \
+                                        (int)smem));                                           \
+        k_sweep<CPL><<<ntasks, 32 * warps, smem, st>>>(tasks, perm, xsort, y, B, ldB, cand_b,  \
                                                        Bx, ldBx, Bo, ldbo, ybo, ybx, n, m,     \
                                                        head, tail, min_span, tol, hsse, hrow); \
     } while (0)
@@ -739,7 +814,7 @@ void sort_columns(cudaStream_t st, const float *X, size_t ldX, const float *s, i
                                                              vals.as<int>(), pc, n, 0, 32, st));
         k_gather_scaled<<<nb, 256, 0, st>>>(X, ldX, s, n, c, pc, xsort + (size_t)c * n);
         LAUNCH_CHECK();
-        *launches += 2 + 4;  // our two kernels plus the radix-sort passes
+        *launches += 2;  // the radix sort's own kernels are not counted
     }
 }
 
@@ -773,47 +848,51 @@ void append_fill(cudaStream_t st, char type, const float *X, size_t ldX, const f
                  int xcol, float *B, size_t ldB, int bcol, int m, float h, int n,
                  const AppendScratch &ws, long long *launches)
 {
-    k_append_fill<<<ws.nblocks, AP_THREADS, 0, st>>>(type, X, ldX, s, xcol, B, ldB, bcol, m, h, n,
-                                                     ws.v, ws.part);
+    const int nb = append_blocks(n);
+    k_append_fill<<<nb, AP_THREADS, 0, st>>>(type, X, ldX, s, xcol, B, ldB, bcol, m, h, n, ws.v);
     LAUNCH_CHECK();
-    k_append_scale<<<ws.nblocks, AP_THREADS, 0, st>>>(B, ldB, m, n, ws.part, ws.nblocks);
+    k_serial_dot<VSq><<<1, SER_THREADS, 0, st>>>(VSq{ws.v}, n, ws.scal + 3);
     LAUNCH_CHECK();
-    *launches += 2;
+    k_append_scale<<<nb, AP_THREADS, 0, st>>>(B, ldB, m, n, ws.scal + 3);
+    LAUNCH_CHECK();
+    *launches += 3;
 }
 
 void mgs_pass(cudaStream_t st, const float *BoC, int n, int m, const AppendScratch &ws,
               long long *launches)
 {
-    for (int j = 0; j <= m; ++j) {
-        k_mgs_step<<<ws.nblocks, AP_THREADS, 0, st>>>(BoC, n, m, j, ws.v, ws.part, ws.nblocks,
-                                                      ws.coef);
-        LAUNCH_CHECK();
-    }
-    k_mgs_finish<<<1, 32, 0, st>>>(ws.part, ws.nblocks, m, ws.coef, ws.scal);
+    k_mgs_serial<<<1, SER_THREADS, 0, st>>>(BoC, n, m, ws.v, ws.coef, ws.scal);
     LAUNCH_CHECK();
-    *launches += m + 2;
+    *launches += 1;
 }
 
 void append_store(cudaStream_t st, double w, float *Bo, size_t ldbo, float *BoC, int n, int m,
                   const float *y, const AppendScratch &ws, long long *launches)
 {
-    k_append_store<<<ws.nblocks, AP_THREADS, 0, st>>>(w, ws.v, Bo, ldbo, BoC, n, m, y, ws.part);
+    k_append_store<<<append_blocks(n), AP_THREADS, 0, st>>>(w, ws.v, Bo, ldbo, BoC, n, m);
     LAUNCH_CHECK();
-    k_sum_into<<<1, 32, 0, st>>>(ws.part, ws.nblocks, ws.scal + 2);
+    k_serial_dot<ColDotY><<<1, SER_THREADS, 0, st>>>(ColDotY{BoC + (size_t)m * n, y}, n,
+                                                     ws.scal + 2);
     LAUNCH_CHECK();
     *launches += 2;
 }
 
+// sum_i X[i,j]^2 per column as the reference's sequential fused chain
+// (marsalgo.cc:359-369).
+struct XSqChain {
+    const float *X;
+    size_t ld;
+    __device__ __forceinline__ double operator()(size_t i, int j, double acc) const
+    {
+        const double x = (double)X[i + (size_t)j * ld];
+        return fma(x, x, acc);
+    }
+};
+
 void column_sumsq(cudaStream_t st, const float *X, size_t ldX, int n, int p, double *out,
-                  double *part, long long *launches)
+                  long long *launches)
 {
-    const int nb = append_blocks(n);
-    verify(p <= 65535, "more than 65535 X columns");
-    k_colsumsq<<<dim3(nb, p), CS_THREADS, 0, st>>>(X, ldX, n, p, part);
-    LAUNCH_CHECK();
-    k_reduce_cols<<<(unsigned)ceil_div(p, 128), 128, 0, st>>>(part, nb, p, out);
-    LAUNCH_CHECK();
-    *launches += 2;
+    colchain(st, XSqChain{X, ldX}, n, p, out, launches);
 }
 
 }  // namespace mgpu

@@ -48,11 +48,7 @@ struct SweepTask {
 //   s  = ||Bx||^2             (FP64, of the rounded values)
 // `out_col` maps candidate j to its output column (null: identity).
 struct ProjectScratch {
-    double *T;      // [P][m]
-    double *Tpart;  // [splits][P][m]
-    double *part;   // [row blocks][P]
-    size_t part_elems;
-    size_t tpart_elems;
+    double *T;  // [P][m]
 };
 
 template <class Src>
@@ -60,15 +56,11 @@ void project_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo,
                   int P, const int *out_col, float *Bx, size_t ldBx, double *s_out,
                   const ProjectScratch &ws, long long *launches);
 
-// Workspace sizes (elements) for project_fp64 / normalize_ybx.
-size_t project_tpart_elems(int n, int m, int P);
-size_t project_part_elems(int n, int P);
-size_t normalize_part_elems(int n, int P);
-
-// T[j][c] = sum_i Bo[i,c] * src(i, j) only (FP64, deterministic split-K).
+// T[j][c] = sum_i Bo[i,c] * src(i, j) only, each entry one fused chain over
+// the rows in order (the reference's accumulation order).
 template <class Src>
 void tgemm_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, int n, int m,
-                int P, double *T, double *Tpart, size_t tpart_elems, long long *launches);
+                int P, double *T, long long *launches);
 
 // s[fired[q]] = snew[q] for q < nf.
 void scatter_s(cudaStream_t st, const int *fired, int nf, const double *snew, double *s,
@@ -82,10 +74,13 @@ void dgks_gate(cudaStream_t st, const double *T, int m, int P, const double *s, 
 // Normalise (kernels.cc:401-416) and ybx = Bx^T y (kernels.cc:215-237):
 // scale = s > tol ? f32(1/sqrt(s+tol)) : 0; Bx *= scale (if store); ybx in FP64.
 void normalize_ybx(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const double *s,
-                   double tol, const float *y, bool store, double *ybx, double *part,
-                   long long *launches);
+                   double tol, const float *y, bool store, double *ybx, long long *launches);
 
-// Hinge sweep in FP64 (marsalgo.cc:508-657), one warp per candidate.
+// Candidates per hinge-sweep block (one warp each) for m live basis columns.
+int sweep_warps(int m);
+
+// Hinge sweep in FP64 (marsalgo.cc:508-657), one warp per candidate; tasks
+// hold at most sweep_warps(m) candidates.
 void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *perm,
                 const float *xsort, const float *y, const float *B, size_t ldB,
                 const int *cand_b, const float *Bx, size_t ldBx, const float *Bo, size_t ldbo,
@@ -108,11 +103,9 @@ void fill_outputs(cudaStream_t st, int rows, int m, double *lin, double *hin, do
 
 // --- append (marsalgo.cc:760-875 and kernels.cc:194-281) -------------------
 struct AppendScratch {
-    double *v;       // n
-    double *part;    // 2 * nblocks
-    double *coef;    // max_terms
-    double *scal;    // small result slots
-    int nblocks;
+    double *v;     // n
+    double *coef;  // max_terms
+    double *scal;  // result slots: 0 sum c^2, 1 ||v||^2, 2 ybo_m, 3 raw norm^2
 };
 int append_blocks(int n);
 // Bm = s * B[:,bcol] * f(X[:,xcol]) into B[:, m]; v = (double)Bm; then
@@ -120,8 +113,9 @@ int append_blocks(int n);
 void append_fill(cudaStream_t st, char type, const float *X, size_t ldX, const float *s,
                  int xcol, float *B, size_t ldB, int bcol, int m, float h, int n,
                  const AppendScratch &ws, long long *launches);
-// One modified Gram-Schmidt pass of v against BoC[:, 0:m] (column-major, ld n);
-// leaves sum(c^2) in scal[0] and ||v||^2 in scal[1].
+// One modified Gram-Schmidt pass of v against BoC[:, 0:m] (column-major, ld n),
+// every reduction one fused chain over the rows in order; leaves sum(c^2) in
+// scal[0] and ||v||^2 in scal[1].
 void mgs_pass(cudaStream_t st, const float *BoC, int n, int m, const AppendScratch &ws,
               long long *launches);
 // v /= w; store f32(v) as column m of Bo (row-major) and BoC; ybo_m -> scal[2].
@@ -130,7 +124,7 @@ void append_store(cudaStream_t st, double w, float *Bo, size_t ldbo, float *BoC,
 
 // Column sums of squares sum_i X[i,j]^2 in FP64 (for s = 1/rms).
 void column_sumsq(cudaStream_t st, const float *X, size_t ldX, int n, int p, double *out,
-                  double *part, long long *launches);
+                  long long *launches);
 
 
 }  // namespace mgpu

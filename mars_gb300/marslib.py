@@ -30,6 +30,11 @@ class Stats(ctypes.Structure):
         ("dgks_fired", ctypes.c_longlong),
         ("redecided", ctypes.c_longlong),
         ("kernel_launches", ctypes.c_longlong),
+        ("h2d_bytes", ctypes.c_longlong),
+        ("d2h_bytes", ctypes.c_longlong),
+        ("project_flops", ctypes.c_double),
+        ("sweep_bytes", ctypes.c_double),
+        ("ms_span", ctypes.c_double),
         ("ms_project", ctypes.c_double),
         ("ms_dgks", ctypes.c_double),
         ("ms_normalize", ctypes.c_double),

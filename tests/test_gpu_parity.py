@@ -1,14 +1,14 @@
 """GPU parity: the CUDA path against the CPU oracle and the reference's goldens.
 
 All calls go through the C ABI (include/mars_gpu.h) via mars_gb300.marslib.
-Tolerances:
-  term path (type, parent, input, knot)   bit-exact vs the reference golden
-  r2 / r2_cv                               1e-6 absolute (f4 fields)
-  linear delta SSE                         1e-12 relative vs the oracle
-  hinge delta SSE                          1e-9 relative vs the oracle
-  knot (cut)                               bit-exact
-  append MSE                               1e-12 relative
-  orthonormalised columns                  1e-6 absolute (f32 storage, one ulp)
+The FP64 path reproduces the reference's scalar arithmetic operation for
+operation (every reduction over rows is one fused chain in row order, every
+reduction over basis columns one chain in column order), so against the
+oracle -- the C restatement of that arithmetic -- it is compared for exact
+equality: linear and hinge delta SSE, knots, append MSE, normalised columns,
+squared norms and DGKS counts. Against the reference goldens (its x86 AVX
+build, whose hinge reductions run in another order) the term path is exact and
+r2 / r2_cv agree to 1e-6 (f4 fields).
 """
 import os
 
@@ -56,17 +56,16 @@ def test_eval_matches_oracle(name, precision, gpu, port):
     a_cpu = oracle.OracleAlgo(X, y, w, cases.EVAL_MAX_TERMS, kind="port")
     assert a_gpu.yvar() == a_cpu.yvar()
     for ap in appends:
-        mg, mc = a_gpu.append(*ap), a_cpu.append(*ap)
-        assert mg == pytest.approx(mc, rel=1e-12, abs=1e-300)
+        assert a_gpu.append(*ap) == a_cpu.append(*ap)
     assert a_gpu.nbasis() == a_cpu.nbasis()
-    assert a_gpu.dsse() == pytest.approx(a_cpu.dsse(), rel=1e-14)
+    assert a_gpu.dsse() == a_cpu.dsse()
     for i, (ms, es, lo) in enumerate(evals):
         mask = cases.eval_mask(X.shape[1], a_cpu.nbasis(), i)
         dg, lg, hg, cg = a_gpu.eval(mask, ms, es, lo, 1)
         dc, lc, hc, cc = a_cpu.eval(mask, ms, es, lo, 1)
-        assert dg == pytest.approx(dc, rel=1e-14)
-        np.testing.assert_allclose(lg, lc, rtol=1e-12, atol=1e-300)
-        np.testing.assert_allclose(hg, hc, rtol=1e-9, atol=1e-300)
+        assert dg == dc
+        np.testing.assert_array_equal(lg, lc)
+        np.testing.assert_array_equal(hg, hc)
         np.testing.assert_array_equal(cg, cc)
     mx, rss = a_gpu.orth_error()
     assert mx < 1e-5
@@ -97,8 +96,8 @@ def test_orthonormalize_stress_matches_oracle(be_gpu, be_port):
     Bx_g, s_g, d_g = scenarios.orthonormalize_stress(be_gpu)
     Bx_c, s_c, d_c = scenarios.orthonormalize_stress(be_port)
     assert d_g == d_c
-    np.testing.assert_allclose(Bx_g, Bx_c, rtol=0, atol=1e-6)
-    np.testing.assert_allclose(s_g, s_c, rtol=1e-10, atol=1e-300)
+    np.testing.assert_array_equal(Bx_g, Bx_c)
+    np.testing.assert_array_equal(s_g, s_c)
 
 
 def test_orthonormalize_matches_oracle_random(be_gpu, be_port):
@@ -112,7 +111,8 @@ def test_orthonormalize_matches_oracle_random(be_gpu, be_port):
     mask = np.sort(rng.permutation(m)[:p]).astype(np.int32)
     r_g = be_gpu.orthonormalize(np.asfortranarray(B), x, mask, Bo, m, 1e-14)
     r_c = be_port.orthonormalize(np.asfortranarray(B), x, mask, Bo, m, 1e-14)
-    np.testing.assert_allclose(r_g[0], r_c[0], rtol=0, atol=1e-6)
+    np.testing.assert_array_equal(r_g[0], r_c[0])
+    np.testing.assert_array_equal(r_g[1], r_c[1])
     assert r_g[2] == r_c[2]
 
 
@@ -156,14 +156,13 @@ def test_edge_end_span(gpu, port, end_span):
     a_g = gpu.MarsAlgo(X, y, w, 6)
     a_c = oracle.OracleAlgo(X, y, w, 6, kind="port")
     for ap in [("l", 0, 0, 0), ("+", 2, 0, 0.1)]:
-        assert a_g.append(*ap) == pytest.approx(a_c.append(*ap), rel=1e-12)
+        assert a_g.append(*ap) == a_c.append(*ap)
     mask = np.ones((3, a_c.nbasis()), bool)
     mask[2, 1] = False
     rg = a_g.eval(mask, 3, end_span, False, 1)
     rc = a_c.eval(mask, 3, end_span, False, 1)
-    np.testing.assert_allclose(rg[1], rc[1], rtol=1e-12, atol=1e-300)
-    np.testing.assert_allclose(rg[2], rc[2], rtol=1e-9, atol=1e-300)
-    np.testing.assert_array_equal(rg[3], rc[3])
+    for k in (1, 2, 3):
+        np.testing.assert_array_equal(rg[k], rc[k])
 
 
 def test_edge_degenerate_columns(gpu, port):
@@ -175,14 +174,14 @@ def test_edge_degenerate_columns(gpu, port):
     a_g = gpu.MarsAlgo(X, y, w, 8)
     a_c = oracle.OracleAlgo(X, y, w, 8, kind="port")
     for ap in [("l", 1, 0, 0), ("l", 2, 0, 0), ("l", 0, 0, 0), ("-", 3, 0, 0.0)]:
-        assert a_g.append(*ap) == pytest.approx(a_c.append(*ap), rel=1e-12)
+        assert a_g.append(*ap) == a_c.append(*ap)
     assert a_g.nbasis() == a_c.nbasis()
     mask = np.ones((4, a_c.nbasis()), bool)
     mask[0, :] = False  # an input with no candidate
     rg = a_g.eval(mask, 1, 0, False, 1)
     rc = a_c.eval(mask, 1, 0, False, 1)
     for k in (1, 2, 3):
-        np.testing.assert_allclose(rg[k], rc[k], rtol=1e-9, atol=1e-300)
+        np.testing.assert_array_equal(rg[k], rc[k])
 
 
 def test_small_n_and_single_column(gpu, port):
@@ -196,7 +195,7 @@ def test_small_n_and_single_column(gpu, port):
         rg = a_g.eval(mask, 1, 0, False, 1)
         rc = a_c.eval(mask, 1, 0, False, 1)
         for k in (1, 2, 3):
-            np.testing.assert_allclose(rg[k], rc[k], rtol=1e-9, atol=1e-300)
+            np.testing.assert_array_equal(rg[k], rc[k])
 
 
 def test_fit_with_weights_and_nan_target(gpu, port_lib):
@@ -209,4 +208,8 @@ def test_fit_with_weights_and_nan_target(gpu, port_lib):
     kw = dict(max_terms=11, min_span=3, tail_span=0.01)
     m_g = mars.fit(X, y, w, **kw)
     m_c = mars.forward_pass(port_lib, X, y, w, **kw)
-    assert [tuple(r)[:4] for r in m_g.tolist()] == [tuple(r)[:4] for r in m_c.tolist()]
+    def path(model):
+        return [(r["type"], int(r["basis"]), int(r["input"]),
+                 None if np.isnan(r["hinge"]) else float(r["hinge"])) for r in model]
+
+    assert path(m_g) == path(m_c)
