@@ -89,7 +89,10 @@ MARS_GPU_API int mars_gpu_device_count(void);
  *  y, w: (n) f32 (w are inverse-variance weights; non-finite y rows get
  *  weight 0). max_terms: basis capacity including the intercept.
  *  Errors: "target Y is all zero or NANs", "not all columns in X are finite".
- *  X is copied to the device; the caller may free it afterwards.
+ *  X is copied to the device and also borrowed, like the reference's
+ *  MarsAlgo borrows it: it must stay valid and unchanged until
+ *  mars_gpu_destroy (the host keeps the reference-order FP64 state of the fit,
+ *  the append and the exact re-scoring of near-tied candidates read it).
  */
 MARS_GPU_API int mars_gpu_create(const float *X, const float *y, const float *w, size_t n, size_t p,
                     size_t ldx, size_t max_terms, mars_gpu_algo **out);

@@ -1,7 +1,8 @@
 """Build recipe for the GB300 forward-pass library.
 
-Compiles every ``csrc/*.cu`` for sm_103a with nvcc (one translation unit per
-process, in parallel) and links ``mars_gb300/lib/libmars_gpu.so``, a plain
+Compiles every ``csrc/*.cu`` for sm_103a with nvcc and every ``csrc/*.cpp``
+(host code) with g++, one translation unit per process in parallel, and links
+``mars_gb300/lib/libmars_gpu.so``, a plain
 C-ABI shared library (include/mars_gpu.h) with the CUDA runtime linked
 statically. Objects go to ``mars_gb300/_build/``.
 
@@ -40,16 +41,28 @@ def flags():
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
+                  if f.endswith(".cu") or f.endswith(".cpp"))
+
+
+def host_flags():
+    # plain C++ (no ISA-specific flags: the library builds on x86_64 and aarch64)
+    return ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden",
+            "-pthread", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 
 def _compile(src, extra):
-    obj = os.path.join(OBJ, os.path.basename(src)[:-3] + ".o")
-    deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".cuh")]
+    base = os.path.basename(src)
+    obj = os.path.join(OBJ, base.rsplit(".", 1)[0] + (".cu.o" if base.endswith(".cu") else ".o"))
+    deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC)
+                    if h.endswith(".cuh") or h.endswith(".h")]
     deps.append(os.path.join(ROOT, "include", "mars_gpu.h"))
     if os.path.isfile(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj, ""
-    cmd = [nvcc()] + flags() + extra + ["-c", src, "-o", obj]
+    if src.endswith(".cpp"):
+        cmd = [os.environ.get("CXX", "g++")] + host_flags() + ["-c", src, "-o", obj]
+    else:
+        cmd = [nvcc()] + flags() + extra + ["-c", src, "-o", obj]
     out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), out.stderr))
@@ -70,7 +83,7 @@ def build(verbose=False, extra=()):
                 sys.stderr.write(log)
     newest = max(os.path.getmtime(o) for o in objs)
     if not (os.path.isfile(LIB) and os.path.getmtime(LIB) >= newest):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-Xcompiler", "-pthread"]
         out = subprocess.run(cmd, capture_output=True, text=True)
         if out.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), out.stderr))

@@ -6,6 +6,7 @@
 #include "../../include/mars_gpu.h"
 #include "common.cuh"
 #include "fp64.cuh"
+#include "host_exact.h"
 
 #include <algorithm>
 #include <cfloat>
@@ -107,13 +108,14 @@ struct mars_gpu_algo {
     bool span_started = false;
     mars_gpu_stats stats;
 
+    // Host copy of the basis, kept in the reference's exact arithmetic.
+    HostBasis hb;
     // Resident state.
     DevBuf X, s, y, B, Bo, BoC, ybo_d, perm, xsort;
     std::vector<char> sorted;
     // Per-eval scratch (grow-only).
     DevBuf Bx, T, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks;
     DevBuf sort_keys, sort_vals, sort_tmp;
-    DevBuf ap_v, ap_coef, ap_scal;
 
     ~mars_gpu_algo()
     {
@@ -151,17 +153,6 @@ void span_mark_end(mars_gpu_algo *a)
     }
 }
 
-AppendScratch append_scratch(mars_gpu_algo *a)
-{
-    a->ap_v.ensure(sizeof(double) * a->n);
-    a->ap_coef.ensure(sizeof(double) * (a->max_terms + 1));
-    a->ap_scal.ensure(sizeof(double) * 8);
-    AppendScratch ws;
-    ws.v = a->ap_v.as<double>();
-    ws.coef = a->ap_coef.as<double>();
-    ws.scal = a->ap_scal.as<double>();
-    return ws;
-}
 
 __global__ void k_col_to_rows(const float *__restrict__ col, int n, float *__restrict__ Bo,
                               size_t ldbo, int c)
@@ -175,111 +166,55 @@ __global__ void k_col_to_rows(const float *__restrict__ col, int n, float *__res
 void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *w, size_t n,
                  size_t p, size_t ldx, size_t max_terms)
 {
-    verify(!std::isfinite(NAN), "NAN check is disabled, recompile without --fast-math");
-    verify(max_terms >= 1, "max_terms must be >= 1");
     verify(ldx >= n || p <= 1, "X column stride smaller than the row count");
     verify(p <= 65535, "more than 65535 X columns");
     verify(n < (size_t)INT32_MAX, "more rows than the GPU path supports (2^31 - 1)");
+    // The weighted, normalised target, the intercept and the column scales in
+    // the reference's arithmetic (marsalgo.cc:266-370), on the host.
+    a->hb.init(X, y, w, n, p, ldx, max_terms);
     a->n = n;
     a->p = p;
     a->max_terms = max_terms;
     a->ldbo = round_up(max_terms, 4);
     a->m = 1;
-    a->tol = ((double)n * 0.02) * DBL_EPSILON;
+    a->tol = a->hb.tol;
+    a->yvar = a->hb.yvar;
+    a->ybo = a->hb.ybo;
     std::memset(&a->stats, 0, sizeof(a->stats));
     CUDA_CHECK(cudaStreamCreateWithFlags(&a->st, cudaStreamNonBlocking));
     CUDA_CHECK(cudaEventCreate(&a->span_begin));
     CUDA_CHECK(cudaEventCreate(&a->span_end));
     a->timer.st = a->st;
 
-    // Weighted, normalised target (marsalgo.cc:278-352), in the reference's
-    // order of operations; fused multiply-adds where the reference fuses.
-    std::vector<double> yd(n), sw(n);
-    for (size_t i = 0; i < n; ++i) {
-        double yi = (double)y[i];
-        double swi = std::sqrt((double)w[i]);
-        if (!std::isfinite(yi)) {
-            yi = swi = 0.0;
-        }
-        sw[i] = swi;
-        yd[i] = yi * swi;
-    }
-    double y_sq = 0.0, w_sq = 0.0;
-    for (size_t i = 0; i < n; ++i) {
-        y_sq = std::fma(yd[i], yd[i], y_sq);
-        w_sq = std::fma(sw[i], sw[i], w_sq);
-    }
-    const double y_norm = std::sqrt(y_sq), w_norm = std::sqrt(w_sq);
-    verify(y_norm > 0.0 && w_norm > 0.0, "target Y is all zero or NANs");
-    std::vector<float> yf(n), b0(n);
-    for (size_t i = 0; i < n; ++i) {
-        yd[i] /= y_norm;
-        sw[i] /= w_norm;
-        yf[i] = (float)yd[i];
-        b0[i] = (float)sw[i];
-    }
-    double ybo0 = 0.0;
-    for (size_t i = 0; i < n; ++i) {
-        ybo0 = std::fma((double)b0[i], (double)yf[i], ybo0);
-    }
-    a->ybo.assign(1, ybo0);
-    double ymean_sum = 0.0;
-    for (size_t i = 0; i < n; ++i) {
-        ymean_sum += yd[i];
-    }
-    const double ymean = ymean_sum / (double)n;
-    double vsum = 0.0;
-    for (size_t i = 0; i < n; ++i) {
-        const double dv = yd[i] - ymean;
-        vsum = std::fma(dv, dv, vsum);
-    }
-    a->yvar = vsum / (double)n;
-
     // Device-resident state.
-    a->stats.h2d_bytes += (long long)(sizeof(float) * (n * p + 3 * n));
+    a->stats.h2d_bytes += (long long)(sizeof(float) * (n * p + 3 * n + p));
     a->X.ensure(sizeof(float) * std::max<size_t>(1, n * p));
     if (n * p) {
         CUDA_CHECK(cudaMemcpy2DAsync(a->X.ptr, n * sizeof(float), X, ldx * sizeof(float),
                                      n * sizeof(float), p, cudaMemcpyHostToDevice, a->st));
     }
+    a->s.ensure(sizeof(float) * std::max<size_t>(1, p));
+    if (p) {
+        CUDA_CHECK(cudaMemcpyAsync(a->s.ptr, a->hb.s.data(), sizeof(float) * p,
+                                   cudaMemcpyHostToDevice, a->st));
+    }
     a->y.ensure(sizeof(float) * n);
-    CUDA_CHECK(cudaMemcpyAsync(a->y.ptr, yf.data(), sizeof(float) * n, cudaMemcpyHostToDevice,
-                               a->st));
+    CUDA_CHECK(cudaMemcpyAsync(a->y.ptr, a->hb.y.data(), sizeof(float) * n,
+                               cudaMemcpyHostToDevice, a->st));
     a->B.ensure(sizeof(float) * n * max_terms);
     a->BoC.ensure(sizeof(float) * n * max_terms);
     a->Bo.ensure(sizeof(float) * n * a->ldbo);
     CUDA_CHECK(cudaMemsetAsync(a->Bo.ptr, 0, sizeof(float) * n * a->ldbo, a->st));
-    CUDA_CHECK(cudaMemcpyAsync(a->B.ptr, b0.data(), sizeof(float) * n, cudaMemcpyHostToDevice,
-                               a->st));
-    CUDA_CHECK(cudaMemcpyAsync(a->BoC.ptr, b0.data(), sizeof(float) * n, cudaMemcpyHostToDevice,
-                               a->st));
+    CUDA_CHECK(cudaMemcpyAsync(a->B.ptr, a->hb.B.data(), sizeof(float) * n,
+                               cudaMemcpyHostToDevice, a->st));
+    CUDA_CHECK(cudaMemcpyAsync(a->BoC.ptr, a->hb.BoC.data(), sizeof(float) * n,
+                               cudaMemcpyHostToDevice, a->st));
     k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(a->BoC.as<float>(), (int)n,
                                                                 a->Bo.as<float>(), a->ldbo, 0);
     LAUNCH_CHECK();
     a->ybo_d.ensure(sizeof(double) * max_terms);
     CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.ptr, &a->ybo[0], sizeof(double), cudaMemcpyHostToDevice,
                                a->st));
-
-    // Column scales s = 1/rms (marsalgo.cc:359-369).
-    a->s.ensure(sizeof(float) * std::max<size_t>(1, p));
-    if (p) {
-        DevBuf sums;
-        sums.ensure(sizeof(double) * p);
-        column_sumsq(a->st, a->X.as<float>(), n, (int)n, (int)p, sums.as<double>(),
-                     &a->stats.kernel_launches);
-        std::vector<double> sq(p);
-        CUDA_CHECK(cudaMemcpyAsync(sq.data(), sums.ptr, sizeof(double) * p, cudaMemcpyDeviceToHost,
-                                   a->st));
-        sync(a);
-        std::vector<float> sv(p);
-        for (size_t j = 0; j < p; ++j) {
-            const double rms = std::sqrt(sq[j] / (double)n);
-            verify(std::isfinite(rms), "not all columns in X are finite");
-            sv[j] = rms > 0.0 ? (float)(1.0 / rms) : 1.0f;
-        }
-        CUDA_CHECK(cudaMemcpyAsync(a->s.ptr, sv.data(), sizeof(float) * p, cudaMemcpyHostToDevice,
-                                   a->st));
-    }
     a->sorted.assign(p, 0);
     sync(a);
 }
@@ -505,50 +440,33 @@ double append_impl(mars_gpu_algo *a, char type, int xcol, int bcol, float h)
     }
     verify(xcol >= 0 && (size_t)xcol < a->p, "invalid X column index");
     verify(type == 'l' || type == '+' || type == '-', "invalid basis type");
-    const int n = (int)a->n, m = (int)a->m;
-    AppendScratch ws = append_scratch(a);
-    double scal[3];
+    const size_t n = a->n, m = a->m;
+    // The serial Gram-Schmidt of the reference, on the host (host_exact.h).
+    long dgks = 0;
+    const double mse = a->hb.append(type, xcol, bcol, h, &dgks);
+    a->stats.dgks_fired += dgks;
     cudaEvent_t t0 = a->timer.begin();
-    append_fill(a->st, type, a->X.as<float>(), a->n, a->s.as<float>(), xcol, a->B.as<float>(),
-                a->n, bcol, m, h, n, ws, &a->stats.kernel_launches);
-    mgs_pass(a->st, a->BoC.as<float>(), n, m, ws, &a->stats.kernel_launches);
-    CUDA_CHECK(cudaMemcpyAsync(scal, ws.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, a->st));
-    sync(a);
-    double v_norm2 = scal[1];
-    if (v_norm2 > a->tol && v_norm2 * 9.0 < scal[0]) {
-        mgs_pass(a->st, a->BoC.as<float>(), n, m, ws, &a->stats.kernel_launches);
-        CUDA_CHECK(cudaMemcpyAsync(scal, ws.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost,
-                                   a->st));
-        sync(a);
-        v_norm2 = scal[1];
-    }
-    const double w = std::sqrt(v_norm2);
-    double result = -1.0;
-    if (w * w > a->tol) {
-        append_store(a->st, w, a->Bo.as<float>(), a->ldbo, a->BoC.as<float>(), n, m,
-                     a->y.as<float>(), ws, &a->stats.kernel_launches);
-        CUDA_CHECK(cudaMemcpyAsync(scal + 2, ws.scal + 2, sizeof(double), cudaMemcpyDeviceToHost,
-                                   a->st));
-        sync(a);
-        const double ybo_m = scal[2];
-        double ybo_sq = ybo_m * ybo_m;
-        for (double e : a->ybo) {
-            ybo_sq = std::fma(e, e, ybo_sq);
-        }
-        const double mse = (1. - ybo_sq) / (double)n;
-        if (mse >= -a->tol) {
-            a->ybo.push_back(ybo_m);
-            CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.as<double>() + m, &a->ybo.back(), sizeof(double),
-                                       cudaMemcpyHostToDevice, a->st));
-            a->m += 1;
-            result = mse < 0.0 ? 0.0 : mse;
-        }
+    CUDA_CHECK(cudaMemcpyAsync(a->B.as<float>() + m * n, a->hb.B.data() + m * n,
+                               sizeof(float) * n, cudaMemcpyHostToDevice, a->st));
+    a->stats.h2d_bytes += (long long)(sizeof(float) * n);
+    if (a->hb.m > m) {
+        CUDA_CHECK(cudaMemcpyAsync(a->BoC.as<float>() + m * n, a->hb.BoC.data() + m * n,
+                                   sizeof(float) * n, cudaMemcpyHostToDevice, a->st));
+        k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(
+            a->BoC.as<float>() + m * n, (int)n, a->Bo.as<float>(), a->ldbo, (int)m);
+        LAUNCH_CHECK();
+        a->stats.kernel_launches += 1;
+        CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.as<double>() + m, &a->hb.ybo[m], sizeof(double),
+                                   cudaMemcpyHostToDevice, a->st));
+        a->stats.h2d_bytes += (long long)(sizeof(float) * n + sizeof(double));
+        a->m = a->hb.m;
+        a->ybo = a->hb.ybo;
     }
     a->timer.end(PH_APPEND, t0);
     span_mark_end(a);
     sync(a);
     a->timer.resolve(a->phase_ms);
-    return result;
+    return mse;
 }
 
 }  // namespace

@@ -8,13 +8,9 @@
 #include <stdexcept>
 #include <string>
 
-namespace mgpu {
+#include "error.h"
 
-// Error carrying a C-ABI status code; converted to a status at the ABI edge.
-struct Error : std::runtime_error {
-    int status;
-    Error(int st, const std::string &msg) : std::runtime_error(msg), status(st) {}
-};
+namespace mgpu {
 
 inline void cuda_check(cudaError_t e, const char *what, const char *file, int line)
 {
@@ -26,13 +22,6 @@ inline void cuda_check(cudaError_t e, const char *what, const char *file, int li
 }
 #define CUDA_CHECK(x) ::mgpu::cuda_check((x), #x, __FILE__, __LINE__)
 #define LAUNCH_CHECK() ::mgpu::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
-
-inline void verify(bool ok, const char *msg, int status = 1)
-{
-    if (!ok) {
-        throw Error(status, msg);
-    }
-}
 
 inline size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
 inline size_t round_up(size_t a, size_t b) { return ceil_div(a, b) * b; }

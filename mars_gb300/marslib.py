@@ -134,6 +134,7 @@ class MarsAlgo:
         self._h = h
         self._L = L
         self._p = p
+        self._X = X  # borrowed by the library until destroy (keep_alive, marslib.cc:166)
         mode = os.environ.get("MARS_GPU_PRECISION", "").strip().lower()
         if mode:
             self.set_precision(mode)
