@@ -55,32 +55,78 @@ __global__ void __launch_bounds__(TG_THREADS)
     }
 }
 
-// out[j] = fused chain over i = 0..n-1 (in order) of a*b for the pairs the
-// functor yields: the reference's sequential f64 accumulations
-// (kernels.cc:361-366 norm of the stored column; kernels.cc:215-237 dot_widen).
+// Column chains: warp 0 of a block runs 32 column chains (lane = column) out
+// of shared memory while warps 1..3 stage the next tile of rows.
+constexpr int CC_COLS = 32, CC_ROWS = 128, CC_THREADS = 128;
+
+// Fused chains over the rows i = 0..n-1 in order: the reference's sequential
+// f64 accumulations (kernels.cc:361-366 norm of the stored column;
+// kernels.cc:215-237 dot_widen; marsalgo.cc:359-369 column norms of X).
 struct SqChain {  // sum of squares of the stored f32 column Bx[:, col[j]]
+    static constexpr bool kUsesY = false;
     const float *Bx;
     size_t ld;
     const int *col;
-    __device__ __forceinline__ double operator()(size_t i, int j, double acc) const
+    __device__ __forceinline__ float load(size_t i, int j) const
     {
-        const double v = (double)Bx[i + (size_t)(col ? col[j] : j) * ld];
-        return fma(v, v, acc);
+        return Bx[i + (size_t)(col ? col[j] : j) * ld];
     }
+    __device__ __forceinline__ float yload(size_t) const { return 0.f; }
+    __device__ __forceinline__ double step(double acc, float v, float) const
+    {
+        const double d = (double)v;
+        return fma(d, d, acc);
+    }
+    __device__ __forceinline__ double finish(double acc, int) const { return acc; }
 };
+
 template <class Op>
-__global__ void __launch_bounds__(64) k_colchain(Op op, int n, int P, double *__restrict__ out)
+__global__ void __launch_bounds__(CC_THREADS) k_colchain(Op op, int n, int P, double *__restrict__ out)
 {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= P) {
-        return;
+    __shared__ float tile[2][CC_COLS][CC_ROWS + 1];
+    __shared__ float ytile[2][CC_ROWS];
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int j0 = blockIdx.x * CC_COLS;
+    const int ncols = min(CC_COLS, P - j0);
+    const int ntiles = (n + CC_ROWS - 1) / CC_ROWS;
+    auto load = [&](int tl, int b) {
+        const int base = tl * CC_ROWS, rows = min(CC_ROWS, n - base);
+        for (int e = t - 32; e < ncols * CC_ROWS; e += CC_THREADS - 32) {
+            const int c = e / CC_ROWS, r = e % CC_ROWS;
+            if (r < rows) {
+                tile[b][c][r] = op.load((size_t)(base + r), j0 + c);
+            }
+        }
+        if (Op::kUsesY) {
+            for (int r = t - 32; r < rows; r += CC_THREADS - 32) {
+                ytile[b][r] = op.yload((size_t)(base + r));
+            }
+        }
+    };
+    if (warp > 0) {
+        load(0, 0);
     }
+    __syncthreads();
     double acc = 0.0;
-    for (int i = 0; i < n; ++i) {
-        acc = op((size_t)i, j, acc);
+    for (int tl = 0; tl < ntiles; ++tl) {
+        const int b = tl & 1;
+        if (warp == 0) {
+            if (lane < ncols) {
+                const int rows = min(CC_ROWS, n - tl * CC_ROWS);
+                for (int r = 0; r < rows; ++r) {
+                    acc = op.step(acc, tile[b][lane][r], ytile[b][r]);
+                }
+            }
+        } else if (tl + 1 < ntiles) {
+            load(tl + 1, b ^ 1);
+        }
+        __syncthreads();
     }
-    out[j] = acc;
+    if (warp == 0 && lane < ncols) {
+        out[j0 + lane] = op.finish(acc, j0 + lane);
+    }
 }
+
 
 // ---------------------------------------------------------------------------
 // Bx <- f32(Bx - Bo T), one element per thread; the projection is the
@@ -157,18 +203,25 @@ __device__ __forceinline__ float norm_scale(double s, double tol)
 }
 
 // ybx[j] = fused chain over i of f32(Bx[i,j] * scale_j) * y[i] (dot_widen of the
-// normalised column, kernels.cc:215-237 after kernels.cc:401-416).
+// normalised column, kernels.cc:215-237 after kernels.cc:401-416). The scale
+// is applied when the tile is loaded.
 struct NormDotChain {
+    static constexpr bool kUsesY = true;
     const float *Bx;
     size_t ld;
     const float *y;
     const double *s;
     double tol;
-    __device__ __forceinline__ double operator()(size_t i, int j, double acc) const
+    __device__ __forceinline__ float load(size_t i, int j) const
     {
-        const float v = Bx[i + (size_t)j * ld] * norm_scale(s[j], tol);
-        return fma((double)v, (double)y[i], acc);
+        return Bx[i + (size_t)j * ld] * norm_scale(s[j], tol);
     }
+    __device__ __forceinline__ float yload(size_t i) const { return y[i]; }
+    __device__ __forceinline__ double step(double acc, float v, float yv) const
+    {
+        return fma((double)v, (double)yv, acc);
+    }
+    __device__ __forceinline__ double finish(double acc, int) const { return acc; }
 };
 
 constexpr int NM_THREADS = 256, NM_COLS = 8;
@@ -194,26 +247,25 @@ __global__ void __launch_bounds__(NM_THREADS)
 }
 
 // ---------------------------------------------------------------------------
-// FP64 hinge sweep (marsalgo.cc:576-649 with covariates_impl :91-151).
-// One warp per candidate; lane l owns components c = l + 32 q of f and g
-// (component m is the candidate column Bx itself). Sorted rows are staged 32
-// at a time: permutation, deltas, y and the gathered Bo rows (shared by all
-// candidates of the block's input column), and per warp B and Bx. At a grid
-// row the warp saves f into a snapshot slot; once SNAP slots are full each
-// lane scores one of them with the reference's sequential fused chains
-// ff = sum_c f_c^2, fy = sum_c f_c y_c (c = 0..m), so the scores match the
-// reference bit for bit while the chains run side by side.
+// FP64 hinge sweep (marsalgo.cc:576-649 with covariates_impl :91-151), in the
+// reference's operation order.
+//
+// Block = one input column and up to W candidates (parent columns): warps
+// 0..W-1 each own one candidate, lane l holding components c = l + 32 q of the
+// running f and g (component m is the candidate column Bx itself); warp W runs
+// the six scalar recurrences (k0, k1, w, bd, b2, vb) for all W candidates at
+// once, one lane per candidate. Sorted rows are staged SW_ROWS at a time as
+// doubles (converted once per block): permutation, delta, delta^2, y, the
+// gathered Bo rows, and B and Bx of every candidate. At a grid row each
+// candidate warp saves f in a snapshot slot and the scalar warp saves k0+k1
+// and w; once SW_SNAP slots are in use, lane q of each candidate warp scores
+// slot q with the reference's sequential chains ff = sum_c f_c^2 and
+// fy = sum_c f_c yc_c (c = 0..m), and the warp keeps the first maximum.
 // ---------------------------------------------------------------------------
-constexpr int SW_ROWS = 32, SW_SNAP = 16;
-
-struct SweepWarp {
-    double k01[SW_SNAP];
-    double w[SW_SNAP];
-    int row[SW_SNAP];
-};
+constexpr int SW_ROWS = 32, SW_SNAP = 32, SW_MAXW = 8;
 
 template <int CPL>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32 * (SW_MAXW + 1))
     k_sweep(const SweepTask *__restrict__ tasks, const int *__restrict__ perm,
             const float *__restrict__ xsort, const float *__restrict__ y,
             const float *__restrict__ B, size_t ldB, const int *__restrict__ cand_b,
@@ -223,137 +275,134 @@ __global__ void __launch_bounds__(256)
             int *__restrict__ hrow)
 {
     extern __shared__ double dyn[];
-    const int nwarps = blockDim.x >> 5;
+    const int W = (blockDim.x >> 5) - 1;  // candidate warps
     const int ldF = m + 1;
-    double *snap_all = dyn;                                  // nwarps * SW_SNAP * ldF
-    double *sY = snap_all + (size_t)nwarps * SW_SNAP * ldF;  // m (ybo)
-    float *sBo = (float *)(sY + m + 1);                      // SW_ROWS * ldS
-    const int ldS = m | 1;
+    double *snap_all = dyn;                                 // W * SW_SNAP * ldF
+    double *sBo = snap_all + (size_t)W * SW_SNAP * ldF;     // SW_ROWS * m (Bo rows, doubles)
+    double *sbd = sBo + (size_t)SW_ROWS * m;                // W * SW_ROWS (B of each candidate)
+    double *sbx = sbd + (size_t)W * SW_ROWS;                // W * SW_ROWS (Bx of each candidate)
+    double *sY = sbx + (size_t)W * SW_ROWS;                 // m + 1 (ybo, then unused)
+    double *mk = sY + (m + 1);                              // W * SW_SNAP (k0 + k1)
+    double *mw = mk + (size_t)W * SW_SNAP;                  // W * SW_SNAP (w)
     __shared__ int sk[SW_ROWS];
-    __shared__ float sd[SW_ROWS], sy[SW_ROWS];
-    __shared__ float sb[8][SW_ROWS], sbx[8][SW_ROWS];
-    __shared__ SweepWarp meta[8];
+    __shared__ double sd[SW_ROWS], sdd[SW_ROWS], syd[SW_ROWS];
+    __shared__ int srow[SW_SNAP];
 
     const SweepTask task = tasks[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bool active = warp < task.count;
-    const int cand = task.cand0 + (active ? warp : 0);
+    const bool cwarp = warp < task.count;           // an active candidate warp
+    const bool swarp = warp == W;                   // the scalar warp
     const int *pk = perm + (size_t)task.xcol * n;
     const float *xs = xsort + (size_t)task.xcol * n;
-    const float *bcol = B + (size_t)cand_b[cand] * ldB;
-    const float *bxcol = Bx + (size_t)cand * ldBx;
-    double *snap = snap_all + (size_t)warp * SW_SNAP * ldF;
-    SweepWarp &mw = meta[warp];
-    const double ybx_c = ybx[cand];
 
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
         sY[c] = ybo[c];
     }
+    const int mycand = task.cand0 + (cwarp ? warp : 0);
+    const double ybx_c = ybx[mycand];
+    double *snap = snap_all + (size_t)(cwarp ? warp : 0) * SW_SNAP * ldF;
     double f[CPL], g[CPL];
 #pragma unroll
     for (int q = 0; q < CPL; ++q) {
         f[q] = 0.0;
         g[q] = 0.0;
     }
+    // scalar-warp state: lane = candidate
+    const bool slane = swarp && lane < task.count;
     double k0 = 0, k1 = 0, w = 0, bd = 0, vb = 0, b2 = 0;
     double best = 0.0;
-    int besti = -1, nsnap = 0;
+    int besti = -1;
+    int nsnap = 0;  // block-uniform
     long next_grid = (long)head + 1;
 
-    // Score the saved grid rows: lane l takes slot l (in row order).
     auto flush = [&]() {
-        __syncwarp();
-        double sse = -1.0;
-        int row = 0x7fffffff;
-        if (lane < nsnap) {
-            const double *fs = snap + (size_t)lane * ldF;
-            double ff = 0.0, fy = 0.0;
-            for (int c = 0; c < m; ++c) {
-                ff = fma(fs[c], fs[c], ff);
-                fy = fma(fs[c], sY[c], fy);
+        if (cwarp) {
+            double sse = -1.0;
+            int row = 0x7fffffff;
+            if (lane < nsnap) {
+                const double *fs = snap + (size_t)lane * ldF;
+                double ff = 0.0, fy = 0.0;
+                for (int c = 0; c < m; ++c) {
+                    ff = fma(fs[c], fs[c], ff);
+                    fy = fma(fs[c], sY[c], fy);
+                }
+                ff = fma(fs[m], fs[m], ff);
+                fy = fma(fs[m], ybx_c, fy);
+                const double uw = fy - mw[warp * SW_SNAP + lane];
+                const double den = mk[warp * SW_SNAP + lane] - ff;
+                sse = den > tol ? (uw * uw) / (den + tol) : 0.0;
+                row = srow[lane];
             }
-            ff = fma(fs[m], fs[m], ff);
-            fy = fma(fs[m], ybx_c, fy);
-            const double uw = fy - mw.w[lane];
-            const double den = mw.k01[lane] - ff;
-            sse = den > tol ? (uw * uw) / (den + tol) : 0.0;
-            row = mw.row[lane];
-        }
-        // first maximum in row order (the reference's strict '>' scan)
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double s2 = __shfl_xor_sync(0xffffffffu, sse, o);
-            const int r2 = __shfl_xor_sync(0xffffffffu, row, o);
-            if (s2 > sse || (s2 == sse && r2 < row)) {
-                sse = s2;
-                row = r2;
+            for (int o = 16; o > 0; o >>= 1) {
+                const double s2 = __shfl_xor_sync(0xffffffffu, sse, o);
+                const int r2 = __shfl_xor_sync(0xffffffffu, row, o);
+                if (s2 > sse || (s2 == sse && r2 < row)) {
+                    sse = s2;
+                    row = r2;
+                }
             }
-        }
-        if (sse > best) {
-            best = sse;
-            besti = row;
+            if (sse > best) {
+                best = sse;
+                besti = row;
+            }
         }
         nsnap = 0;
-        __syncwarp();
     };
 
     for (int i0 = 0; i0 < tail; i0 += SW_ROWS) {
         const int rows = min(SW_ROWS, tail - i0);
+        // grid rows in this chunk (block-uniform)
+        int gcount = 0;
+        for (long gr = next_grid; gr < i0 + rows; gr += min_span) {
+            if (gr >= i0) {
+                ++gcount;
+            }
+        }
+        if (nsnap + gcount > SW_SNAP) {
+            flush();
+            __syncthreads();  // slots are reused below
+        }
         if (threadIdx.x < rows) {
             const int r = threadIdx.x, i = i0 + r;
             const int k = pk[i];
             sk[r] = k;
-            sy[r] = y[k];
-            sd[r] = i > 0 ? xs[i - 1] - xs[i] : 0.f;
+            syd[r] = (double)y[k];
+            const double d = i > 0 ? (double)(xs[i - 1] - xs[i]) : 0.0;
+            sd[r] = d;
+            sdd[r] = d * d;
         }
         __syncthreads();
         for (int e = threadIdx.x; e < rows * m; e += blockDim.x) {
             const int r = e / m, c = e % m;
-            sBo[r * ldS + c] = Bo[(size_t)sk[r] * ldbo + c];
+            sBo[r * m + c] = (double)Bo[(size_t)sk[r] * ldbo + c];
         }
-        if (active && lane < rows) {
-            sb[warp][lane] = bcol[sk[lane]];
-            sbx[warp][lane] = bxcol[sk[lane]];
+        for (int e = threadIdx.x; e < task.count * rows; e += blockDim.x) {
+            const int cw = e / rows, r = e % rows;
+            const int cand = task.cand0 + cw;
+            sbd[cw * SW_ROWS + r] = (double)B[(size_t)sk[r] + (size_t)cand_b[cand] * ldB];
+            sbx[cw * SW_ROWS + r] = (double)Bx[(size_t)sk[r] + (size_t)cand * ldBx];
         }
         __syncthreads();
-        if (active) {
+        if (cwarp) {
+            const double *bw = sbd + warp * SW_ROWS, *xw = sbx + warp * SW_ROWS;
+            long ng = next_grid;
+            int slot = nsnap;
             for (int r = 0; r < rows; ++r) {
                 const int i = i0 + r;
-                const double bk = sb[warp][r], bxk = sbx[warp][r], yk = sy[r];
-                const float *rowp = sBo + r * ldS;
-                if (i == 0) {
-                    // covariates_impl<false>(.., k0 = 0, k1 = b_k): g = b_k * row
-#pragma unroll
-                    for (int q = 0; q < CPL; ++q) {
-                        const int c = lane + 32 * q;
-                        const double xv = c < m ? (double)rowp[c] : (c == m ? bxk : 0.0);
-                        f[q] = fma(0.0, g[q], f[q]);
-                        g[q] = fma(bk, xv, g[q]);
-                    }
-                    vb = bk * yk;
-                    b2 = bk * bk;
-                    continue;
-                }
-                const double di = (double)sd[r];
-                const bool on_grid = (i == next_grid);
-                if (on_grid) {
-                    next_grid += min_span;
-                }
+                const double bk = bw[r], bxk = xw[r];
+                const double *rowp = sBo + r * m;
+                const double di = (i == 0) ? 0.0 : sd[r];
 #pragma unroll
                 for (int q = 0; q < CPL; ++q) {
                     const int c = lane + 32 * q;
-                    const double xv = c < m ? (double)rowp[c] : (c == m ? bxk : 0.0);
+                    const double xv = c < m ? rowp[c] : (c == m ? bxk : 0.0);
                     f[q] = fma(di, g[q], f[q]);
                     g[q] = fma(bk, xv, g[q]);
                 }
-                k0 = fma(di * di, b2, k0);
-                k1 = fma(di * 2, bd, k1);
-                w = fma(di, vb, w);
-                bd = fma(di, b2, bd);
-                b2 = fma(bk, bk, b2);
-                vb = fma(yk, bk, vb);
-                if (on_grid) {
-                    double *fs = snap + (size_t)nsnap * ldF;
+                if (i > 0 && i == ng) {
+                    ng += min_span;
+                    double *fs = snap + (size_t)slot * ldF;
 #pragma unroll
                     for (int q = 0; q < CPL; ++q) {
                         const int c = lane + 32 * q;
@@ -361,28 +410,53 @@ __global__ void __launch_bounds__(256)
                             fs[c] = f[q];
                         }
                     }
-                    if (lane == 0) {
-                        mw.k01[nsnap] = k0 + k1;
-                        mw.w[nsnap] = w;
-                        mw.row[nsnap] = i;
+                    if (lane == 0 && warp == 0) {
+                        srow[slot] = i;
                     }
-                    ++nsnap;
-                    if (nsnap == SW_SNAP) {
-                        flush();
-                    }
+                    ++slot;
                 }
+            }
+        } else if (slane) {
+            const double *bw = sbd + lane * SW_ROWS;
+            long ng = next_grid;
+            int slot = nsnap;
+            for (int r = 0; r < rows; ++r) {
+                const int i = i0 + r;
+                const double bk = bw[r], yk = syd[r];
+                if (i == 0) {
+                    vb = bk * yk;
+                    b2 = bk * bk;
+                    continue;
+                }
+                const double di = sd[r];
+                k0 = fma(sdd[r], b2, k0);
+                k1 = fma(di * 2, bd, k1);
+                w = fma(di, vb, w);
+                bd = fma(di, b2, bd);
+                b2 = fma(bk, bk, b2);
+                vb = fma(yk, bk, vb);
+                if (i == ng) {
+                    ng += min_span;
+                    mk[lane * SW_SNAP + slot] = k0 + k1;
+                    mw[lane * SW_SNAP + slot] = w;
+                    ++slot;
+                }
+            }
+        }
+        // advance the block-uniform grid cursor past this chunk
+        for (; next_grid < i0 + rows; next_grid += min_span) {
+            if (next_grid >= 1 && next_grid >= i0) {
+                ++nsnap;
             }
         }
         __syncthreads();
     }
-    if (active) {
-        if (nsnap > 0) {
-            flush();
-        }
-        if (lane == 0) {
-            hsse[cand] = best;
-            hrow[cand] = besti >= 0 ? pk[besti] : -1;
-        }
+    if (nsnap > 0) {
+        flush();
+    }
+    if (cwarp && lane == 0) {
+        hsse[mycand] = best;
+        hrow[mycand] = besti >= 0 ? pk[besti] : -1;
     }
 }
 
@@ -671,7 +745,7 @@ void colchain(cudaStream_t st, const Op &op, int n, int P, double *out, long lon
     if (P <= 0) {
         return;
     }
-    k_colchain<Op><<<(unsigned)ceil_div(P, 64), 64, 0, st>>>(op, n, P, out);
+    k_colchain<Op><<<(unsigned)ceil_div(P, CC_COLS), CC_THREADS, 0, st>>>(op, n, P, out);
     LAUNCH_CHECK();
     *launches += 1;
 }
@@ -739,14 +813,18 @@ void normalize_ybx(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const 
     }
 }
 
-// Warps per sweep block: the snapshot buffers take SW_SNAP * (m+1) doubles
-// per warp; keep the block's shared memory near 200 KB.
+// Candidate warps per sweep block: the snapshot buffers take SW_SNAP * (m+1)
+// doubles per warp; keep the block's shared memory near 200 KB.
+static size_t sweep_smem(int m, int w)
+{
+    return sizeof(double) * ((size_t)w * SW_SNAP * (m + 1) + (size_t)SW_ROWS * m +
+                             2 * (size_t)w * SW_ROWS + (m + 1) + 2 * (size_t)w * SW_SNAP);
+}
+
 int sweep_warps(int m)
 {
-    const size_t per_warp = sizeof(double) * SW_SNAP * (size_t)(m + 1);
-    const size_t fixed = sizeof(double) * (m + 1) + sizeof(float) * SW_ROWS * (size_t)(m | 1);
-    int w = 8;
-    while (w > 1 && fixed + per_warp * w > 200 * 1024) {
+    int w = 4;
+    while (w > 1 && sweep_smem(m, w) > 200 * 1024) {
         --w;
     }
     return w;
@@ -762,17 +840,17 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
         return;
     }
     const int warps = sweep_warps(m);
-    const size_t smem = sizeof(double) * ((size_t)warps * SW_SNAP * (m + 1) + (m + 1)) +
-                        sizeof(float) * SW_ROWS * (size_t)(m | 1);
+    const size_t smem = sweep_smem(m, warps);
+    verify(smem <= 227 * 1024, "the GPU hinge sweep supports at most 430 basis functions");
     const int comps = m + 1;
 #define LAUNCH_SWEEP(CPL)                                                                      \
     do {                                                                                       \
         CUDA_CHECK(cudaFuncSetAttribute(k_sweep<CPL>,                                          \
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,           \
                                         (int)smem));                                           \
-        k_sweep<CPL><<<ntasks, 32 * warps, smem, st>>>(tasks, perm, xsort, y, B, ldB, cand_b,  \
-                                                       Bx, ldBx, Bo, ldbo, ybo, ybx, n, m,     \
-                                                       head, tail, min_span, tol, hsse, hrow); \
+        k_sweep<CPL><<<ntasks, 32 * (warps + 1), smem, st>>>(                                  \
+            tasks, perm, xsort, y, B, ldB, cand_b, Bx, ldBx, Bo, ldbo, ybo, ybx, n, m, head,   \
+            tail, min_span, tol, hsse, hrow);                                                  \
     } while (0)
     if (comps <= 32) {
         LAUNCH_SWEEP(1);
@@ -880,13 +958,17 @@ void append_store(cudaStream_t st, double w, float *Bo, size_t ldbo, float *BoC,
 // sum_i X[i,j]^2 per column as the reference's sequential fused chain
 // (marsalgo.cc:359-369).
 struct XSqChain {
+    static constexpr bool kUsesY = false;
     const float *X;
     size_t ld;
-    __device__ __forceinline__ double operator()(size_t i, int j, double acc) const
+    __device__ __forceinline__ float load(size_t i, int j) const { return X[i + (size_t)j * ld]; }
+    __device__ __forceinline__ float yload(size_t) const { return 0.f; }
+    __device__ __forceinline__ double step(double acc, float v, float) const
     {
-        const double x = (double)X[i + (size_t)j * ld];
+        const double x = (double)v;
         return fma(x, x, acc);
     }
+    __device__ __forceinline__ double finish(double acc, int) const { return acc; }
 };
 
 void column_sumsq(cudaStream_t st, const float *X, size_t ldX, int n, int p, double *out,
