@@ -312,7 +312,7 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
         return;
     }
     std::vector<SweepTask> tasks;
-    const int warps = sweep_warps(m);
+    const int warps = sweep_warps(m, Pc);
     for (int b = 0; b < Pc;) {
         int e = b;
         while (e < Pc && cx_h[c0 + e] == cx_h[c0 + b]) {
@@ -331,7 +331,7 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
     sweep_fp64(a->st, a->tasks.as<SweepTask>(), (int)tasks.size(), a->perm.as<int>(),
                a->xsort.as<float>(), a->y.as<float>(), a->B.as<float>(), a->n, cb_d, Bx, a->n,
                a->Bo.as<float>(), a->ldbo, a->ybo_d.as<double>(), a->ybx.as<double>(), n, m,
-               head, tail, min_span, a->tol, a->hsse.as<double>(), a->hrow.as<int>(),
+               head, tail, min_span, a->tol, a->hsse.as<double>(), a->hrow.as<int>(), warps,
                &a->stats.kernel_launches);
     a->timer.end(PH_SWEEP, t0);
     a->stats.knot_evals += (long long)Pc *

@@ -29,8 +29,8 @@ __global__ void __launch_bounds__(TG_THREADS)
             double *__restrict__ T)
 {
     constexpr int JT = TG_THREADS / KT;
-    __shared__ float sBo[TG_ROWS][KT + 1];
-    __shared__ float sV[TG_ROWS][JT + 1];
+    __shared__ double sBo[TG_ROWS][KT + 1];
+    __shared__ double sV[TG_ROWS][JT + 1];
     const int t = threadIdx.x, kk = t % KT, jj = t / KT;
     const int k0 = blockIdx.x * KT, j0 = blockIdx.y * JT;
     double acc = 0.0;
@@ -38,15 +38,15 @@ __global__ void __launch_bounds__(TG_THREADS)
         const int rows = min(TG_ROWS, n - r0);
         for (int e = t; e < TG_ROWS * KT; e += TG_THREADS) {
             const int rr = e / KT, cc = e % KT;
-            sBo[rr][cc] = (rr < rows && k0 + cc < m) ? Bo[(size_t)(r0 + rr) * ldbo + k0 + cc] : 0.f;
+            sBo[rr][cc] = (rr < rows && k0 + cc < m) ? (double)Bo[(size_t)(r0 + rr) * ldbo + k0 + cc] : 0.0;
         }
         for (int e = t; e < TG_ROWS * JT; e += TG_THREADS) {
             const int rr = e % TG_ROWS, cj = e / TG_ROWS;
-            sV[rr][cj] = (rr < rows && j0 + cj < P) ? src((size_t)(r0 + rr), j0 + cj) : 0.f;
+            sV[rr][cj] = (rr < rows && j0 + cj < P) ? (double)src((size_t)(r0 + rr), j0 + cj) : 0.0;
         }
         __syncthreads();
         for (int rr = 0; rr < rows; ++rr) {
-            acc = fma((double)sBo[rr][kk], (double)sV[rr][jj], acc);
+            acc = fma(sBo[rr][kk], sV[rr][jj], acc);
         }
         __syncthreads();
     }
@@ -67,7 +67,8 @@ struct SqChain {  // sum of squares of the stored f32 column Bx[:, col[j]]
     const float *Bx;
     size_t ld;
     const int *col;
-    __device__ __forceinline__ float load(size_t i, int j) const
+    __device__ __forceinline__ float param(int) const { return 0.f; }
+    __device__ __forceinline__ float load(size_t i, int j, float) const
     {
         return Bx[i + (size_t)(col ? col[j] : j) * ld];
     }
@@ -89,12 +90,17 @@ __global__ void __launch_bounds__(CC_THREADS) k_colchain(Op op, int n, int P, do
     const int j0 = blockIdx.x * CC_COLS;
     const int ncols = min(CC_COLS, P - j0);
     const int ntiles = (n + CC_ROWS - 1) / CC_ROWS;
+    __shared__ float cparam[CC_COLS];
+    if (t < ncols) {
+        cparam[t] = op.param(j0 + t);
+    }
+    __syncthreads();
     auto load = [&](int tl, int b) {
         const int base = tl * CC_ROWS, rows = min(CC_ROWS, n - base);
         for (int e = t - 32; e < ncols * CC_ROWS; e += CC_THREADS - 32) {
             const int c = e / CC_ROWS, r = e % CC_ROWS;
             if (r < rows) {
-                tile[b][c][r] = op.load((size_t)(base + r), j0 + c);
+                tile[b][c][r] = op.load((size_t)(base + r), j0 + c, cparam[c]);
             }
         }
         if (Op::kUsesY) {
@@ -152,19 +158,27 @@ __global__ void __launch_bounds__(PJ_THREADS)
         return;
     }
     const float *bo = Bo + i * ldbo;
+    double proj[PJ_COLS];
+#pragma unroll
+    for (int q = 0; q < PJ_COLS; ++q) {
+        proj[q] = 0.0;
+    }
+    // each column's chain runs over k in order; the conversion of bo[k] is shared
+    for (int k = 0; k < m; ++k) {
+        const double bk = (double)bo[k];
+#pragma unroll
+        for (int q = 0; q < PJ_COLS; ++q) {
+            proj[q] = fma(bk, sT[q * m + k], proj[q]);
+        }
+    }
+#pragma unroll
     for (int q = 0; q < PJ_COLS; ++q) {
         const int j = j0 + q;
-        if (j >= P) {
-            break;
+        if (j < P) {
+            const double v = (double)src(i, j) - proj[q];
+            const int oc = out_col ? out_col[j] : j;
+            Bx[i + (size_t)oc * ldBx] = (float)v;
         }
-        double proj = 0.0;
-        const double *tj = sT + q * m;
-        for (int k = 0; k < m; ++k) {
-            proj = fma((double)bo[k], tj[k], proj);
-        }
-        const double v = (double)src(i, j) - proj;
-        const int oc = out_col ? out_col[j] : j;
-        Bx[i + (size_t)oc * ldBx] = (float)v;
     }
 }
 
@@ -212,9 +226,10 @@ struct NormDotChain {
     const float *y;
     const double *s;
     double tol;
-    __device__ __forceinline__ float load(size_t i, int j) const
+    __device__ __forceinline__ float param(int j) const { return norm_scale(s[j], tol); }
+    __device__ __forceinline__ float load(size_t i, int j, float scale) const
     {
-        return Bx[i + (size_t)j * ld] * norm_scale(s[j], tol);
+        return Bx[i + (size_t)j * ld] * scale;
     }
     __device__ __forceinline__ float yload(size_t i) const { return y[i]; }
     __device__ __forceinline__ double step(double acc, float v, float yv) const
@@ -821,9 +836,13 @@ static size_t sweep_smem(int m, int w)
                              2 * (size_t)w * SW_ROWS + (m + 1) + 2 * (size_t)w * SW_SNAP);
 }
 
-int sweep_warps(int m)
+int sweep_warps(int m, int candidates)
 {
+    // enough blocks to cover two per SM when the epoch has few candidates
     int w = 4;
+    while (w > 2 && (candidates + w - 1) / w < 2 * 152) {
+        --w;
+    }
     while (w > 1 && sweep_smem(m, w) > 200 * 1024) {
         --w;
     }
@@ -834,12 +853,13 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
                 const float *xsort, const float *y, const float *B, size_t ldB,
                 const int *cand_b, const float *Bx, size_t ldBx, const float *Bo, size_t ldbo,
                 const double *ybo, const double *ybx, int n, int m, int head, int tail,
-                int min_span, double tol, double *hsse, int *hrow, long long *launches)
+                int min_span, double tol, double *hsse, int *hrow, int warps_per_block,
+                long long *launches)
 {
     if (ntasks <= 0) {
         return;
     }
-    const int warps = sweep_warps(m);
+    const int warps = warps_per_block;
     const size_t smem = sweep_smem(m, warps);
     verify(smem <= 227 * 1024, "the GPU hinge sweep supports at most 430 basis functions");
     const int comps = m + 1;
@@ -961,7 +981,8 @@ struct XSqChain {
     static constexpr bool kUsesY = false;
     const float *X;
     size_t ld;
-    __device__ __forceinline__ float load(size_t i, int j) const { return X[i + (size_t)j * ld]; }
+    __device__ __forceinline__ float param(int) const { return 0.f; }
+    __device__ __forceinline__ float load(size_t i, int j, float) const { return X[i + (size_t)j * ld]; }
     __device__ __forceinline__ float yload(size_t) const { return 0.f; }
     __device__ __forceinline__ double step(double acc, float v, float) const
     {

@@ -76,8 +76,9 @@ void dgks_gate(cudaStream_t st, const double *T, int m, int P, const double *s, 
 void normalize_ybx(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const double *s,
                    double tol, const float *y, bool store, double *ybx, long long *launches);
 
-// Candidates per hinge-sweep block (one warp each) for m live basis columns.
-int sweep_warps(int m);
+// Candidates per hinge-sweep block (one warp each) for m live basis columns
+// and `candidates` candidates in the launch.
+int sweep_warps(int m, int candidates);
 
 // Hinge sweep in FP64 (marsalgo.cc:508-657), one warp per candidate; tasks
 // hold at most sweep_warps(m) candidates.
@@ -85,7 +86,8 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
                 const float *xsort, const float *y, const float *B, size_t ldB,
                 const int *cand_b, const float *Bx, size_t ldBx, const float *Bo, size_t ldbo,
                 const double *ybo, const double *ybx, int n, int m, int head, int tail,
-                int min_span, double tol, double *hsse, int *hrow, long long *launches);
+                int min_span, double tol, double *hsse, int *hrow, int warps_per_block,
+                long long *launches);
 
 // Stable descending argsort of X columns (marsalgo.cc:33-39) and the scaled
 // sorted values xsort[i] = X[perm[i]] * s.
