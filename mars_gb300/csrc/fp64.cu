@@ -265,22 +265,54 @@ __global__ void __launch_bounds__(NM_THREADS)
 // FP64 hinge sweep (marsalgo.cc:576-649 with covariates_impl :91-151), in the
 // reference's operation order.
 //
-// Block = one input column and up to W candidates (parent columns): warps
-// 0..W-1 each own one candidate, lane l holding components c = l + 32 q of the
-// running f and g (component m is the candidate column Bx itself); warp W runs
-// the six scalar recurrences (k0, k1, w, bd, b2, vb) for all W candidates at
-// once, one lane per candidate. Sorted rows are staged SW_ROWS at a time as
-// doubles (converted once per block): permutation, delta, delta^2, y, the
-// gathered Bo rows, and B and Bx of every candidate. At a grid row each
-// candidate warp saves f in a snapshot slot and the scalar warp saves k0+k1
-// and w; once SW_SNAP slots are in use, lane q of each candidate warp scores
-// slot q with the reference's sequential chains ff = sum_c f_c^2 and
-// fy = sum_c f_c yc_c (c = 0..m), and the warp keeps the first maximum.
+// Block = one input column and up to W candidates (parent columns):
+//   warps 0..W-1  one candidate each; lane l holds components c = l + 32 q of
+//                 the running f and g (component m is the candidate column Bx)
+//   warp  W       the six scalar recurrences (k0, k1, w, bd, b2, vb) of all W
+//                 candidates, one lane per candidate
+//   warp  W+1     the loader: stages the next SW_ROWS sorted rows as doubles
+//                 (permutation, delta, delta^2, y, the gathered Bo rows, B and
+//                 Bx of every candidate) into the other half of a double buffer
+// At a grid row each candidate warp saves f in a snapshot slot and the scalar
+// warp saves k0 + k1 and w; when SW_SNAP slots are in use, lane q of each
+// candidate warp scores slot q with the reference's sequential chains
+// ff = sum_c f_c^2 and fy = sum_c f_c yc_c (c = 0..m) and the warp keeps the
+// first maximum in row order.
 // ---------------------------------------------------------------------------
 constexpr int SW_ROWS = 32, SW_SNAP = 32, SW_MAXW = 8;
 
+struct SweepSmem {
+    // offsets (in doubles) into the dynamic shared memory
+    size_t snap, bo, bd, bx, d, dd, yd, ybo, mk, mw, total;
+    __host__ __device__ SweepSmem(int m, int W)
+    {
+        size_t o = 0;
+        snap = o;
+        o += (size_t)W * SW_SNAP * (m + 1);
+        bo = o;
+        o += 2 * (size_t)SW_ROWS * m;
+        bd = o;
+        o += 2 * (size_t)W * SW_ROWS;
+        bx = o;
+        o += 2 * (size_t)W * SW_ROWS;
+        d = o;
+        o += 2 * SW_ROWS;
+        dd = o;
+        o += 2 * SW_ROWS;
+        yd = o;
+        o += 2 * SW_ROWS;
+        ybo = o;
+        o += (size_t)m + 1;
+        mk = o;
+        o += (size_t)W * SW_SNAP;
+        mw = o;
+        o += (size_t)W * SW_SNAP;
+        total = o;
+    }
+};
+
 template <int CPL>
-__global__ void __launch_bounds__(32 * (SW_MAXW + 1))
+__global__ void __launch_bounds__(32 * (SW_MAXW + 2))
     k_sweep(const SweepTask *__restrict__ tasks, const int *__restrict__ perm,
             const float *__restrict__ xsort, const float *__restrict__ y,
             const float *__restrict__ B, size_t ldB, const int *__restrict__ cand_b,
@@ -290,39 +322,58 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1))
             int *__restrict__ hrow)
 {
     extern __shared__ double dyn[];
-    const int W = (blockDim.x >> 5) - 1;  // candidate warps
+    const int W = (blockDim.x >> 5) - 2;  // candidate warps
+    const SweepSmem L(m, W);
     const int ldF = m + 1;
-    double *snap_all = dyn;                                 // W * SW_SNAP * ldF
-    double *sBo = snap_all + (size_t)W * SW_SNAP * ldF;     // SW_ROWS * m (Bo rows, doubles)
-    double *sbd = sBo + (size_t)SW_ROWS * m;                // W * SW_ROWS (B of each candidate)
-    double *sbx = sbd + (size_t)W * SW_ROWS;                // W * SW_ROWS (Bx of each candidate)
-    double *sY = sbx + (size_t)W * SW_ROWS;                 // m + 1 (ybo, then unused)
-    double *mk = sY + (m + 1);                              // W * SW_SNAP (k0 + k1)
-    double *mw = mk + (size_t)W * SW_SNAP;                  // W * SW_SNAP (w)
-    __shared__ int sk[SW_ROWS];
-    __shared__ double sd[SW_ROWS], sdd[SW_ROWS], syd[SW_ROWS];
     __shared__ int srow[SW_SNAP];
 
     const SweepTask task = tasks[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bool cwarp = warp < task.count;           // an active candidate warp
-    const bool swarp = warp == W;                   // the scalar warp
+    const bool cwarp = warp < task.count;
+    const bool swarp = warp == W;
+    const bool lwarp = warp == W + 1;
     const int *pk = perm + (size_t)task.xcol * n;
     const float *xs = xsort + (size_t)task.xcol * n;
 
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
-        sY[c] = ybo[c];
+        dyn[L.ybo + c] = ybo[c];
     }
+    // The loader stages rows [i0, i0 + rows) into buffer half h.
+    auto stage = [&](int i0, int h) {
+        const int rows = min(SW_ROWS, tail - i0);
+        int k = 0;
+        if (lane < rows) {
+            const int i = i0 + lane;
+            k = pk[i];
+            dyn[L.yd + h * SW_ROWS + lane] = (double)y[k];
+            const double d = i > 0 ? (double)(xs[i - 1] - xs[i]) : 0.0;
+            dyn[L.d + h * SW_ROWS + lane] = d;
+            dyn[L.dd + h * SW_ROWS + lane] = d * d;
+            const float *row = Bo + (size_t)k * ldbo;
+            double *dst = dyn + L.bo + ((size_t)h * SW_ROWS + lane) * m;
+            for (int c = 0; c < m; ++c) {
+                dst[c] = (double)row[c];
+            }
+            for (int cw = 0; cw < task.count; ++cw) {
+                const int cand = task.cand0 + cw;
+                dyn[L.bd + (h * W + cw) * SW_ROWS + lane] =
+                    (double)B[(size_t)k + (size_t)cand_b[cand] * ldB];
+                dyn[L.bx + (h * W + cw) * SW_ROWS + lane] =
+                    (double)Bx[(size_t)k + (size_t)cand * ldBx];
+            }
+        }
+    };
+
     const int mycand = task.cand0 + (cwarp ? warp : 0);
     const double ybx_c = ybx[mycand];
-    double *snap = snap_all + (size_t)(cwarp ? warp : 0) * SW_SNAP * ldF;
+    double *snap = dyn + L.snap + (size_t)(cwarp ? warp : 0) * SW_SNAP * ldF;
+    double *mk = dyn + L.mk, *mw = dyn + L.mw;
     double f[CPL], g[CPL];
 #pragma unroll
     for (int q = 0; q < CPL; ++q) {
         f[q] = 0.0;
         g[q] = 0.0;
     }
-    // scalar-warp state: lane = candidate
     const bool slane = swarp && lane < task.count;
     double k0 = 0, k1 = 0, w = 0, bd = 0, vb = 0, b2 = 0;
     double best = 0.0;
@@ -336,10 +387,11 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1))
             int row = 0x7fffffff;
             if (lane < nsnap) {
                 const double *fs = snap + (size_t)lane * ldF;
+                const double *yb = dyn + L.ybo;
                 double ff = 0.0, fy = 0.0;
                 for (int c = 0; c < m; ++c) {
                     ff = fma(fs[c], fs[c], ff);
-                    fy = fma(fs[c], sY[c], fy);
+                    fy = fma(fs[c], yb[c], fy);
                 }
                 ff = fma(fs[m], fs[m], ff);
                 fy = fma(fs[m], ybx_c, fy);
@@ -365,49 +417,33 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1))
         nsnap = 0;
     };
 
-    for (int i0 = 0; i0 < tail; i0 += SW_ROWS) {
+    if (lwarp && tail > 0) {
+        stage(0, 0);
+    }
+    __syncthreads();
+    int h = 0;
+    for (int i0 = 0; i0 < tail; i0 += SW_ROWS, h ^= 1) {
         const int rows = min(SW_ROWS, tail - i0);
-        // grid rows in this chunk (block-uniform)
         int gcount = 0;
         for (long gr = next_grid; gr < i0 + rows; gr += min_span) {
-            if (gr >= i0) {
-                ++gcount;
-            }
+            ++gcount;
         }
         if (nsnap + gcount > SW_SNAP) {
             flush();
-            __syncthreads();  // slots are reused below
+            __syncthreads();  // slots are rewritten below
         }
-        if (threadIdx.x < rows) {
-            const int r = threadIdx.x, i = i0 + r;
-            const int k = pk[i];
-            sk[r] = k;
-            syd[r] = (double)y[k];
-            const double d = i > 0 ? (double)(xs[i - 1] - xs[i]) : 0.0;
-            sd[r] = d;
-            sdd[r] = d * d;
-        }
-        __syncthreads();
-        for (int e = threadIdx.x; e < rows * m; e += blockDim.x) {
-            const int r = e / m, c = e % m;
-            sBo[r * m + c] = (double)Bo[(size_t)sk[r] * ldbo + c];
-        }
-        for (int e = threadIdx.x; e < task.count * rows; e += blockDim.x) {
-            const int cw = e / rows, r = e % rows;
-            const int cand = task.cand0 + cw;
-            sbd[cw * SW_ROWS + r] = (double)B[(size_t)sk[r] + (size_t)cand_b[cand] * ldB];
-            sbx[cw * SW_ROWS + r] = (double)Bx[(size_t)sk[r] + (size_t)cand * ldBx];
-        }
-        __syncthreads();
         if (cwarp) {
-            const double *bw = sbd + warp * SW_ROWS, *xw = sbx + warp * SW_ROWS;
+            const double *bw = dyn + L.bd + (h * W + warp) * SW_ROWS;
+            const double *xw = dyn + L.bx + (h * W + warp) * SW_ROWS;
+            const double *sd = dyn + L.d + h * SW_ROWS;
+            const double *rowb = dyn + L.bo + (size_t)h * SW_ROWS * m;
             long ng = next_grid;
             int slot = nsnap;
             for (int r = 0; r < rows; ++r) {
                 const int i = i0 + r;
                 const double bk = bw[r], bxk = xw[r];
-                const double *rowp = sBo + r * m;
-                const double di = (i == 0) ? 0.0 : sd[r];
+                const double *rowp = rowb + r * m;
+                const double di = sd[r];  // 0 for the first row
 #pragma unroll
                 for (int q = 0; q < CPL; ++q) {
                     const int c = lane + 32 * q;
@@ -415,7 +451,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1))
                     f[q] = fma(di, g[q], f[q]);
                     g[q] = fma(bk, xv, g[q]);
                 }
-                if (i > 0 && i == ng) {
+                if (i == ng) {
                     ng += min_span;
                     double *fs = snap + (size_t)slot * ldF;
 #pragma unroll
@@ -432,7 +468,10 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1))
                 }
             }
         } else if (slane) {
-            const double *bw = sbd + lane * SW_ROWS;
+            const double *bw = dyn + L.bd + (h * W + lane) * SW_ROWS;
+            const double *sd = dyn + L.d + h * SW_ROWS;
+            const double *sdd = dyn + L.dd + h * SW_ROWS;
+            const double *syd = dyn + L.yd + h * SW_ROWS;
             long ng = next_grid;
             int slot = nsnap;
             for (int r = 0; r < rows; ++r) {
@@ -457,13 +496,11 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1))
                     ++slot;
                 }
             }
+        } else if (lwarp && i0 + SW_ROWS < tail) {
+            stage(i0 + SW_ROWS, h ^ 1);
         }
-        // advance the block-uniform grid cursor past this chunk
-        for (; next_grid < i0 + rows; next_grid += min_span) {
-            if (next_grid >= 1 && next_grid >= i0) {
-                ++nsnap;
-            }
-        }
+        nsnap += gcount;
+        next_grid += (long)gcount * min_span;
         __syncthreads();
     }
     if (nsnap > 0) {
@@ -828,17 +865,12 @@ void normalize_ybx(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const 
     }
 }
 
-// Candidate warps per sweep block: the snapshot buffers take SW_SNAP * (m+1)
-// doubles per warp; keep the block's shared memory near 200 KB.
-static size_t sweep_smem(int m, int w)
-{
-    return sizeof(double) * ((size_t)w * SW_SNAP * (m + 1) + (size_t)SW_ROWS * m +
-                             2 * (size_t)w * SW_ROWS + (m + 1) + 2 * (size_t)w * SW_SNAP);
-}
+// Candidate warps per sweep block: at most 4, fewer when the launch has few
+// candidates (two blocks per SM) or the snapshots would not fit.
+static size_t sweep_smem(int m, int w) { return sizeof(double) * SweepSmem(m, w).total; }
 
 int sweep_warps(int m, int candidates)
 {
-    // enough blocks to cover two per SM when the epoch has few candidates
     int w = 4;
     while (w > 2 && (candidates + w - 1) / w < 2 * 152) {
         --w;
@@ -868,7 +900,7 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
         CUDA_CHECK(cudaFuncSetAttribute(k_sweep<CPL>,                                          \
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,           \
                                         (int)smem));                                           \
-        k_sweep<CPL><<<ntasks, 32 * (warps + 1), smem, st>>>(                                  \
+        k_sweep<CPL><<<ntasks, 32 * (warps + 2), smem, st>>>(                                  \
             tasks, perm, xsort, y, B, ldB, cand_b, Bx, ldBx, Bo, ldbo, ybo, ybx, n, m, head,   \
             tail, min_span, tol, hsse, hrow);                                                  \
     } while (0)
