@@ -29,24 +29,66 @@ __global__ void __launch_bounds__(TG_THREADS)
             double *__restrict__ T)
 {
     constexpr int JT = TG_THREADS / KT;
-    __shared__ double sBo[TG_ROWS][KT + 1];
-    __shared__ double sV[TG_ROWS][JT + 1];
+    __shared__ double sBo[2][TG_ROWS][KT + 1];
+    __shared__ double sV[2][TG_ROWS][JT + 1];
     const int t = threadIdx.x, kk = t % KT, jj = t / KT;
     const int k0 = blockIdx.x * KT, j0 = blockIdx.y * JT;
-    double acc = 0.0;
-    for (int r0 = 0; r0 < n; r0 += TG_ROWS) {
+    // Rows of the next tile are loaded into registers before the current tile's
+    // chain steps, and stored to the other half after them.
+    constexpr int NB = (TG_ROWS * KT + TG_THREADS - 1) / TG_THREADS;
+    constexpr int NV = (TG_ROWS * JT + TG_THREADS - 1) / TG_THREADS;
+    double rb[NB], rv[NV];
+    auto fetch = [&](int r0) {
         const int rows = min(TG_ROWS, n - r0);
-        for (int e = t; e < TG_ROWS * KT; e += TG_THREADS) {
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int e = t + q * TG_THREADS;
             const int rr = e / KT, cc = e % KT;
-            sBo[rr][cc] = (rr < rows && k0 + cc < m) ? (double)Bo[(size_t)(r0 + rr) * ldbo + k0 + cc] : 0.0;
+            rb[q] = (e < TG_ROWS * KT && rr < rows && k0 + cc < m)
+                        ? (double)Bo[(size_t)(r0 + rr) * ldbo + k0 + cc] : 0.0;
         }
-        for (int e = t; e < TG_ROWS * JT; e += TG_THREADS) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            const int e = t + q * TG_THREADS;
             const int rr = e % TG_ROWS, cj = e / TG_ROWS;
-            sV[rr][cj] = (rr < rows && j0 + cj < P) ? (double)src((size_t)(r0 + rr), j0 + cj) : 0.0;
+            rv[q] = (e < TG_ROWS * JT && rr < rows && j0 + cj < P)
+                        ? (double)src((size_t)(r0 + rr), j0 + cj) : 0.0;
         }
-        __syncthreads();
+    };
+    auto put = [&](int h) {
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int e = t + q * TG_THREADS;
+            if (e < TG_ROWS * KT) {
+                sBo[h][e / KT][e % KT] = rb[q];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            const int e = t + q * TG_THREADS;
+            if (e < TG_ROWS * JT) {
+                sV[h][e % TG_ROWS][e / TG_ROWS] = rv[q];
+            }
+        }
+    };
+    double acc = 0.0;
+    if (n > 0) {
+        fetch(0);
+        put(0);
+    }
+    __syncthreads();
+    int h = 0;
+    for (int r0 = 0; r0 < n; r0 += TG_ROWS, h ^= 1) {
+        const int rows = min(TG_ROWS, n - r0);
+        const bool more = r0 + TG_ROWS < n;
+        if (more) {
+            fetch(r0 + TG_ROWS);
+        }
         for (int rr = 0; rr < rows; ++rr) {
-            acc = fma(sBo[rr][kk], sV[rr][jj], acc);
+            acc = fma(sBo[h][rr][kk], sV[h][rr][jj], acc);
+        }
+        if (more) {
+            put(h ^ 1);
         }
         __syncthreads();
     }
@@ -57,7 +99,7 @@ __global__ void __launch_bounds__(TG_THREADS)
 
 // Column chains: warp 0 of a block runs 32 column chains (lane = column) out
 // of shared memory while warps 1..3 stage the next tile of rows.
-constexpr int CC_COLS = 32, CC_ROWS = 128, CC_THREADS = 128;
+constexpr int CC_COLS = 32, CC_ROWS = 64, CC_THREADS = 128;
 
 // Fused chains over the rows i = 0..n-1 in order: the reference's sequential
 // f64 accumulations (kernels.cc:361-366 norm of the stored column;
@@ -73,10 +115,9 @@ struct SqChain {  // sum of squares of the stored f32 column Bx[:, col[j]]
         return Bx[i + (size_t)(col ? col[j] : j) * ld];
     }
     __device__ __forceinline__ float yload(size_t) const { return 0.f; }
-    __device__ __forceinline__ double step(double acc, float v, float) const
+    __device__ __forceinline__ double step(double acc, double v, double) const
     {
-        const double d = (double)v;
-        return fma(d, d, acc);
+        return fma(v, v, acc);
     }
     __device__ __forceinline__ double finish(double acc, int) const { return acc; }
 };
@@ -84,8 +125,8 @@ struct SqChain {  // sum of squares of the stored f32 column Bx[:, col[j]]
 template <class Op>
 __global__ void __launch_bounds__(CC_THREADS) k_colchain(Op op, int n, int P, double *__restrict__ out)
 {
-    __shared__ float tile[2][CC_COLS][CC_ROWS + 1];
-    __shared__ float ytile[2][CC_ROWS];
+    __shared__ double tile[2][CC_COLS][CC_ROWS + 1];
+    __shared__ double ytile[2][CC_ROWS];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int j0 = blockIdx.x * CC_COLS;
     const int ncols = min(CC_COLS, P - j0);
@@ -100,12 +141,12 @@ __global__ void __launch_bounds__(CC_THREADS) k_colchain(Op op, int n, int P, do
         for (int e = t - 32; e < ncols * CC_ROWS; e += CC_THREADS - 32) {
             const int c = e / CC_ROWS, r = e % CC_ROWS;
             if (r < rows) {
-                tile[b][c][r] = op.load((size_t)(base + r), j0 + c, cparam[c]);
+                tile[b][c][r] = (double)op.load((size_t)(base + r), j0 + c, cparam[c]);
             }
         }
         if (Op::kUsesY) {
             for (int r = t - 32; r < rows; r += CC_THREADS - 32) {
-                ytile[b][r] = op.yload((size_t)(base + r));
+                ytile[b][r] = (double)op.yload((size_t)(base + r));
             }
         }
     };
@@ -232,9 +273,9 @@ struct NormDotChain {
         return Bx[i + (size_t)j * ld] * scale;
     }
     __device__ __forceinline__ float yload(size_t i) const { return y[i]; }
-    __device__ __forceinline__ double step(double acc, float v, float yv) const
+    __device__ __forceinline__ double step(double acc, double v, double yv) const
     {
-        return fma((double)v, (double)yv, acc);
+        return fma(v, yv, acc);
     }
     __device__ __forceinline__ double finish(double acc, int) const { return acc; }
 };
@@ -763,7 +804,7 @@ void tgemm_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, i
     if (P <= 0 || m <= 0) {
         return;
     }
-    int kt = 1;
+    int kt = 4;  // narrower tiles would need more than 48 KB of static shared memory
     while (kt < m && kt < 32) {
         kt *= 2;
     }
@@ -774,8 +815,6 @@ void tgemm_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, i
         k_tgemm<Src, K><<<dim3(gx, gy), TG_THREADS, 0, st>>>(src, Bo, ldbo, n, m, P, T); \
         break;
     switch (kt) {
-        TG_CASE(1)
-        TG_CASE(2)
         TG_CASE(4)
         TG_CASE(8)
         TG_CASE(16)
@@ -1016,10 +1055,9 @@ struct XSqChain {
     __device__ __forceinline__ float param(int) const { return 0.f; }
     __device__ __forceinline__ float load(size_t i, int j, float) const { return X[i + (size_t)j * ld]; }
     __device__ __forceinline__ float yload(size_t) const { return 0.f; }
-    __device__ __forceinline__ double step(double acc, float v, float) const
+    __device__ __forceinline__ double step(double acc, double v, double) const
     {
-        const double x = (double)v;
-        return fma(x, x, acc);
+        return fma(v, v, acc);
     }
     __device__ __forceinline__ double finish(double acc, int) const { return acc; }
 };
