@@ -40,6 +40,12 @@ int guarded(F &&f)
     }
 }
 
+}  // namespace
+
+void mgpu::set_last_error(const std::string &msg) { g_last_error = msg; }
+
+namespace {
+
 double env_double(const char *name, double dflt)
 {
     const char *v = std::getenv(name);

@@ -12,6 +12,9 @@ struct Error : std::runtime_error {
     Error(int st, const std::string &msg) : std::runtime_error(msg), status(st) {}
 };
 
+// Records the message returned by mars_gpu_last_error() on this thread.
+void set_last_error(const std::string &msg);
+
 inline void verify(bool ok, const char *msg, int status = 1)
 {
     if (!ok) {

@@ -904,6 +904,19 @@ void normalize_ybx(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const 
     }
 }
 
+void scale_columns(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const double *s,
+                   double tol, long long *launches)
+{
+    if (P <= 0) {
+        return;
+    }
+    verify(ceil_div(P, NM_COLS) <= 65535, "too many candidate columns for one launch", 2);
+    k_scale<<<dim3((unsigned)ceil_div(n, NM_THREADS), (unsigned)ceil_div(P, NM_COLS)), NM_THREADS,
+              0, st>>>(Bx, ldBx, n, P, s, tol);
+    LAUNCH_CHECK();
+    *launches += 1;
+}
+
 // Candidate warps per sweep block: at most 4, fewer when the launch has few
 // candidates (two blocks per SM) or the snapshots would not fit.
 static size_t sweep_smem(int m, int w) { return sizeof(double) * SweepSmem(m, w).total; }

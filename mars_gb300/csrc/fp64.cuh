@@ -76,6 +76,10 @@ void dgks_gate(cudaStream_t st, const double *T, int m, int P, const double *s, 
 void normalize_ybx(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const double *s,
                    double tol, const float *y, bool store, double *ybx, long long *launches);
 
+// Bx[:, j] *= scale(s[j]) for j < P, the scaling step of normalize_ybx alone.
+void scale_columns(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const double *s,
+                   double tol, long long *launches);
+
 // Candidates per hinge-sweep block (one warp each) for m live basis columns
 // and `candidates` candidates in the launch.
 int sweep_warps(int m, int candidates);

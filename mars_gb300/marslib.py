@@ -78,6 +78,8 @@ def load():
         "mars_gpu_orth_error": (i, [vp, dp, dp]),
         "mars_gpu_orthonormalize": (i, [sz, sz, sz, fp, sz, fp, ip, fp, sz, fp, sz, dp, d, lp]),
         "mars_gpu_orthonormalize_col": (i, [sz, sz, dp, fp, sz, d, dp, lp]),
+        "mars_gpu_orthonormalize_noalloc": (i, [sz, sz, sz, vp, sz, vp, ip, vp, sz, vp, sz, vp,
+                                                d, vp, lp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -248,3 +250,24 @@ def orthonormalize_col(v, Bo, m, tol):
     check(L.mars_gpu_orthonormalize_col(len(v), m, _p(v, ctypes.c_double), _p(Bo, ctypes.c_float),
                                         Bo.shape[1], tol, ctypes.byref(w), ctypes.byref(c)))
     return w.value, v, c.value
+
+
+# Limits of the fixed scratch of mars_gpu_orthonormalize_noalloc (mars_gpu.h).
+NOALLOC_MAX_CANDIDATES = 4096
+NOALLOC_MAX_COEFS = 262144
+
+
+def orthonormalize_noalloc(n, m, mask, B_ptr, ldB, x_ptr, Bo_ptr, ldBo, Bx_ptr, ldBx, s_ptr, tol,
+                           stream_ptr=0):
+    """mars_gpu_orthonormalize on caller-owned device arrays (integer device
+    addresses), queued on `stream_ptr` (a cudaStream_t; 0 = default stream),
+    with no device allocation. mask is a host int array of parent columns.
+    Returns the number of columns DGKS retried."""
+    L = load()
+    mask = np.ascontiguousarray(mask, dtype=np.int32)
+    c = ctypes.c_long(0)
+    check(L.mars_gpu_orthonormalize_noalloc(n, m, len(mask), B_ptr, ldB, x_ptr,
+                                            _p(mask, ctypes.c_int), Bo_ptr, ldBo, Bx_ptr, ldBx,
+                                            s_ptr or None, tol, stream_ptr or None,
+                                            ctypes.byref(c)))
+    return c.value
