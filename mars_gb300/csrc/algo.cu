@@ -160,12 +160,13 @@ void span_mark_end(mars_gpu_algo *a)
 }
 
 
-__global__ void k_col_to_rows(const float *__restrict__ col, int n, float *__restrict__ Bo,
+// Column c of the f64 row-major basis copy from the f32 column (exact widening).
+__global__ void k_col_to_rows(const float *__restrict__ col, int n, double *__restrict__ Bo,
                               size_t ldbo, int c)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        Bo[(size_t)i * ldbo + c] = col[i];
+        Bo[(size_t)i * ldbo + c] = (double)col[i];
     }
 }
 
@@ -209,14 +210,14 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
                                cudaMemcpyHostToDevice, a->st));
     a->B.ensure(sizeof(float) * n * max_terms);
     a->BoC.ensure(sizeof(float) * n * max_terms);
-    a->Bo.ensure(sizeof(float) * n * a->ldbo);
-    CUDA_CHECK(cudaMemsetAsync(a->Bo.ptr, 0, sizeof(float) * n * a->ldbo, a->st));
+    a->Bo.ensure(sizeof(double) * n * a->ldbo);
+    CUDA_CHECK(cudaMemsetAsync(a->Bo.ptr, 0, sizeof(double) * n * a->ldbo, a->st));
     CUDA_CHECK(cudaMemcpyAsync(a->B.ptr, a->hb.B.data(), sizeof(float) * n,
                                cudaMemcpyHostToDevice, a->st));
     CUDA_CHECK(cudaMemcpyAsync(a->BoC.ptr, a->hb.BoC.data(), sizeof(float) * n,
                                cudaMemcpyHostToDevice, a->st));
     k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(a->BoC.as<float>(), (int)n,
-                                                                a->Bo.as<float>(), a->ldbo, 0);
+                                                                a->Bo.as<double>(), a->ldbo, 0);
     LAUNCH_CHECK();
     a->ybo_d.ensure(sizeof(double) * max_terms);
     CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.ptr, &a->ybo[0], sizeof(double), cudaMemcpyHostToDevice,
@@ -289,7 +290,7 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
     a->stats.project_flops += 4.0 * (double)n * (double)m * (double)Pc;
     cudaEvent_t t0 = a->timer.begin();
     FillSrc src{a->B.as<float>(), a->n, a->X.as<float>(), a->n, a->s.as<float>(), cx_d, cb_d};
-    project_fp64(a->st, src, a->Bo.as<float>(), a->ldbo, n, m, Pc, nullptr, Bx, a->n, s, ws,
+    project_fp64(a->st, src, a->Bo.as<double>(), a->ldbo, n, m, Pc, nullptr, Bx, a->n, s, ws,
                  &a->stats.kernel_launches);
     a->timer.end(PH_PROJECT, t0);
 
@@ -301,7 +302,7 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
     sync(a);
     if (nf > 0) {
         StoredSrc src2{Bx, a->n, a->fired.as<int>()};
-        project_fp64(a->st, src2, a->Bo.as<float>(), a->ldbo, n, m, nf, a->fired.as<int>(), Bx,
+        project_fp64(a->st, src2, a->Bo.as<double>(), a->ldbo, n, m, nf, a->fired.as<int>(), Bx,
                      a->n, a->snew.as<double>(), ws, &a->stats.kernel_launches);
         scatter_s(a->st, a->fired.as<int>(), nf, a->snew.as<double>(), s,
                   &a->stats.kernel_launches);
@@ -336,7 +337,7 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
     t0 = a->timer.begin();
     sweep_fp64(a->st, a->tasks.as<SweepTask>(), (int)tasks.size(), a->perm.as<int>(),
                a->xsort.as<float>(), a->y.as<float>(), a->B.as<float>(), a->n, cb_d, Bx, a->n,
-               a->Bo.as<float>(), a->ldbo, a->ybo_d.as<double>(), a->ybx.as<double>(), n, m,
+               a->Bo.as<double>(), a->ldbo, a->ybo_d.as<double>(), a->ybx.as<double>(), n, m,
                head, tail, min_span, a->tol, a->hsse.as<double>(), a->hrow.as<int>(), warps,
                &a->stats.kernel_launches);
     a->timer.end(PH_SWEEP, t0);
@@ -459,7 +460,7 @@ double append_impl(mars_gpu_algo *a, char type, int xcol, int bcol, float h)
         CUDA_CHECK(cudaMemcpyAsync(a->BoC.as<float>() + m * n, a->hb.BoC.data() + m * n,
                                    sizeof(float) * n, cudaMemcpyHostToDevice, a->st));
         k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(
-            a->BoC.as<float>() + m * n, (int)n, a->Bo.as<float>(), a->ldbo, (int)m);
+            a->BoC.as<float>() + m * n, (int)n, a->Bo.as<double>(), a->ldbo, (int)m);
         LAUNCH_CHECK();
         a->stats.kernel_launches += 1;
         CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.as<double>() + m, &a->hb.ybo[m], sizeof(double),
@@ -622,13 +623,13 @@ int mars_gpu_orth_error(mars_gpu_algo *a, double *max_abs, double *rss)
         DevBuf T;
         T.ensure(sizeof(double) * (size_t)m * (m + 1));
         StoredSrc q{a->BoC.as<float>(), a->n, nullptr};
-        tgemm_fp64(a->st, q, a->Bo.as<float>(), a->ldbo, n, m, m, T.as<double>(),
+        tgemm_fp64(a->st, q, a->Bo.as<double>(), a->ldbo, n, m, m, T.as<double>(),
                    &a->stats.kernel_launches);
         std::vector<double> G((size_t)m * m);
         CUDA_CHECK(cudaMemcpyAsync(G.data(), T.ptr, sizeof(double) * m * m,
                                    cudaMemcpyDeviceToHost, a->st));
         StoredSrc yy{a->y.as<float>(), a->n, nullptr};
-        tgemm_fp64(a->st, yy, a->Bo.as<float>(), a->ldbo, n, m, 1, T.as<double>(),
+        tgemm_fp64(a->st, yy, a->Bo.as<double>(), a->ldbo, n, m, 1, T.as<double>(),
                    &a->stats.kernel_launches);
         std::vector<double> r(m);
         CUDA_CHECK(cudaMemcpyAsync(r.data(), T.ptr, sizeof(double) * m, cudaMemcpyDeviceToHost,

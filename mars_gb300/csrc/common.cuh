@@ -64,6 +64,35 @@ struct DevBuf {
 };
 
 // ---------------------------------------------------------------------------
+// Asynchronous global -> shared copies (cp.async, sm_80+). A copy with
+// `valid` false writes zero and reads nothing.
+// ---------------------------------------------------------------------------
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem, bool valid = true)
+{
+    static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async size");
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    const int bytes = valid ? BYTES : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s), "l"(gmem), "n"(BYTES),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem, bool valid = true)
+{
+    cp_async<4>(smem, gmem, valid);
+}
+__device__ __forceinline__ void cp_async_commit()
+{
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// Wait until at most N of this thread's committed groups are pending.
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Deterministic block reductions (fixed tree order for a fixed block size).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v)

@@ -18,78 +18,129 @@ namespace {
 // T = Bo^T Bx with every entry accumulated over the rows in order
 // i = 0..n-1 by one fused-multiply-add chain, which is the reference's order
 // (kernels.cc:327-335: tc[k] += bo_row[k] * bx[i], rows outermost). The block
-// tile is KT components x (128 / KT) columns, one accumulator per thread; the
-// rows are staged 32 at a time in shared memory.
+// tile is KT components x (128 / KT) columns, one chain per thread.
+//
+// GB300's FP64 pipe issues one warp instruction per ~64 cycles per SM
+// sub-partition, conversions to f64 included, and a lone dependent chain
+// advances once per ~86 cycles. So every operand is converted to f64 exactly
+// once, with all lanes busy, and the chains see only f64 loads and FMAs:
+//   - rows arrive TG_ROWS at a time through a TG_STAGES-deep cp.async ring
+//     (Bo as stored -- the device copy of the fit state is f64 -- and the raw
+//     f32 candidate columns);
+//   - in the iteration before a tile's chain steps, the block converts it:
+//     the candidate value (for FillSrc the f32 product B * (X * s)) once per
+//     element, and Bo when it is stored as f32;
+//   - the chain steps of the tile before run meanwhile.
 // ---------------------------------------------------------------------------
-constexpr int TG_ROWS = 32, TG_THREADS = 128;
+constexpr int TG_ROWS = 32, TG_THREADS = 128, TG_STAGES = 4;
 
-template <class Src, int KT>
+__host__ __device__ constexpr size_t align16(size_t b) { return (b + 15) / 16 * 16; }
+
+template <class BoT, int KT, int R>
+struct TgemmSmem {
+    static constexpr int JT = TG_THREADS / KT;
+    static constexpr bool kConvBo = sizeof(BoT) != sizeof(double);
+    static constexpr size_t rawBo = 0;  // [TG_STAGES][TG_ROWS][KT + 1] BoT
+    static constexpr size_t rawV =      // [TG_STAGES][R][JT][TG_ROWS + 1] f32
+        align16(rawBo + sizeof(BoT) * TG_STAGES * TG_ROWS * (KT + 1));
+    static constexpr size_t dV =  // [2][JT][TG_ROWS + 1] f64
+        align16(rawV + 4 * TG_STAGES * R * JT * (TG_ROWS + 1));
+    static constexpr size_t dBo =  // [2][TG_ROWS][KT + 1] f64 (f32 Bo only)
+        align16(dV + 8 * 2 * JT * (TG_ROWS + 1));
+    static constexpr size_t total = align16(dBo + (kConvBo ? 8 * 2 * TG_ROWS * (KT + 1) : 0));
+};
+
+template <class Src, class BoT, int KT>
 __global__ void __launch_bounds__(TG_THREADS)
-    k_tgemm(Src src, const float *__restrict__ Bo, size_t ldbo, int n, int m, int P,
+    k_tgemm(Src src, const BoT *__restrict__ Bo, size_t ldbo, int n, int m, int P,
             double *__restrict__ T)
 {
-    constexpr int JT = TG_THREADS / KT;
-    __shared__ double sBo[2][TG_ROWS][KT + 1];
-    __shared__ double sV[2][TG_ROWS][JT + 1];
+    constexpr int R = Src::kRaw, S = TG_STAGES;
+    using L = TgemmSmem<BoT, KT, R>;
+    constexpr int JT = L::JT;
+    extern __shared__ __align__(16) unsigned char tsm[];
+    auto rBo = reinterpret_cast<BoT(*)[TG_ROWS][KT + 1]>(tsm + L::rawBo);
+    auto rV = reinterpret_cast<float(*)[R][JT][TG_ROWS + 1]>(tsm + L::rawV);
+    auto dV = reinterpret_cast<double(*)[JT][TG_ROWS + 1]>(tsm + L::dV);
+    auto dBo = reinterpret_cast<double(*)[TG_ROWS][KT + 1]>(tsm + L::dBo);
+    __shared__ const float *vcol[R][JT];
+    __shared__ float vprm[JT];
     const int t = threadIdx.x, kk = t % KT, jj = t / KT;
     const int k0 = blockIdx.x * KT, j0 = blockIdx.y * JT;
-    // Rows of the next tile are loaded into registers before the current tile's
-    // chain steps, and stored to the other half after them.
-    constexpr int NB = (TG_ROWS * KT + TG_THREADS - 1) / TG_THREADS;
-    constexpr int NV = (TG_ROWS * JT + TG_THREADS - 1) / TG_THREADS;
-    double rb[NB], rv[NV];
-    auto fetch = [&](int r0) {
-        const int rows = min(TG_ROWS, n - r0);
-#pragma unroll
-        for (int q = 0; q < NB; ++q) {
-            const int e = t + q * TG_THREADS;
-            const int rr = e / KT, cc = e % KT;
-            rb[q] = (e < TG_ROWS * KT && rr < rows && k0 + cc < m)
-                        ? (double)Bo[(size_t)(r0 + rr) * ldbo + k0 + cc] : 0.0;
-        }
-#pragma unroll
-        for (int q = 0; q < NV; ++q) {
-            const int e = t + q * TG_THREADS;
-            const int rr = e % TG_ROWS, cj = e / TG_ROWS;
-            rv[q] = (e < TG_ROWS * JT && rr < rows && j0 + cj < P)
-                        ? (double)src((size_t)(r0 + rr), j0 + cj) : 0.0;
-        }
-    };
-    auto put = [&](int h) {
-#pragma unroll
-        for (int q = 0; q < NB; ++q) {
-            const int e = t + q * TG_THREADS;
-            if (e < TG_ROWS * KT) {
-                sBo[h][e / KT][e % KT] = rb[q];
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < NV; ++q) {
-            const int e = t + q * TG_THREADS;
-            if (e < TG_ROWS * JT) {
-                sV[h][e % TG_ROWS][e / TG_ROWS] = rv[q];
-            }
-        }
-    };
-    double acc = 0.0;
-    if (n > 0) {
-        fetch(0);
-        put(0);
+    if (t < JT) {
+        const int j = j0 + t;
+        vcol[0][t] = j < P ? src.raw0(j) : nullptr;
+        vcol[R - 1][t] = j < P ? src.raw1(j) : nullptr;
+        vprm[t] = j < P ? src.param(j) : 0.f;
     }
     __syncthreads();
-    int h = 0;
-    for (int r0 = 0; r0 < n; r0 += TG_ROWS, h ^= 1) {
-        const int rows = min(TG_ROWS, n - r0);
-        const bool more = r0 + TG_ROWS < n;
-        if (more) {
-            fetch(r0 + TG_ROWS);
+    const int ntiles = (n + TG_ROWS - 1) / TG_ROWS;
+    auto issue = [&](int tl) {
+        const int sg = tl % S, r0 = tl * TG_ROWS;
+        for (int e = t; e < TG_ROWS * KT; e += TG_THREADS) {
+            const int rr = e / KT, cc = e % KT;
+            const bool ok = r0 + rr < n && k0 + cc < m;
+            cp_async<sizeof(BoT)>(&rBo[sg][rr][cc],
+                                  ok ? Bo + (size_t)(r0 + rr) * ldbo + k0 + cc : Bo, ok);
         }
-        for (int rr = 0; rr < rows; ++rr) {
-            acc = fma(sBo[h][rr][kk], sV[h][rr][jj], acc);
+        for (int e = t; e < R * JT * TG_ROWS; e += TG_THREADS) {
+            const int rr = e % TG_ROWS, cj = (e / TG_ROWS) % JT, q = e / (TG_ROWS * JT);
+            const float *col = vcol[q][cj];
+            const bool ok = col != nullptr && r0 + rr < n;
+            cp_async4(&rV[sg][q][cj][rr], ok ? col + r0 + rr : vcol[0][0], ok);
         }
-        if (more) {
-            put(h ^ 1);
+    };
+    auto convert = [&](int tl) {  // raw tile tl (landed) -> f64 slot tl & 1
+        const int sg = tl % S, h = tl & 1;
+        for (int e = t; e < JT * TG_ROWS; e += TG_THREADS) {
+            const int cj = e / TG_ROWS, rr = e % TG_ROWS;
+            dV[h][cj][rr] = (double)src.combine(rV[sg][0][cj][rr], rV[sg][R - 1][cj][rr], vprm[cj]);
         }
+        if (L::kConvBo) {
+            for (int e = t; e < TG_ROWS * KT; e += TG_THREADS) {
+                const int rr = e / KT, cc = e % KT;
+                dBo[h][rr][cc] = (double)rBo[sg][rr][cc];
+            }
+        }
+    };
+#pragma unroll
+    for (int q = 0; q < S - 1; ++q) {
+        if (q < ntiles) {
+            issue(q);
+        }
+        cp_async_commit();
+    }
+    cp_async_wait<S - 3>();  // tiles 0 and 1 landed
+    __syncthreads();
+    if (ntiles > 0) {
+        convert(0);
+    }
+    __syncthreads();
+    double acc = 0.0;
+    for (int tl = 0; tl < ntiles; ++tl) {
+        const int h = tl & 1;
+        if (tl + S - 1 < ntiles) {
+            issue(tl + S - 1);  // into the ring slot of tile tl - 1 (converted and consumed)
+        }
+        cp_async_commit();
+        if (tl + 1 < ntiles) {
+            convert(tl + 1);
+        }
+        const double *bo = L::kConvBo ? &dBo[h][0][kk]
+                                      : reinterpret_cast<const double *>(&rBo[tl % S][0][kk]);
+        const double *v = dV[h][jj];
+        const int rows = min(TG_ROWS, n - tl * TG_ROWS);
+        if (rows == TG_ROWS) {
+#pragma unroll 8
+            for (int rr = 0; rr < TG_ROWS; ++rr) {
+                acc = fma(bo[rr * (KT + 1)], v[rr], acc);
+            }
+        } else {
+            for (int rr = 0; rr < rows; ++rr) {
+                acc = fma(bo[rr * (KT + 1)], v[rr], acc);
+            }
+        }
+        cp_async_wait<S - 3>();  // tile tl + 2 landed
         __syncthreads();
     }
     if (k0 + kk < m && j0 + jj < P) {
@@ -97,80 +148,125 @@ __global__ void __launch_bounds__(TG_THREADS)
     }
 }
 
-// Column chains: warp 0 of a block runs 32 column chains (lane = column) out
-// of shared memory while warps 1..3 stage the next tile of rows.
-constexpr int CC_COLS = 32, CC_ROWS = 64, CC_THREADS = 128;
+// Column chains: warp 0 of a block runs 32 column chains (lane = column) in
+// f64 out of shared memory. Warps 1..3 keep CC_STAGES - 1 tiles of raw f32
+// rows in flight with cp.async (one warp instruction = 32 consecutive rows of
+// one column) and convert the next tile to f64 once per element while warp 0
+// steps through the current one.
+constexpr int CC_COLS = 32, CC_ROWS = 32, CC_STAGES = 4, CC_THREADS = 128;
 
 // Fused chains over the rows i = 0..n-1 in order: the reference's sequential
 // f64 accumulations (kernels.cc:361-366 norm of the stored column;
 // kernels.cc:215-237 dot_widen; marsalgo.cc:359-369 column norms of X).
+// column(j) is the f32 column read by chain j, value() the f32 operand made
+// from its raw value and param(j); step() runs on the f64 conversions.
 struct SqChain {  // sum of squares of the stored f32 column Bx[:, col[j]]
     static constexpr bool kUsesY = false;
     const float *Bx;
     size_t ld;
     const int *col;
-    __device__ __forceinline__ float param(int) const { return 0.f; }
-    __device__ __forceinline__ float load(size_t i, int j, float) const
+    __device__ __forceinline__ const float *column(int j) const
     {
-        return Bx[i + (size_t)(col ? col[j] : j) * ld];
+        return Bx + (size_t)(col ? col[j] : j) * ld;
     }
-    __device__ __forceinline__ float yload(size_t) const { return 0.f; }
+    __device__ __forceinline__ const float *ycolumn() const { return nullptr; }
+    __device__ __forceinline__ float param(int) const { return 0.f; }
+    __device__ __forceinline__ float value(float v, float) const { return v; }
     __device__ __forceinline__ double step(double acc, double v, double) const
     {
         return fma(v, v, acc);
     }
-    __device__ __forceinline__ double finish(double acc, int) const { return acc; }
 };
 
 template <class Op>
 __global__ void __launch_bounds__(CC_THREADS) k_colchain(Op op, int n, int P, double *__restrict__ out)
 {
-    __shared__ double tile[2][CC_COLS][CC_ROWS + 1];
-    __shared__ double ytile[2][CC_ROWS];
+    constexpr int LOADERS = CC_THREADS / 32 - 1, S = CC_STAGES;
+    __shared__ float raw[S][CC_COLS][CC_ROWS + 1];
+    __shared__ float yraw[S][CC_ROWS];
+    __shared__ double dt[2][CC_COLS][CC_ROWS + 1];
+    __shared__ double dy[2][CC_ROWS];
+    __shared__ const float *cptr[CC_COLS];
+    __shared__ float cparam[CC_COLS];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int j0 = blockIdx.x * CC_COLS;
     const int ncols = min(CC_COLS, P - j0);
     const int ntiles = (n + CC_ROWS - 1) / CC_ROWS;
-    __shared__ float cparam[CC_COLS];
     if (t < ncols) {
+        cptr[t] = op.column(j0 + t);
         cparam[t] = op.param(j0 + t);
     }
     __syncthreads();
-    auto load = [&](int tl, int b) {
-        const int base = tl * CC_ROWS, rows = min(CC_ROWS, n - base);
-        for (int e = t - 32; e < ncols * CC_ROWS; e += CC_THREADS - 32) {
-            const int c = e / CC_ROWS, r = e % CC_ROWS;
-            if (r < rows) {
-                tile[b][c][r] = (double)op.load((size_t)(base + r), j0 + c, cparam[c]);
-            }
+    const float *yc = op.ycolumn();
+    const int lt = t - 32;  // loader thread index
+    auto issue = [&](int tl) {
+        const int sg = tl % S, i = tl * CC_ROWS + lane;
+        const bool ok = i < n;
+        for (int c = warp - 1; c < ncols; c += LOADERS) {
+            cp_async4(&raw[sg][c][lane], cptr[c] + (ok ? i : 0), ok);
         }
-        if (Op::kUsesY) {
-            for (int r = t - 32; r < rows; r += CC_THREADS - 32) {
-                ytile[b][r] = (double)op.yload((size_t)(base + r));
-            }
+        if (Op::kUsesY && warp == 1) {
+            cp_async4(&yraw[sg][lane], yc + (ok ? i : 0), ok);
+        }
+    };
+    auto convert = [&](int tl) {  // raw tile tl (landed) -> f64 slot tl & 1
+        const int sg = tl % S, h = tl & 1;
+        for (int e = lt; e < ncols * CC_ROWS; e += 32 * LOADERS) {
+            const int c = e / CC_ROWS, r = e % CC_ROWS;
+            dt[h][c][r] = (double)op.value(raw[sg][c][r], cparam[c]);
+        }
+        if (Op::kUsesY && lt < CC_ROWS) {
+            dy[h][lt] = (double)yraw[sg][lt];
         }
     };
     if (warp > 0) {
-        load(0, 0);
+#pragma unroll
+        for (int q = 0; q < S - 1; ++q) {
+            if (q < ntiles) {
+                issue(q);
+            }
+            cp_async_commit();
+        }
+        cp_async_wait<S - 3>();  // tiles 0 and 1 landed
+    }
+    __syncthreads();
+    if (warp > 0 && ntiles > 0) {
+        convert(0);
     }
     __syncthreads();
     double acc = 0.0;
     for (int tl = 0; tl < ntiles; ++tl) {
-        const int b = tl & 1;
+        const int h = tl & 1;
         if (warp == 0) {
             if (lane < ncols) {
+                const double *col = dt[h][lane];
+                const double *yr = dy[h];
                 const int rows = min(CC_ROWS, n - tl * CC_ROWS);
-                for (int r = 0; r < rows; ++r) {
-                    acc = op.step(acc, tile[b][lane][r], ytile[b][r]);
+                if (rows == CC_ROWS) {
+#pragma unroll 8
+                    for (int r = 0; r < CC_ROWS; ++r) {
+                        acc = op.step(acc, col[r], Op::kUsesY ? yr[r] : 0.0);
+                    }
+                } else {
+                    for (int r = 0; r < rows; ++r) {
+                        acc = op.step(acc, col[r], Op::kUsesY ? yr[r] : 0.0);
+                    }
                 }
             }
-        } else if (tl + 1 < ntiles) {
-            load(tl + 1, b ^ 1);
+        } else {
+            if (tl + S - 1 < ntiles) {
+                issue(tl + S - 1);  // into the ring slot of tile tl - 1 (already converted)
+            }
+            cp_async_commit();
+            if (tl + 1 < ntiles) {
+                convert(tl + 1);
+            }
+            cp_async_wait<S - 3>();  // tile tl + 2 landed
         }
         __syncthreads();
     }
     if (warp == 0 && lane < ncols) {
-        out[j0 + lane] = op.finish(acc, j0 + lane);
+        out[j0 + lane] = acc;
     }
 }
 
@@ -181,9 +277,9 @@ __global__ void __launch_bounds__(CC_THREADS) k_colchain(Op op, int n, int P, do
 // ---------------------------------------------------------------------------
 constexpr int PJ_THREADS = 128, PJ_COLS = 8;
 
-template <class Src>
+template <class Src, class BoT>
 __global__ void __launch_bounds__(PJ_THREADS)
-    k_project(Src src, const float *__restrict__ Bo, size_t ldbo, int n, int m, int P,
+    k_project(Src src, const BoT *__restrict__ Bo, size_t ldbo, int n, int m, int P,
               const double *__restrict__ T, const int *__restrict__ out_col,
               float *__restrict__ Bx, size_t ldBx)
 {
@@ -198,7 +294,7 @@ __global__ void __launch_bounds__(PJ_THREADS)
     if (i >= (size_t)n) {
         return;
     }
-    const float *bo = Bo + i * ldbo;
+    const BoT *bo = Bo + i * ldbo;
     double proj[PJ_COLS];
 #pragma unroll
     for (int q = 0; q < PJ_COLS; ++q) {
@@ -260,24 +356,21 @@ __device__ __forceinline__ float norm_scale(double s, double tol)
 // ybx[j] = fused chain over i of f32(Bx[i,j] * scale_j) * y[i] (dot_widen of the
 // normalised column, kernels.cc:215-237 after kernels.cc:401-416). The scale
 // is applied when the tile is loaded.
-struct NormDotChain {
+struct NormDotChain {  // ybx = sum_i f32(Bx[i, j] * scale_j) * y[i]
     static constexpr bool kUsesY = true;
     const float *Bx;
     size_t ld;
     const float *y;
     const double *s;
     double tol;
+    __device__ __forceinline__ const float *column(int j) const { return Bx + (size_t)j * ld; }
+    __device__ __forceinline__ const float *ycolumn() const { return y; }
     __device__ __forceinline__ float param(int j) const { return norm_scale(s[j], tol); }
-    __device__ __forceinline__ float load(size_t i, int j, float scale) const
-    {
-        return Bx[i + (size_t)j * ld] * scale;
-    }
-    __device__ __forceinline__ float yload(size_t i) const { return y[i]; }
+    __device__ __forceinline__ float value(float v, float scale) const { return v * scale; }
     __device__ __forceinline__ double step(double acc, double v, double yv) const
     {
         return fma(v, yv, acc);
     }
-    __device__ __forceinline__ double finish(double acc, int) const { return acc; }
 };
 
 constexpr int NM_THREADS = 256, NM_COLS = 8;
@@ -306,67 +399,87 @@ __global__ void __launch_bounds__(NM_THREADS)
 // FP64 hinge sweep (marsalgo.cc:576-649 with covariates_impl :91-151), in the
 // reference's operation order.
 //
-// Block = one input column and up to W candidates (parent columns):
+// Block = one input column and up to W <= 5 candidates (parent columns):
 //   warps 0..W-1  one candidate each; lane l holds components c = l + 32 q of
 //                 the running f and g (component m is the candidate column Bx)
-//   warp  W       the six scalar recurrences (k0, k1, w, bd, b2, vb) of all W
-//                 candidates, one lane per candidate
-//   warp  W+1     the loader: stages the next SW_ROWS sorted rows as doubles
-//                 (permutation, delta, delta^2, y, the gathered Bo rows, B and
-//                 Bx of every candidate) into the other half of a double buffer
+//   warp  W       the six scalar recurrences (k0, k1, w, bd, b2, vb) of the W
+//                 candidates, one lane per (candidate, recurrence): one FMA
+//                 warp instruction per row for all of them, each lane taking
+//                 the previous row's value of the recurrence it reads from
+//                 another lane by a shuffle
+//   warp  W+1     the loader: keeps S - 1 stages of SW_ROWS sorted rows in
+//                 flight with cp.async -- each gathered row of the f64 Bo is
+//                 one warp instruction (lanes over components); y and the B
+//                 and Bx values of every candidate (f32, lanes over rows) are
+//                 converted to f64 once, one stage ahead of their use; the
+//                 deltas of the sorted x (and delta^2, 2 delta) are formed at
+//                 issue from the permutation and x prefetched one stage ahead
 // At a grid row each candidate warp saves f in a snapshot slot and the scalar
 // warp saves k0 + k1 and w; when SW_SNAP slots are in use, lane q of each
 // candidate warp scores slot q with the reference's sequential chains
 // ff = sum_c f_c^2 and fy = sum_c f_c yc_c (c = 0..m) and the warp keeps the
 // first maximum in row order.
 // ---------------------------------------------------------------------------
-constexpr int SW_ROWS = 32, SW_SNAP = 32, SW_MAXW = 8;
+constexpr int SW_ROWS = 32, SW_SNAP = 32, SW_MAXW = 5;
 
 struct SweepSmem {
-    // offsets (in doubles) into the dynamic shared memory
-    size_t snap, bo, bd, bx, d, dd, yd, ybo, mk, mw, total;
-    __host__ __device__ SweepSmem(int m, int W)
+    // byte offsets into the dynamic shared memory (f64 regions first)
+    size_t snap, mk, mw, ybo, d, dd, d2, bo, cvt, raw, total;
+    __host__ __device__ SweepSmem(int m, int W, int S)
     {
+        const int nv = 2 * W + 1;  // B and Bx of each candidate, then y
         size_t o = 0;
         snap = o;
-        o += (size_t)W * SW_SNAP * (m + 1);
-        bo = o;
-        o += 2 * (size_t)SW_ROWS * m;
-        bd = o;
-        o += 2 * (size_t)W * SW_ROWS;
-        bx = o;
-        o += 2 * (size_t)W * SW_ROWS;
-        d = o;
-        o += 2 * SW_ROWS;
-        dd = o;
-        o += 2 * SW_ROWS;
-        yd = o;
-        o += 2 * SW_ROWS;
-        ybo = o;
-        o += (size_t)m + 1;
+        o += 8 * (size_t)W * SW_SNAP * (m + 1);
         mk = o;
-        o += (size_t)W * SW_SNAP;
+        o += 8 * (size_t)W * SW_SNAP;
         mw = o;
-        o += (size_t)W * SW_SNAP;
-        total = o;
+        o += 8 * (size_t)W * SW_SNAP;
+        ybo = o;
+        o += 8 * ((size_t)m + 1);
+        d = o;
+        o += 8 * (size_t)S * SW_ROWS;
+        dd = o;
+        o += 8 * (size_t)S * SW_ROWS;
+        d2 = o;
+        o += 8 * (size_t)S * SW_ROWS;
+        bo = o;
+        o += 8 * (size_t)S * SW_ROWS * m;
+        cvt = o;
+        o += 8 * 2 * (size_t)nv * SW_ROWS;
+        raw = o;
+        o += 4 * (size_t)S * nv * SW_ROWS;
+        total = (o + 15) / 16 * 16;
     }
 };
 
-template <int CPL>
-__global__ void __launch_bounds__(32 * (SW_MAXW + 2))
+template <int CPL, int S>
+__global__ void __launch_bounds__(32 * (SW_MAXW + 2), 1)
     k_sweep(const SweepTask *__restrict__ tasks, const int *__restrict__ perm,
             const float *__restrict__ xsort, const float *__restrict__ y,
             const float *__restrict__ B, size_t ldB, const int *__restrict__ cand_b,
-            const float *__restrict__ Bx, size_t ldBx, const float *__restrict__ Bo,
+            const float *__restrict__ Bx, size_t ldBx, const double *__restrict__ Bo,
             size_t ldbo, const double *__restrict__ ybo, const double *__restrict__ ybx, int n,
             int m, int head, int tail, int min_span, double tol, double *__restrict__ hsse,
             int *__restrict__ hrow)
 {
-    extern __shared__ double dyn[];
+    extern __shared__ __align__(16) unsigned char sraw[];
     const int W = (blockDim.x >> 5) - 2;  // candidate warps
-    const SweepSmem L(m, W);
+    const int NV = 2 * W + 1;
+    const SweepSmem L(m, W, S);
     const int ldF = m + 1;
+    double *snapbase = reinterpret_cast<double *>(sraw + L.snap);
+    double *mk = reinterpret_cast<double *>(sraw + L.mk);
+    double *mw = reinterpret_cast<double *>(sraw + L.mw);
+    double *sybo = reinterpret_cast<double *>(sraw + L.ybo);
+    double *sd = reinterpret_cast<double *>(sraw + L.d);
+    double *sdd = reinterpret_cast<double *>(sraw + L.dd);
+    double *sd2 = reinterpret_cast<double *>(sraw + L.d2);
+    double *sbo = reinterpret_cast<double *>(sraw + L.bo);
+    double *scvt = reinterpret_cast<double *>(sraw + L.cvt);  // [2][NV][SW_ROWS]
+    float *sraw4 = reinterpret_cast<float *>(sraw + L.raw);   // [S][NV][SW_ROWS]
     __shared__ int srow[SW_SNAP];
+    __shared__ int sbcol[SW_MAXW];
 
     const SweepTask task = tasks[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -377,46 +490,76 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2))
     const float *xs = xsort + (size_t)task.xcol * n;
 
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
-        dyn[L.ybo + c] = ybo[c];
+        sybo[c] = ybo[c];
     }
-    // The loader stages rows [i0, i0 + rows) into buffer half h.
-    auto stage = [&](int i0, int h) {
+    if (threadIdx.x < task.count) {
+        sbcol[threadIdx.x] = cand_b[task.cand0 + threadIdx.x];
+    }
+    __syncthreads();
+
+    const int nstages = (tail + SW_ROWS - 1) / SW_ROWS;
+    // Loader registers: row index and sorted x (and its predecessor) of this
+    // lane's row in the next stage to issue.
+    int pf_k = 0;
+    float pf_x = 0.f, pf_xp = 0.f;
+    auto prefetch = [&](int sq) {
+        const int i = sq * SW_ROWS + lane;
+        if (sq < nstages && i < tail) {
+            pf_k = pk[i];
+            pf_x = xs[i];
+            pf_xp = i > 0 ? xs[i - 1] : 0.f;
+        }
+    };
+    auto issue = [&](int sq) {
+        const int sg = sq % S, i0 = sq * SW_ROWS;
         const int rows = min(SW_ROWS, tail - i0);
-        int k = 0;
-        if (lane < rows) {
-            const int i = i0 + lane;
-            k = pk[i];
-            dyn[L.yd + h * SW_ROWS + lane] = (double)y[k];
-            const double d = i > 0 ? (double)(xs[i - 1] - xs[i]) : 0.0;
-            dyn[L.d + h * SW_ROWS + lane] = d;
-            dyn[L.dd + h * SW_ROWS + lane] = d * d;
-            const float *row = Bo + (size_t)k * ldbo;
-            double *dst = dyn + L.bo + ((size_t)h * SW_ROWS + lane) * m;
-            for (int c = 0; c < m; ++c) {
-                dst[c] = (double)row[c];
-            }
-            for (int cw = 0; cw < task.count; ++cw) {
-                const int cand = task.cand0 + cw;
-                dyn[L.bd + (h * W + cw) * SW_ROWS + lane] =
-                    (double)B[(size_t)k + (size_t)cand_b[cand] * ldB];
-                dyn[L.bx + (h * W + cw) * SW_ROWS + lane] =
-                    (double)Bx[(size_t)k + (size_t)cand * ldBx];
+        const int k = pf_k;
+        double *bo = sbo + (size_t)sg * SW_ROWS * m;
+        for (int r = 0; r < rows; ++r) {
+            const int kr = __shfl_sync(0xffffffffu, k, r);
+            const double *src = Bo + (size_t)kr * ldbo;
+            for (int c = lane; c < m; c += 32) {
+                cp_async<8>(bo + r * m + c, src + c);
             }
         }
+        if (lane < rows) {
+            float *rw = sraw4 + (size_t)sg * NV * SW_ROWS;
+            for (int cw = 0; cw < task.count; ++cw) {
+                cp_async4(rw + cw * SW_ROWS + lane, B + (size_t)k + (size_t)sbcol[cw] * ldB);
+                cp_async4(rw + (W + cw) * SW_ROWS + lane,
+                          Bx + (size_t)k + (size_t)(task.cand0 + cw) * ldBx);
+            }
+            cp_async4(rw + 2 * W * SW_ROWS + lane, y + k);
+            const double dl = i0 + lane > 0 ? (double)(pf_xp - pf_x) : 0.0;
+            sd[sg * SW_ROWS + lane] = dl;
+            sdd[sg * SW_ROWS + lane] = dl * dl;
+            sd2[sg * SW_ROWS + lane] = dl * 2;
+        }
+    };
+    auto convert = [&](int sq) {  // stage sq (landed) -> f64 slot sq & 1, lanes over rows
+        const float *rw = sraw4 + (size_t)(sq % S) * NV * SW_ROWS;
+        double *cv = scvt + (size_t)(sq & 1) * NV * SW_ROWS;
+        for (int cw = 0; cw < task.count; ++cw) {
+            cv[cw * SW_ROWS + lane] = (double)rw[cw * SW_ROWS + lane];
+            cv[(W + cw) * SW_ROWS + lane] = (double)rw[(W + cw) * SW_ROWS + lane];
+        }
+        cv[2 * W * SW_ROWS + lane] = (double)rw[2 * W * SW_ROWS + lane];
     };
 
     const int mycand = task.cand0 + (cwarp ? warp : 0);
     const double ybx_c = ybx[mycand];
-    double *snap = dyn + L.snap + (size_t)(cwarp ? warp : 0) * SW_SNAP * ldF;
-    double *mk = dyn + L.mk, *mw = dyn + L.mw;
+    double *snap = snapbase + (size_t)(cwarp ? warp : 0) * SW_SNAP * ldF;
     double f[CPL], g[CPL];
 #pragma unroll
     for (int q = 0; q < CPL; ++q) {
         f[q] = 0.0;
         g[q] = 0.0;
     }
-    const bool slane = swarp && lane < task.count;
-    double k0 = 0, k1 = 0, w = 0, bd = 0, vb = 0, b2 = 0;
+    // scalar warp: lane = 6 * candidate + recurrence (b2, vb, bd, w, k0, k1)
+    const int sc = lane / 6, role = lane % 6;
+    const bool sact = swarp && sc < task.count;
+    const int ssrc = sc * 6 + (role == 3 ? 1 : role == 5 ? 2 : role >= 2 ? 0 : role);
+    double sacc = 0.0;
     double best = 0.0;
     int besti = -1;
     int nsnap = 0;  // block-uniform
@@ -428,11 +571,10 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2))
             int row = 0x7fffffff;
             if (lane < nsnap) {
                 const double *fs = snap + (size_t)lane * ldF;
-                const double *yb = dyn + L.ybo;
                 double ff = 0.0, fy = 0.0;
                 for (int c = 0; c < m; ++c) {
                     ff = fma(fs[c], fs[c], ff);
-                    fy = fma(fs[c], yb[c], fy);
+                    fy = fma(fs[c], sybo[c], fy);
                 }
                 ff = fma(fs[m], fs[m], ff);
                 fy = fma(fs[m], ybx_c, fy);
@@ -458,12 +600,25 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2))
         nsnap = 0;
     };
 
-    if (lwarp && tail > 0) {
-        stage(0, 0);
+    if (lwarp) {
+        prefetch(0);
+#pragma unroll
+        for (int q = 0; q < S - 1; ++q) {
+            if (q < nstages) {
+                issue(q);
+            }
+            cp_async_commit();
+            prefetch(q + 1);
+        }
+        cp_async_wait<S - 2>();  // stage 0 landed
+        __syncwarp();
+        if (nstages > 0) {
+            convert(0);
+        }
     }
     __syncthreads();
-    int h = 0;
-    for (int i0 = 0; i0 < tail; i0 += SW_ROWS, h ^= 1) {
+    for (int sq = 0; sq < nstages; ++sq) {
+        const int sg = sq % S, h = sq & 1, i0 = sq * SW_ROWS;
         const int rows = min(SW_ROWS, tail - i0);
         int gcount = 0;
         for (long gr = next_grid; gr < i0 + rows; gr += min_span) {
@@ -473,18 +628,19 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2))
             flush();
             __syncthreads();  // slots are rewritten below
         }
+        const double *cv = scvt + (size_t)h * NV * SW_ROWS;
+        const double *dv = sd + sg * SW_ROWS;
         if (cwarp) {
-            const double *bw = dyn + L.bd + (h * W + warp) * SW_ROWS;
-            const double *xw = dyn + L.bx + (h * W + warp) * SW_ROWS;
-            const double *sd = dyn + L.d + h * SW_ROWS;
-            const double *rowb = dyn + L.bo + (size_t)h * SW_ROWS * m;
+            const double *bw = cv + warp * SW_ROWS;
+            const double *xw = cv + (W + warp) * SW_ROWS;
+            const double *rowb = sbo + (size_t)sg * SW_ROWS * m;
             long ng = next_grid;
             int slot = nsnap;
             for (int r = 0; r < rows; ++r) {
                 const int i = i0 + r;
                 const double bk = bw[r], bxk = xw[r];
                 const double *rowp = rowb + r * m;
-                const double di = sd[r];  // 0 for the first row
+                const double di = dv[r];  // 0 for the first row
 #pragma unroll
                 for (int q = 0; q < CPL; ++q) {
                     const int c = lane + 32 * q;
@@ -508,37 +664,53 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2))
                     ++slot;
                 }
             }
-        } else if (slane) {
-            const double *bw = dyn + L.bd + (h * W + lane) * SW_ROWS;
-            const double *sd = dyn + L.d + h * SW_ROWS;
-            const double *sdd = dyn + L.dd + h * SW_ROWS;
-            const double *syd = dyn + L.yd + h * SW_ROWS;
+        } else if (swarp) {
+            // marsalgo.cc covariates_impl order: k0 += dd b2; k1 += 2d bd; w += d vb;
+            // bd += d b2; b2 += bk^2; vb += yk bk (right-hand sides are the previous
+            // row's values); the first row sets vb = bk yk, b2 = bk^2.
+            const double *bw = cv + (sc < W ? sc : 0) * SW_ROWS;
+            const double *yw = cv + 2 * W * SW_ROWS;
+            const double *ddv = sdd + sg * SW_ROWS;
+            const double *d2v = sd2 + sg * SW_ROWS;
             long ng = next_grid;
             int slot = nsnap;
             for (int r = 0; r < rows; ++r) {
                 const int i = i0 + r;
-                const double bk = bw[r], yk = syd[r];
+                const double bk = bw[r], yk = yw[r];
+                const double other = __shfl_sync(0xffffffffu, sacc, ssrc);
                 if (i == 0) {
-                    vb = bk * yk;
-                    b2 = bk * bk;
+                    if (role <= 1) {
+                        sacc = fma(role == 0 ? bk : yk, bk, -0.0);
+                    }
                     continue;
                 }
-                const double di = sd[r];
-                k0 = fma(sdd[r], b2, k0);
-                k1 = fma(di * 2, bd, k1);
-                w = fma(di, vb, w);
-                bd = fma(di, b2, bd);
-                b2 = fma(bk, bk, b2);
-                vb = fma(yk, bk, vb);
+                const double a = role == 0 ? bk : role == 1 ? yk : role == 4 ? ddv[r]
+                                                     : role == 5 ? d2v[r] : dv[r];
+                const double b = role <= 1 ? bk : other;
+                sacc = fma(a, b, sacc);
                 if (i == ng) {
                     ng += min_span;
-                    mk[lane * SW_SNAP + slot] = k0 + k1;
-                    mw[lane * SW_SNAP + slot] = w;
+                    const double k1v = __shfl_down_sync(0xffffffffu, sacc, 1);
+                    if (sact && role == 4) {
+                        mk[sc * SW_SNAP + slot] = sacc + k1v;
+                    }
+                    if (sact && role == 3) {
+                        mw[sc * SW_SNAP + slot] = sacc;
+                    }
                     ++slot;
                 }
             }
-        } else if (lwarp && i0 + SW_ROWS < tail) {
-            stage(i0 + SW_ROWS, h ^ 1);
+        } else if (lwarp) {
+            if (sq + S - 1 < nstages) {
+                issue(sq + S - 1);  // into the ring slot of stage sq - 1 (consumed)
+            }
+            cp_async_commit();
+            prefetch(sq + S);
+            cp_async_wait<S - 2>();  // stage sq + 1 landed
+            __syncwarp();
+            if (sq + 1 < nstages) {
+                convert(sq + 1);
+            }
         }
         nsnap += gcount;
         next_grid += (long)gcount * min_span;
@@ -797,23 +969,30 @@ __global__ void __launch_bounds__(AP_THREADS)
 
 int append_blocks(int n) { return (int)std::max<size_t>(1, std::min<size_t>(608, ceil_div(n, 2048))); }
 
-template <class Src>
-void tgemm_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, int n, int m,
-                int P, double *T, long long *launches)
+template <class Src, class BoT>
+void tgemm_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, int n, int m, int P,
+                double *T, long long *launches)
 {
     if (P <= 0 || m <= 0) {
         return;
     }
-    int kt = 4;  // narrower tiles would need more than 48 KB of static shared memory
+    int kt = 4;
     while (kt < m && kt < 32) {
         kt *= 2;
     }
     const unsigned gx = (unsigned)ceil_div(m, kt), gy = (unsigned)ceil_div(P, TG_THREADS / kt);
     verify(gy <= 65535, "too many candidate columns for one launch", 2);
-#define TG_CASE(K)                                                                    \
-    case K:                                                                           \
-        k_tgemm<Src, K><<<dim3(gx, gy), TG_THREADS, 0, st>>>(src, Bo, ldbo, n, m, P, T); \
-        break;
+#define TG_CASE(K)                                                                           \
+    case K: {                                                                                \
+        const size_t smem = TgemmSmem<BoT, K, Src::kRaw>::total;                             \
+        if (smem > 48 * 1024) {                                                              \
+            CUDA_CHECK(cudaFuncSetAttribute(k_tgemm<Src, BoT, K>,                            \
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                            (int)smem));                                     \
+        }                                                                                    \
+        k_tgemm<Src, BoT, K><<<dim3(gx, gy), TG_THREADS, smem, st>>>(src, Bo, ldbo, n, m, P, T); \
+        break;                                                                               \
+    }
     switch (kt) {
         TG_CASE(4)
         TG_CASE(8)
@@ -825,10 +1004,14 @@ void tgemm_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, i
     *launches += 1;
 }
 
-template void tgemm_fp64<FillSrc>(cudaStream_t, const FillSrc &, const float *, size_t, int, int,
-                                  int, double *, long long *);
-template void tgemm_fp64<StoredSrc>(cudaStream_t, const StoredSrc &, const float *, size_t, int,
-                                    int, int, double *, long long *);
+#define TG_INST(SRC, BOT)                                                                     \
+    template void tgemm_fp64<SRC, BOT>(cudaStream_t, const SRC &, const BOT *, size_t, int, int, \
+                                       int, double *, long long *);
+TG_INST(FillSrc, float)
+TG_INST(FillSrc, double)
+TG_INST(StoredSrc, float)
+TG_INST(StoredSrc, double)
+#undef TG_INST
 
 template <class Op>
 void colchain(cudaStream_t st, const Op &op, int n, int P, double *out, long long *launches)
@@ -841,9 +1024,9 @@ void colchain(cudaStream_t st, const Op &op, int n, int P, double *out, long lon
     *launches += 1;
 }
 
-template <class Src>
-void project_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, int n, int m,
-                  int P, const int *out_col, float *Bx, size_t ldBx, double *s_out,
+template <class Src, class BoT>
+void project_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, int n, int m, int P,
+                  const int *out_col, float *Bx, size_t ldBx, double *s_out,
                   const ProjectScratch &ws, long long *launches)
 {
     if (P <= 0) {
@@ -853,23 +1036,26 @@ void project_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo,
     const int rb = (int)ceil_div(n, PJ_THREADS);
     const size_t smem = sizeof(double) * PJ_COLS * std::max(m, 1);
     if (smem > 48 * 1024) {
-        CUDA_CHECK(cudaFuncSetAttribute(k_project<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
+        CUDA_CHECK(cudaFuncSetAttribute(k_project<Src, BoT>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     verify(ceil_div(P, PJ_COLS) <= 65535, "too many candidate columns for one launch", 2);
-    k_project<Src><<<dim3(rb, (unsigned)ceil_div(P, PJ_COLS)), PJ_THREADS, smem, st>>>(
+    k_project<Src, BoT><<<dim3(rb, (unsigned)ceil_div(P, PJ_COLS)), PJ_THREADS, smem, st>>>(
         src, Bo, ldbo, n, m, P, ws.T, out_col, Bx, ldBx);
     LAUNCH_CHECK();
     *launches += 1;
     colchain(st, SqChain{Bx, ldBx, out_col}, n, P, s_out, launches);
 }
 
-template void project_fp64<FillSrc>(cudaStream_t, const FillSrc &, const float *, size_t, int,
-                                    int, int, const int *, float *, size_t, double *,
-                                    const ProjectScratch &, long long *);
-template void project_fp64<StoredSrc>(cudaStream_t, const StoredSrc &, const float *, size_t,
-                                      int, int, int, const int *, float *, size_t, double *,
-                                      const ProjectScratch &, long long *);
+#define PJ_INST(SRC, BOT)                                                                      \
+    template void project_fp64<SRC, BOT>(cudaStream_t, const SRC &, const BOT *, size_t, int,   \
+                                         int, int, const int *, float *, size_t, double *,      \
+                                         const ProjectScratch &, long long *);
+PJ_INST(FillSrc, float)
+PJ_INST(FillSrc, double)
+PJ_INST(StoredSrc, float)
+PJ_INST(StoredSrc, double)
+#undef PJ_INST
 
 void dgks_gate(cudaStream_t st, const double *T, int m, int P, const double *s, double tol,
                int *fired, int *nfired, long long *launches)
@@ -918,8 +1104,9 @@ void scale_columns(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const 
 }
 
 // Candidate warps per sweep block: at most 4, fewer when the launch has few
-// candidates (two blocks per SM) or the snapshots would not fit.
-static size_t sweep_smem(int m, int w) { return sizeof(double) * SweepSmem(m, w).total; }
+// candidates (two blocks per SM) or the snapshots would not fit; the row ring
+// is 4 stages deep when it fits in 200 KB with the snapshots, else 2.
+static size_t sweep_smem(int m, int w, int stages) { return SweepSmem(m, w, stages).total; }
 
 int sweep_warps(int m, int candidates)
 {
@@ -927,7 +1114,7 @@ int sweep_warps(int m, int candidates)
     while (w > 2 && (candidates + w - 1) / w < 2 * 152) {
         --w;
     }
-    while (w > 1 && sweep_smem(m, w) > 200 * 1024) {
+    while (w > 1 && sweep_smem(m, w, 2) > 200 * 1024) {
         --w;
     }
     return w;
@@ -935,7 +1122,7 @@ int sweep_warps(int m, int candidates)
 
 void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *perm,
                 const float *xsort, const float *y, const float *B, size_t ldB,
-                const int *cand_b, const float *Bx, size_t ldBx, const float *Bo, size_t ldbo,
+                const int *cand_b, const float *Bx, size_t ldBx, const double *Bo, size_t ldbo,
                 const double *ybo, const double *ybx, int n, int m, int head, int tail,
                 int min_span, double tol, double *hsse, int *hrow, int warps_per_block,
                 long long *launches)
@@ -944,31 +1131,47 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
         return;
     }
     const int warps = warps_per_block;
-    const size_t smem = sweep_smem(m, warps);
-    verify(smem <= 227 * 1024, "the GPU hinge sweep supports at most 430 basis functions");
+    verify(warps >= 1 && warps <= SW_MAXW, "sweep block size out of range", 2);
+    const int stages = sweep_smem(m, warps, 4) <= 200 * 1024 ? 4 : 2;
+    const size_t smem = sweep_smem(m, warps, stages);
+    if (smem > 227 * 1024) {
+        int mmax = 1;
+        while (sweep_smem(mmax + 1, 1, 2) <= 227 * 1024) {
+            ++mmax;
+        }
+        throw Error(1, "the GPU hinge sweep supports at most " + std::to_string(mmax) +
+                           " basis functions");
+    }
     const int comps = m + 1;
-#define LAUNCH_SWEEP(CPL)                                                                      \
+#define LAUNCH_SWEEP(CPL, S)                                                                   \
     do {                                                                                       \
-        CUDA_CHECK(cudaFuncSetAttribute(k_sweep<CPL>,                                          \
+        CUDA_CHECK(cudaFuncSetAttribute(k_sweep<CPL, S>,                                       \
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,           \
                                         (int)smem));                                           \
-        k_sweep<CPL><<<ntasks, 32 * (warps + 2), smem, st>>>(                                  \
+        k_sweep<CPL, S><<<ntasks, 32 * (warps + 2), smem, st>>>(                               \
             tasks, perm, xsort, y, B, ldB, cand_b, Bx, ldBx, Bo, ldbo, ybo, ybx, n, m, head,   \
             tail, min_span, tol, hsse, hrow);                                                  \
     } while (0)
+#define LAUNCH_CPL(CPL)            \
+    do {                           \
+        if (stages == 4) {         \
+            LAUNCH_SWEEP(CPL, 4);  \
+        } else {                   \
+            LAUNCH_SWEEP(CPL, 2);  \
+        }                          \
+    } while (0)
     if (comps <= 32) {
-        LAUNCH_SWEEP(1);
+        LAUNCH_CPL(1);
     } else if (comps <= 64) {
-        LAUNCH_SWEEP(2);
+        LAUNCH_CPL(2);
     } else if (comps <= 128) {
-        LAUNCH_SWEEP(4);
+        LAUNCH_CPL(4);
     } else if (comps <= 256) {
-        LAUNCH_SWEEP(8);
-    } else if (comps <= 512) {
-        LAUNCH_SWEEP(16);
+        LAUNCH_CPL(8);
     } else {
-        throw Error(1, "the GPU hinge sweep supports at most 511 basis functions");
+        LAUNCH_CPL(10);
     }
+#undef LAUNCH_CPL
 #undef LAUNCH_SWEEP
     LAUNCH_CHECK();
     *launches += 1;
@@ -1061,18 +1264,18 @@ void append_store(cudaStream_t st, double w, float *Bo, size_t ldbo, float *BoC,
 
 // sum_i X[i,j]^2 per column as the reference's sequential fused chain
 // (marsalgo.cc:359-369).
-struct XSqChain {
+struct XSqChain {  // sum of squares of the X column j
     static constexpr bool kUsesY = false;
     const float *X;
     size_t ld;
+    __device__ __forceinline__ const float *column(int j) const { return X + (size_t)j * ld; }
+    __device__ __forceinline__ const float *ycolumn() const { return nullptr; }
     __device__ __forceinline__ float param(int) const { return 0.f; }
-    __device__ __forceinline__ float load(size_t i, int j, float) const { return X[i + (size_t)j * ld]; }
-    __device__ __forceinline__ float yload(size_t) const { return 0.f; }
+    __device__ __forceinline__ float value(float v, float) const { return v; }
     __device__ __forceinline__ double step(double acc, double v, double) const
     {
         return fma(v, v, acc);
     }
-    __device__ __forceinline__ double finish(double acc, int) const { return acc; }
 };
 
 void column_sumsq(cudaStream_t st, const float *X, size_t ldX, int n, int p, double *out,

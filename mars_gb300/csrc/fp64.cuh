@@ -21,6 +21,12 @@ struct FillSrc {
         const int xc = cand_x[j];
         return B[i + (size_t)cand_b[j] * ldB] * (X[i + (size_t)xc * ldX] * s[xc]);
     }
+    // The same value from its raw columns: combine(B[i, cand_b[j]], X[i, cand_x[j]], s[cand_x[j]]).
+    static constexpr int kRaw = 2;
+    __device__ __forceinline__ const float *raw0(int j) const { return B + (size_t)cand_b[j] * ldB; }
+    __device__ __forceinline__ const float *raw1(int j) const { return X + (size_t)cand_x[j] * ldX; }
+    __device__ __forceinline__ float param(int j) const { return s[cand_x[j]]; }
+    __device__ __forceinline__ static float combine(float b, float x, float sx) { return b * (x * sx); }
 };
 
 // Candidate column source: an already-stored f32 column Bx[:, col[j]] (col may be null).
@@ -33,6 +39,14 @@ struct StoredSrc {
         const int c = col ? col[j] : j;
         return Bx[i + (size_t)c * ldBx];
     }
+    static constexpr int kRaw = 1;
+    __device__ __forceinline__ const float *raw0(int j) const
+    {
+        return Bx + (size_t)(col ? col[j] : j) * ldBx;
+    }
+    __device__ __forceinline__ const float *raw1(int j) const { return raw0(j); }
+    __device__ __forceinline__ float param(int) const { return 0.f; }
+    __device__ __forceinline__ static float combine(float v, float, float) { return v; }
 };
 
 // One block of the hinge sweep: up to 8 candidates that share an input column.
@@ -51,15 +65,16 @@ struct ProjectScratch {
     double *T;  // [P][m]
 };
 
-template <class Src>
-void project_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, int n, int m,
+// Bo may be stored as f64 (the fit state) or f32 (the kernel-level entry points).
+template <class Src, class BoT>
+void project_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, int n, int m,
                   int P, const int *out_col, float *Bx, size_t ldBx, double *s_out,
                   const ProjectScratch &ws, long long *launches);
 
 // T[j][c] = sum_i Bo[i,c] * src(i, j) only, each entry one fused chain over
 // the rows in order (the reference's accumulation order).
-template <class Src>
-void tgemm_fp64(cudaStream_t st, const Src &src, const float *Bo, size_t ldbo, int n, int m,
+template <class Src, class BoT>
+void tgemm_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, int n, int m,
                 int P, double *T, long long *launches);
 
 // s[fired[q]] = snew[q] for q < nf.
@@ -88,7 +103,7 @@ int sweep_warps(int m, int candidates);
 // hold at most sweep_warps(m) candidates.
 void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *perm,
                 const float *xsort, const float *y, const float *B, size_t ldB,
-                const int *cand_b, const float *Bx, size_t ldBx, const float *Bo, size_t ldbo,
+                const int *cand_b, const float *Bx, size_t ldBx, const double *Bo, size_t ldbo,
                 const double *ybo, const double *ybx, int n, int m, int head, int tail,
                 int min_span, double tol, double *hsse, int *hrow, int warps_per_block,
                 long long *launches);
