@@ -108,6 +108,10 @@ struct mars_gpu_algo {
     int precision = MARS_GPU_PREC_FP64;
     std::vector<double> ybo;
     cudaStream_t st = nullptr;
+    // Side stream for the hinge-sweep scalar recurrences, which run
+    // concurrently with the projection (fork/join events below).
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     PhaseTimer timer;
     double phase_ms[PH_N] = {0};
     cudaEvent_t span_begin = nullptr, span_end = nullptr;
@@ -117,10 +121,11 @@ struct mars_gpu_algo {
     // Host copy of the basis, kept in the reference's exact arithmetic.
     HostBasis hb;
     // Resident state.
-    DevBuf X, s, y, B, Bo, BoC, ybo_d, perm, xsort;
+    DevBuf X, s, y, B, Bo, BoC, ybo_d, perm, xsort, ysort;
     std::vector<char> sorted;
     // Per-eval scratch (grow-only).
-    DevBuf Bx, T, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks;
+    DevBuf Bx, T, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks, stasks, scal;
+    DevBuf bsort, bxsort;  // per candidate: parent and normalised column in sorted order
     DevBuf sort_keys, sort_vals, sort_tmp;
 
     ~mars_gpu_algo()
@@ -128,6 +133,16 @@ struct mars_gpu_algo {
         if (st) {
             cudaStreamSynchronize(st);
             cudaStreamDestroy(st);
+        }
+        if (st2) {
+            cudaStreamSynchronize(st2);
+            cudaStreamDestroy(st2);
+        }
+        if (ev_fork) {
+            cudaEventDestroy(ev_fork);
+        }
+        if (ev_join) {
+            cudaEventDestroy(ev_join);
         }
         if (span_begin) {
             cudaEventDestroy(span_begin);
@@ -189,6 +204,9 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     a->ybo = a->hb.ybo;
     std::memset(&a->stats, 0, sizeof(a->stats));
     CUDA_CHECK(cudaStreamCreateWithFlags(&a->st, cudaStreamNonBlocking));
+    CUDA_CHECK(cudaStreamCreateWithFlags(&a->st2, cudaStreamNonBlocking));
+    CUDA_CHECK(cudaEventCreateWithFlags(&a->ev_fork, cudaEventDisableTiming));
+    CUDA_CHECK(cudaEventCreateWithFlags(&a->ev_join, cudaEventDisableTiming));
     CUDA_CHECK(cudaEventCreate(&a->span_begin));
     CUDA_CHECK(cudaEventCreate(&a->span_end));
     a->timer.st = a->st;
@@ -265,10 +283,12 @@ void ensure_sorted(mars_gpu_algo *a, const std::vector<int> &cols)
     const size_t np = a->n * a->p;
     a->perm.ensure(sizeof(int) * np);
     a->xsort.ensure(sizeof(float) * np);
+    a->ysort.ensure(sizeof(float) * np);
     cudaEvent_t t0 = a->timer.begin();
-    sort_columns(a->st, a->X.as<float>(), a->n, a->s.as<float>(), (int)a->n, todo.data(),
-                 (int)todo.size(), a->perm.as<int>(), a->xsort.as<float>(), a->sort_keys,
-                 a->sort_vals, a->sort_tmp, &a->stats.kernel_launches);
+    sort_columns(a->st, a->X.as<float>(), a->n, a->s.as<float>(), a->y.as<float>(), (int)a->n,
+                 todo.data(), (int)todo.size(), a->perm.as<int>(), a->xsort.as<float>(),
+                 a->ysort.as<float>(), a->sort_keys, a->sort_vals, a->sort_tmp,
+                 &a->stats.kernel_launches);
     a->timer.end(PH_SORT, t0);
     for (int c : todo) {
         a->sorted[c] = 1;
@@ -288,6 +308,36 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
     double *s = a->svec.as<double>();
 
     a->stats.project_flops += 4.0 * (double)n * (double)m * (double)Pc;
+    // The sweep's scalar recurrences need only the parents, y and the sorted
+    // inputs: start them on the side stream, concurrent with the projection.
+    if (!linear_only) {
+        std::vector<SweepTask> stasks;
+        for (int b = 0; b < Pc;) {
+            int e = b;
+            while (e < Pc && cx_h[c0 + e] == cx_h[c0 + b]) {
+                ++e;
+            }
+            for (int t = b; t < e; t += 32) {
+                stasks.push_back({cx_h[c0 + b], t, std::min(32, e - t)});
+            }
+            b = e;
+        }
+        a->stasks.ensure(sizeof(SweepTask) * stasks.size());
+        CUDA_CHECK(cudaMemcpyAsync(a->stasks.ptr, stasks.data(),
+                                   sizeof(SweepTask) * stasks.size(), cudaMemcpyHostToDevice,
+                                   a->st));
+        a->stats.h2d_bytes += (long long)(sizeof(SweepTask) * stasks.size());
+        // The gather is a wide, short kernel: on the handle's stream, so it does
+        // not crowd out the single-wave chain kernels that the scalars overlap.
+        gather_parents(a->st, a->perm.as<int>(), a->B.as<float>(), a->n, cx_d, cb_d, n, tail, Pc,
+                       a->bsort.as<float>(), &a->stats.kernel_launches);
+        CUDA_CHECK(cudaEventRecord(a->ev_fork, a->st));
+        CUDA_CHECK(cudaStreamWaitEvent(a->st2, a->ev_fork, 0));
+        hinge_scalars(a->st2, a->stasks.as<SweepTask>(), (int)stasks.size(), a->xsort.as<float>(),
+                      a->ysort.as<float>(), a->bsort.as<float>(), n, head, tail, min_span,
+                      a->scal.as<double>(), &a->stats.kernel_launches);
+        CUDA_CHECK(cudaEventRecord(a->ev_join, a->st2));
+    }
     cudaEvent_t t0 = a->timer.begin();
     FillSrc src{a->B.as<float>(), a->n, a->X.as<float>(), a->n, a->s.as<float>(), cx_d, cb_d};
     project_fp64(a->st, src, a->Bo.as<double>(), a->ldbo, n, m, Pc, nullptr, Bx, a->n, s, ws,
@@ -311,8 +361,12 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
     a->timer.end(PH_DGKS, t0);
 
     t0 = a->timer.begin();
-    normalize_ybx(a->st, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), !linear_only,
+    normalize_ybx(a->st, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), false,
                   a->ybx.as<double>(), &a->stats.kernel_launches);
+    if (!linear_only) {
+        gather_candidates(a->st, a->perm.as<int>(), Bx, a->n, cx_d, s, a->tol, n, tail, Pc,
+                          a->bxsort.as<float>(), &a->stats.kernel_launches);
+    }
     a->timer.end(PH_NORMALIZE, t0);
 
     if (linear_only) {
@@ -334,15 +388,16 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
     a->tasks.ensure(sizeof(SweepTask) * tasks.size());
     CUDA_CHECK(cudaMemcpyAsync(a->tasks.ptr, tasks.data(), sizeof(SweepTask) * tasks.size(),
                                cudaMemcpyHostToDevice, a->st));
+    a->stats.h2d_bytes += (long long)(sizeof(SweepTask) * tasks.size());
+    CUDA_CHECK(cudaStreamWaitEvent(a->st, a->ev_join, 0));
     t0 = a->timer.begin();
     sweep_fp64(a->st, a->tasks.as<SweepTask>(), (int)tasks.size(), a->perm.as<int>(),
-               a->xsort.as<float>(), a->y.as<float>(), a->B.as<float>(), a->n, cb_d, Bx, a->n,
-               a->Bo.as<double>(), a->ldbo, a->ybo_d.as<double>(), a->ybx.as<double>(), n, m,
-               head, tail, min_span, a->tol, a->hsse.as<double>(), a->hrow.as<int>(), warps,
-               &a->stats.kernel_launches);
+               a->xsort.as<float>(), a->bsort.as<float>(), a->bxsort.as<float>(),
+               a->Bo.as<double>(), a->ldbo, a->ybo_d.as<double>(), a->ybx.as<double>(),
+               a->scal.as<double>(), n, m, head, tail, min_span, a->tol, a->hsse.as<double>(),
+               a->hrow.as<int>(), warps, &a->stats.kernel_launches);
     a->timer.end(PH_SWEEP, t0);
-    a->stats.knot_evals += (long long)Pc *
-                           (tail - 1 >= head + 1 ? ((tail - 1 - (head + 1)) / min_span + 1) : 0);
+    a->stats.knot_evals += (long long)Pc * sweep_grid_rows(head, tail, min_span);
 }
 
 void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, int min_span,
@@ -387,7 +442,10 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         const double budget = env_double("MARS_GPU_BLOCK_GB", 32.0) * 1e9;
         // Candidate columns per block: the Bx scratch budget, and at most
         // 2^18 so every per-column grid dimension stays within 65535 blocks.
-        size_t cap = (size_t)std::max(1.0, budget / (4.0 * n + 64.0 * m + 64.0));
+        const double ngrid = linear_only ? 0.0 : (double)sweep_grid_rows(head, tail, min_span);
+        const double sorted_b = linear_only ? 0.0 : 8.0 * n;  // bsort + bxsort
+        size_t cap = (size_t)std::max(
+            1.0, budget / (4.0 * n + sorted_b + 24.0 * ngrid + 64.0 * m + 64.0));
         cap = std::min<size_t>(cap, 262144);
         const auto blocks = block_candidates(cx, cap);
         size_t maxPc = 0;
@@ -401,6 +459,12 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         a->ybx.ensure(sizeof(double) * maxPc);
         a->hsse.ensure(sizeof(double) * maxPc);
         a->hrow.ensure(sizeof(int) * maxPc);
+        if (!linear_only) {
+            a->scal.ensure(sizeof(double) * 3 *
+                           std::max<size_t>(1, maxPc * (size_t)sweep_grid_rows(head, tail, min_span)));
+            a->bsort.ensure(sizeof(float) * a->n * maxPc);
+            a->bxsort.ensure(sizeof(float) * a->n * maxPc);
+        }
         a->fired.ensure(sizeof(int) * maxPc);
         a->nfired.ensure(sizeof(int) * 4);
         a->cand.ensure(sizeof(int) * 2 * (size_t)P);

@@ -399,115 +399,90 @@ __global__ void __launch_bounds__(NM_THREADS)
 // FP64 hinge sweep (marsalgo.cc:576-649 with covariates_impl :91-151), in the
 // reference's operation order.
 //
-// Block = one input column and up to W <= 5 candidates (parent columns):
+// Block = one input column and up to W candidates (parent columns):
 //   warps 0..W-1  one candidate each; lane l holds components c = l + 32 q of
 //                 the running f and g (component m is the candidate column Bx)
-//   warp  W       the six scalar recurrences (k0, k1, w, bd, b2, vb) of the W
-//                 candidates, one lane per (candidate, recurrence): one FMA
-//                 warp instruction per row for all of them, each lane taking
-//                 the previous row's value of the recurrence it reads from
-//                 another lane by a shuffle
-//   warp  W+1     the loader: keeps S - 1 stages of SW_ROWS sorted rows in
+//   warp  W       the loader: keeps S - 1 stages of SW_ROWS sorted rows in
 //                 flight with cp.async -- each gathered row of the f64 Bo is
-//                 one warp instruction (lanes over components); y and the B
-//                 and Bx values of every candidate (f32, lanes over rows) are
+//                 one warp instruction (lanes over components); the B and Bx
+//                 values of every candidate (f32, lanes over rows) are
 //                 converted to f64 once, one stage ahead of their use; the
-//                 deltas of the sorted x (and delta^2, 2 delta) are formed at
-//                 issue from the permutation and x prefetched one stage ahead
-// At a grid row each candidate warp saves f in a snapshot slot and the scalar
-// warp saves k0 + k1 and w; when SW_SNAP slots are in use, lane q of each
-// candidate warp scores slot q with the reference's sequential chains
-// ff = sum_c f_c^2 and fy = sum_c f_c yc_c (c = 0..m) and the warp keeps the
-// first maximum in row order.
+//                 deltas of the sorted x are formed at issue from the
+//                 permutation and x prefetched one stage ahead
+// The six scalar recurrences (k0, k1, w and their helpers) do not depend on
+// the basis and come precomputed per grid row from k_hinge_scalars. At a grid
+// row each candidate warp saves f in a snapshot slot; when SW_SNAP slots are
+// in use, lane q of each candidate warp scores slot q with the reference's
+// sequential chains ff = sum_c f_c^2 and fy = sum_c f_c yc_c (c = 0..m),
+// den = (k0 + k1) - ff, uw = fy - w, and the warp keeps the first maximum in
+// row order.
 // ---------------------------------------------------------------------------
 constexpr int SW_ROWS = 32, SW_SNAP = 32, SW_MAXW = 5;
 
 struct SweepSmem {
     // byte offsets into the dynamic shared memory (f64 regions first)
-    size_t snap, mk, mw, ybo, d, dd, d2, bo, cvt, raw, total;
+    size_t snap, ybo, bo, cvt, raw, total;
     __host__ __device__ SweepSmem(int m, int W, int S)
     {
-        const int nv = 2 * W + 1;  // B and Bx of each candidate, then y
         size_t o = 0;
         snap = o;
         o += 8 * (size_t)W * SW_SNAP * (m + 1);
-        mk = o;
-        o += 8 * (size_t)W * SW_SNAP;
-        mw = o;
-        o += 8 * (size_t)W * SW_SNAP;
         ybo = o;
         o += 8 * ((size_t)m + 1);
-        d = o;
-        o += 8 * (size_t)S * SW_ROWS;
-        dd = o;
-        o += 8 * (size_t)S * SW_ROWS;
-        d2 = o;
-        o += 8 * (size_t)S * SW_ROWS;
-        bo = o;
+        bo = o;  // [S][SW_ROWS][m] f64 rows of Bo
         o += 8 * (size_t)S * SW_ROWS * m;
-        cvt = o;
-        o += 8 * 2 * (size_t)nv * SW_ROWS;
-        raw = o;
-        o += 4 * (size_t)S * nv * SW_ROWS;
+        cvt = o;  // [2][2W + 1][SW_ROWS] f64: B and Bx of each candidate, then the deltas
+        o += 8 * 2 * (size_t)(2 * W + 1) * SW_ROWS;
+        raw = o;  // [S][2W * SW_ROWS + SW_ROWS + 1] f32: B, Bx, then x from row i0 - 1
+        o += 4 * (size_t)S * (2 * W * SW_ROWS + SW_ROWS + 1);
         total = (o + 15) / 16 * 16;
     }
 };
 
 template <int CPL, int S>
-__global__ void __launch_bounds__(32 * (SW_MAXW + 2), 1)
+__global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
     k_sweep(const SweepTask *__restrict__ tasks, const int *__restrict__ perm,
-            const float *__restrict__ xsort, const float *__restrict__ y,
-            const float *__restrict__ B, size_t ldB, const int *__restrict__ cand_b,
-            const float *__restrict__ Bx, size_t ldBx, const double *__restrict__ Bo,
-            size_t ldbo, const double *__restrict__ ybo, const double *__restrict__ ybx, int n,
-            int m, int head, int tail, int min_span, double tol, double *__restrict__ hsse,
-            int *__restrict__ hrow)
+            const float *__restrict__ xsort, const float *__restrict__ bs,
+            const float *__restrict__ bxs, const double *__restrict__ Bo, size_t ldbo,
+            const double *__restrict__ ybo, const double *__restrict__ ybx,
+            const double *__restrict__ scal, int ngrid, int n, int m, int head, int tail,
+            int min_span, double tol, double *__restrict__ hsse, int *__restrict__ hrow)
 {
     extern __shared__ __align__(16) unsigned char sraw[];
-    const int W = (blockDim.x >> 5) - 2;  // candidate warps
+    const int W = (blockDim.x >> 5) - 1;  // candidate warps
     const int NV = 2 * W + 1;
+    const int RAW = 2 * W * SW_ROWS + SW_ROWS + 1;
     const SweepSmem L(m, W, S);
     const int ldF = m + 1;
     double *snapbase = reinterpret_cast<double *>(sraw + L.snap);
-    double *mk = reinterpret_cast<double *>(sraw + L.mk);
-    double *mw = reinterpret_cast<double *>(sraw + L.mw);
     double *sybo = reinterpret_cast<double *>(sraw + L.ybo);
-    double *sd = reinterpret_cast<double *>(sraw + L.d);
-    double *sdd = reinterpret_cast<double *>(sraw + L.dd);
-    double *sd2 = reinterpret_cast<double *>(sraw + L.d2);
     double *sbo = reinterpret_cast<double *>(sraw + L.bo);
     double *scvt = reinterpret_cast<double *>(sraw + L.cvt);  // [2][NV][SW_ROWS]
-    float *sraw4 = reinterpret_cast<float *>(sraw + L.raw);   // [S][NV][SW_ROWS]
+    float *sraw4 = reinterpret_cast<float *>(sraw + L.raw);   // [S][RAW]
     __shared__ int srow[SW_SNAP];
-    __shared__ int sbcol[SW_MAXW];
 
     const SweepTask task = tasks[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool cwarp = warp < task.count;
-    const bool swarp = warp == W;
-    const bool lwarp = warp == W + 1;
+    const bool lwarp = warp == W;
     const int *pk = perm + (size_t)task.xcol * n;
     const float *xs = xsort + (size_t)task.xcol * n;
+    const float *bsb = bs + (size_t)task.cand0 * n;
+    const float *bxb = bxs + (size_t)task.cand0 * n;
 
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
         sybo[c] = ybo[c];
     }
-    if (threadIdx.x < task.count) {
-        sbcol[threadIdx.x] = cand_b[task.cand0 + threadIdx.x];
-    }
     __syncthreads();
 
     const int nstages = (tail + SW_ROWS - 1) / SW_ROWS;
-    // Loader registers: row index and sorted x (and its predecessor) of this
-    // lane's row in the next stage to issue.
+    // Loader: the permutation of this lane's row in the next stage to issue,
+    // prefetched one stage ahead (it addresses the Bo row gathers).
     int pf_k = 0;
-    float pf_x = 0.f, pf_xp = 0.f;
     auto prefetch = [&](int sq) {
         const int i = sq * SW_ROWS + lane;
         if (sq < nstages && i < tail) {
             pf_k = pk[i];
-            pf_x = xs[i];
-            pf_xp = i > 0 ? xs[i - 1] : 0.f;
         }
     };
     auto issue = [&](int sq) {
@@ -522,32 +497,34 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2), 1)
                 cp_async<8>(bo + r * m + c, src + c);
             }
         }
-        if (lane < rows) {
-            float *rw = sraw4 + (size_t)sg * NV * SW_ROWS;
-            for (int cw = 0; cw < task.count; ++cw) {
-                cp_async4(rw + cw * SW_ROWS + lane, B + (size_t)k + (size_t)sbcol[cw] * ldB);
-                cp_async4(rw + (W + cw) * SW_ROWS + lane,
-                          Bx + (size_t)k + (size_t)(task.cand0 + cw) * ldBx);
-            }
-            cp_async4(rw + 2 * W * SW_ROWS + lane, y + k);
-            const double dl = i0 + lane > 0 ? (double)(pf_xp - pf_x) : 0.0;
-            sd[sg * SW_ROWS + lane] = dl;
-            sdd[sg * SW_ROWS + lane] = dl * dl;
-            sd2[sg * SW_ROWS + lane] = dl * 2;
+        // B, Bx (sorted per candidate) and x: coalesced, lanes over rows
+        float *rw = sraw4 + (size_t)sg * RAW;
+        const int i = i0 + lane;
+        const bool ok = lane < rows;
+        for (int cw = 0; cw < task.count; ++cw) {
+            cp_async4(rw + cw * SW_ROWS + lane, bsb + (size_t)cw * n + (ok ? i : 0), ok);
+            cp_async4(rw + (W + cw) * SW_ROWS + lane, bxb + (size_t)cw * n + (ok ? i : 0), ok);
+        }
+        cp_async4(rw + 2 * W * SW_ROWS + 1 + lane, xs + (ok ? i : 0), ok);
+        if (lane == 0) {
+            cp_async4(rw + 2 * W * SW_ROWS, xs + (i0 > 0 ? i0 - 1 : 0), i0 > 0);
         }
     };
     auto convert = [&](int sq) {  // stage sq (landed) -> f64 slot sq & 1, lanes over rows
-        const float *rw = sraw4 + (size_t)(sq % S) * NV * SW_ROWS;
+        const float *rw = sraw4 + (size_t)(sq % S) * RAW;
         double *cv = scvt + (size_t)(sq & 1) * NV * SW_ROWS;
         for (int cw = 0; cw < task.count; ++cw) {
             cv[cw * SW_ROWS + lane] = (double)rw[cw * SW_ROWS + lane];
             cv[(W + cw) * SW_ROWS + lane] = (double)rw[(W + cw) * SW_ROWS + lane];
         }
-        cv[2 * W * SW_ROWS + lane] = (double)rw[2 * W * SW_ROWS + lane];
+        const float *xr = rw + 2 * W * SW_ROWS;  // xr[r] = x of row i0 + r - 1
+        cv[2 * W * SW_ROWS + lane] =
+            sq * SW_ROWS + lane > 0 ? (double)(xr[lane] - xr[lane + 1]) : 0.0;
     };
 
     const int mycand = task.cand0 + (cwarp ? warp : 0);
     const double ybx_c = ybx[mycand];
+    const double *mysc = scal + (size_t)mycand * ngrid * 3;
     double *snap = snapbase + (size_t)(cwarp ? warp : 0) * SW_SNAP * ldF;
     double f[CPL], g[CPL];
 #pragma unroll
@@ -555,11 +532,6 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2), 1)
         f[q] = 0.0;
         g[q] = 0.0;
     }
-    // scalar warp: lane = 6 * candidate + recurrence (b2, vb, bd, w, k0, k1)
-    const int sc = lane / 6, role = lane % 6;
-    const bool sact = swarp && sc < task.count;
-    const int ssrc = sc * 6 + (role == 3 ? 1 : role == 5 ? 2 : role >= 2 ? 0 : role);
-    double sacc = 0.0;
     double best = 0.0;
     int besti = -1;
     int nsnap = 0;  // block-uniform
@@ -570,6 +542,9 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2), 1)
             double sse = -1.0;
             int row = 0x7fffffff;
             if (lane < nsnap) {
+                row = srow[lane];
+                const double *sc = mysc + (size_t)((row - (head + 1)) / min_span) * 3;
+                const double k0 = sc[0], k1 = sc[1], w = sc[2];
                 const double *fs = snap + (size_t)lane * ldF;
                 double ff = 0.0, fy = 0.0;
                 for (int c = 0; c < m; ++c) {
@@ -578,10 +553,9 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2), 1)
                 }
                 ff = fma(fs[m], fs[m], ff);
                 fy = fma(fs[m], ybx_c, fy);
-                const double uw = fy - mw[warp * SW_SNAP + lane];
-                const double den = mk[warp * SW_SNAP + lane] - ff;
+                const double uw = fy - w;
+                const double den = (k0 + k1) - ff;
                 sse = den > tol ? (uw * uw) / (den + tol) : 0.0;
-                row = srow[lane];
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -628,11 +602,11 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2), 1)
             flush();
             __syncthreads();  // slots are rewritten below
         }
-        const double *cv = scvt + (size_t)h * NV * SW_ROWS;
-        const double *dv = sd + sg * SW_ROWS;
         if (cwarp) {
+            const double *cv = scvt + (size_t)h * NV * SW_ROWS;
             const double *bw = cv + warp * SW_ROWS;
             const double *xw = cv + (W + warp) * SW_ROWS;
+            const double *dv = cv + 2 * W * SW_ROWS;
             const double *rowb = sbo + (size_t)sg * SW_ROWS * m;
             long ng = next_grid;
             int slot = nsnap;
@@ -644,7 +618,8 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2), 1)
 #pragma unroll
                 for (int q = 0; q < CPL; ++q) {
                     const int c = lane + 32 * q;
-                    const double xv = c < m ? rowp[c] : (c == m ? bxk : 0.0);
+                    const double bv = rowp[min(c, m - 1)];  // unconditional load, then select
+                    const double xv = c < m ? bv : (c == m ? bxk : 0.0);
                     f[q] = fma(di, g[q], f[q]);
                     g[q] = fma(bk, xv, g[q]);
                 }
@@ -660,42 +635,6 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2), 1)
                     }
                     if (lane == 0 && warp == 0) {
                         srow[slot] = i;
-                    }
-                    ++slot;
-                }
-            }
-        } else if (swarp) {
-            // marsalgo.cc covariates_impl order: k0 += dd b2; k1 += 2d bd; w += d vb;
-            // bd += d b2; b2 += bk^2; vb += yk bk (right-hand sides are the previous
-            // row's values); the first row sets vb = bk yk, b2 = bk^2.
-            const double *bw = cv + (sc < W ? sc : 0) * SW_ROWS;
-            const double *yw = cv + 2 * W * SW_ROWS;
-            const double *ddv = sdd + sg * SW_ROWS;
-            const double *d2v = sd2 + sg * SW_ROWS;
-            long ng = next_grid;
-            int slot = nsnap;
-            for (int r = 0; r < rows; ++r) {
-                const int i = i0 + r;
-                const double bk = bw[r], yk = yw[r];
-                const double other = __shfl_sync(0xffffffffu, sacc, ssrc);
-                if (i == 0) {
-                    if (role <= 1) {
-                        sacc = fma(role == 0 ? bk : yk, bk, -0.0);
-                    }
-                    continue;
-                }
-                const double a = role == 0 ? bk : role == 1 ? yk : role == 4 ? ddv[r]
-                                                     : role == 5 ? d2v[r] : dv[r];
-                const double b = role <= 1 ? bk : other;
-                sacc = fma(a, b, sacc);
-                if (i == ng) {
-                    ng += min_span;
-                    const double k1v = __shfl_down_sync(0xffffffffu, sacc, 1);
-                    if (sact && role == 4) {
-                        mk[sc * SW_SNAP + slot] = sacc + k1v;
-                    }
-                    if (sact && role == 3) {
-                        mw[sc * SW_SNAP + slot] = sacc;
                     }
                     ++slot;
                 }
@@ -725,6 +664,155 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 2), 1)
     }
 }
 
+// ---------------------------------------------------------------------------
+// The hinge sweep's scalar recurrences (marsalgo.cc:91-151 covariates_impl,
+// used at :603-626): per row i >= 1 of the descending sort, with the previous
+// row's values on the right-hand sides,
+//   k0 += d^2 b2;  k1 += 2d bd;  w += d vb;  bd += d b2;  b2 += bk^2;  vb += yk bk,
+// and vb = bk yk, b2 = bk^2 on the first row. They depend on the parent
+// column, y and the sorted input only -- not on the basis or the candidate
+// column -- so they run here, concurrently with the projection, and the sweep
+// reads k0, k1, w at its grid rows.
+//
+// Block = one input column and up to 32 parents (lane = parent). A result of
+// GB300's FP64 pipe reaches a dependent FP64 instruction after ~86 cycles but
+// a shuffle or store only after a few hundred, so no value crosses lanes or
+// warps per row; instead the six chains are split over three warps, none of
+// them issuing more than three FMAs per row:
+//   warp 0: vb, w      warp 1: b2, bd, k1      warp 2: b2, k0
+// (b2 is computed twice, identically). Warp 3 stages the rows with coalesced
+// cp.async from the sorted copies (the parents' B per candidate, y and x per
+// input column) and converts them to f64 once, with the deltas.
+// Output per candidate and grid row g: scal[(cand * ngrid + g) * 3 + {0,1,2}] =
+// k0, k1, w.
+// ---------------------------------------------------------------------------
+constexpr int SC_ROWS = 32, SC_STAGES = 4, SC_THREADS = 128, SC_MAXP = 32;
+
+__global__ void __launch_bounds__(SC_THREADS)
+    k_hinge_scalars(const SweepTask *__restrict__ tasks, const float *__restrict__ xsort,
+                    const float *__restrict__ ysort, const float *__restrict__ bs, int n,
+                    int head, int tail, int min_span, int ngrid, double *__restrict__ scal)
+{
+    constexpr int S = SC_STAGES;
+    __shared__ float rb[S][SC_MAXP][SC_ROWS];  // B of each parent, lanes over rows
+    __shared__ float ry[S][SC_ROWS];
+    __shared__ float rx[S][SC_ROWS + 1];  // x of rows i0 - 1 .. i0 + 31
+    __shared__ double db[2][SC_ROWS][SC_MAXP + 1];
+    __shared__ double dy[2][SC_ROWS];
+    __shared__ double sd[2][SC_ROWS], sdd[2][SC_ROWS], sd2[2][SC_ROWS];
+
+    const SweepTask task = tasks[blockIdx.x];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float *xs = xsort + (size_t)task.xcol * n;
+    const float *ys = ysort + (size_t)task.xcol * n;
+    const float *bsb = bs + (size_t)task.cand0 * n;
+    const int nstages = (tail + SC_ROWS - 1) / SC_ROWS;
+    const bool lwarp = warp == 3;
+
+    auto issue = [&](int sq) {
+        const int sg = sq % S, i0 = sq * SC_ROWS, i = i0 + lane;
+        const bool ok = i < tail;
+        for (int q = 0; q < task.count; ++q) {
+            cp_async4(&rb[sg][q][lane], bsb + (size_t)q * n + (ok ? i : 0), ok);
+        }
+        cp_async4(&ry[sg][lane], ys + (ok ? i : 0), ok);
+        cp_async4(&rx[sg][lane + 1], xs + (ok ? i : 0), ok);
+        if (lane == 0) {
+            cp_async4(&rx[sg][0], xs + (i0 > 0 ? i0 - 1 : 0), i0 > 0);
+        }
+    };
+    auto convert = [&](int sq) {  // stage sq (landed) -> f64 slot sq & 1, lanes over rows
+        const int sg = sq % S, h = sq & 1, i = sq * SC_ROWS + lane;
+        for (int q = 0; q < task.count; ++q) {
+            db[h][lane][q] = (double)rb[sg][q][lane];
+        }
+        dy[h][lane] = (double)ry[sg][lane];
+        const double dl = i > 0 ? (double)(rx[sg][lane] - rx[sg][lane + 1]) : 0.0;
+        sd[h][lane] = dl;
+        sdd[h][lane] = dl * dl;
+        sd2[h][lane] = dl * 2;
+    };
+
+    if (lwarp) {
+#pragma unroll
+        for (int q = 0; q < S - 1; ++q) {
+            if (q < nstages) {
+                issue(q);
+            }
+            cp_async_commit();
+        }
+        cp_async_wait<S - 2>();
+        __syncwarp();
+        if (nstages > 0) {
+            convert(0);
+        }
+    }
+    __syncthreads();
+    const bool active = !lwarp && lane < task.count;
+    double *out = scal + (size_t)(task.cand0 + (lane < task.count ? lane : 0)) * ngrid * 3;
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+    long ng = (long)head + 1;
+    int gi = 0;
+    for (int sq = 0; sq < nstages; ++sq) {
+        const int h = sq & 1, i0 = sq * SC_ROWS;
+        const int rows = min(SC_ROWS, tail - i0);
+        if (active) {
+            const double *dv = sd[h], *ddv = sdd[h], *d2v = sd2[h];
+            for (int r = 0; r < rows; ++r) {
+                const int i = i0 + r;
+                const double bk = db[h][r][lane];
+                if (warp == 0) {  // v0 = vb, v1 = w
+                    const double yk = dy[h][r];
+                    if (i == 0) {
+                        v0 = bk * yk;
+                    } else {
+                        v1 = fma(dv[r], v0, v1);
+                        v0 = fma(yk, bk, v0);
+                    }
+                } else if (warp == 1) {  // v0 = b2, v1 = bd, v2 = k1
+                    if (i == 0) {
+                        v0 = bk * bk;
+                    } else {
+                        v2 = fma(d2v[r], v1, v2);
+                        v1 = fma(dv[r], v0, v1);
+                        v0 = fma(bk, bk, v0);
+                    }
+                } else {  // v0 = b2, v1 = k0
+                    if (i == 0) {
+                        v0 = bk * bk;
+                    } else {
+                        v1 = fma(ddv[r], v0, v1);
+                        v0 = fma(bk, bk, v0);
+                    }
+                }
+                if (i == ng) {
+                    ng += min_span;
+                    double *o = out + (size_t)gi * 3;
+                    if (warp == 0) {
+                        o[2] = v1;
+                    } else if (warp == 1) {
+                        o[1] = v2;
+                    } else {
+                        o[0] = v1;
+                    }
+                    ++gi;
+                }
+            }
+        } else if (lwarp) {
+            if (sq + S - 1 < nstages) {
+                issue(sq + S - 1);
+            }
+            cp_async_commit();
+            cp_async_wait<S - 2>();
+            __syncwarp();
+            if (sq + 1 < nstages) {
+                convert(sq + 1);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void k_sort_keys(const float *__restrict__ X, size_t ldX, int n, int col,
                             float *__restrict__ keys, int *__restrict__ vals)
 {
@@ -737,12 +825,50 @@ __global__ void k_sort_keys(const float *__restrict__ X, size_t ldX, int n, int 
 }
 
 __global__ void k_gather_scaled(const float *__restrict__ X, size_t ldX, const float *__restrict__ s,
-                                int n, int col, const int *__restrict__ perm,
-                                float *__restrict__ xsort)
+                                const float *__restrict__ y, int n, int col,
+                                const int *__restrict__ perm, float *__restrict__ xsort,
+                                float *__restrict__ ysort)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        xsort[i] = X[perm[i] + (size_t)col * ldX] * s[col];
+        const int k = perm[i];
+        xsort[i] = X[k + (size_t)col * ldX] * s[col];
+        ysort[i] = y[k];
+    }
+}
+
+// Per candidate j, its parent column B[:, cand_b[j]] in the descending order
+// of its input column: bs[j * n + i] = B[perm_x[i], cand_b[j]], i < rows.
+__global__ void k_gather_parent(const int *__restrict__ perm, const float *__restrict__ B,
+                                size_t ldB, const int *__restrict__ cand_x,
+                                const int *__restrict__ cand_b, int n, int rows, int P,
+                                float *__restrict__ bs)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int j = blockIdx.y; j < P; j += gridDim.y) {
+        if (i < rows) {
+            const int k = perm[(size_t)cand_x[j] * n + i];
+            bs[(size_t)j * n + i] = B[(size_t)k + (size_t)cand_b[j] * ldB];
+        }
+    }
+}
+
+// Per candidate j, its normalised column in the descending order of its
+// input column: bxs[j * n + i] = Bx[perm_x[i], j] * scale_j (the f32 product
+// of kernels.cc:401-416).
+__global__ void k_gather_scaled_candidate(const int *__restrict__ perm,
+                                          const float *__restrict__ Bx, size_t ldBx,
+                                          const int *__restrict__ cand_x,
+                                          const double *__restrict__ s, double tol, int n,
+                                          int rows, int P, float *__restrict__ bxs)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int j = blockIdx.y; j < P; j += gridDim.y) {
+        const float sc = norm_scale(s[j], tol);
+        if (i < rows) {
+            const int k = perm[(size_t)cand_x[j] * n + i];
+            bxs[(size_t)j * n + i] = Bx[(size_t)k + (size_t)j * ldBx] * sc;
+        }
     }
 }
 
@@ -1110,22 +1236,69 @@ static size_t sweep_smem(int m, int w, int stages) { return SweepSmem(m, w, stag
 
 int sweep_warps(int m, int candidates)
 {
-    int w = 4;
-    while (w > 2 && (candidates + w - 1) / w < 2 * 152) {
-        --w;
-    }
+    // Each candidate warp issues two dependent FP64 FMAs per row and an SM
+    // sub-partition's FP64 pipe takes one warp instruction per ~64 cycles, so
+    // a candidate warp wants a sub-partition of its own: 4 candidates per
+    // block (warps map to sub-partitions by index mod 4; the light loader
+    // shares one), one block per SM up to 4 x 152 candidates, then 5.
+    int w = candidates <= 4 * 152 ? 4 : SW_MAXW;
     while (w > 1 && sweep_smem(m, w, 2) > 200 * 1024) {
         --w;
     }
     return w;
 }
 
+int sweep_grid_rows(int head, int tail, int min_span)
+{
+    return tail - 1 >= head + 1 ? (tail - 1 - (head + 1)) / min_span + 1 : 0;
+}
+
+void gather_parents(cudaStream_t st, const int *perm, const float *B, size_t ldB,
+                    const int *cand_x, const int *cand_b, int n, int rows, int P, float *bs,
+                    long long *launches)
+{
+    if (P <= 0 || rows <= 0) {
+        return;
+    }
+    const dim3 grid((unsigned)ceil_div(rows, 256), (unsigned)std::min(P, 65535));
+    k_gather_parent<<<grid, 256, 0, st>>>(perm, B, ldB, cand_x, cand_b, n, rows, P, bs);
+    LAUNCH_CHECK();
+    *launches += 1;
+}
+
+void gather_candidates(cudaStream_t st, const int *perm, const float *Bx, size_t ldBx,
+                       const int *cand_x, const double *s, double tol, int n, int rows, int P,
+                       float *bxs, long long *launches)
+{
+    if (P <= 0 || rows <= 0) {
+        return;
+    }
+    const dim3 grid((unsigned)ceil_div(rows, 256), (unsigned)std::min(P, 65535));
+    k_gather_scaled_candidate<<<grid, 256, 0, st>>>(perm, Bx, ldBx, cand_x, s, tol, n, rows, P,
+                                                    bxs);
+    LAUNCH_CHECK();
+    *launches += 1;
+}
+
+void hinge_scalars(cudaStream_t st, const SweepTask *tasks, int ntasks, const float *xsort,
+                   const float *ysort, const float *bs, int n, int head, int tail, int min_span,
+                   double *scal, long long *launches)
+{
+    if (ntasks <= 0) {
+        return;
+    }
+    k_hinge_scalars<<<ntasks, SC_THREADS, 0, st>>>(tasks, xsort, ysort, bs, n, head, tail,
+                                                   min_span, sweep_grid_rows(head, tail, min_span),
+                                                   scal);
+    LAUNCH_CHECK();
+    *launches += 1;
+}
+
 void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *perm,
-                const float *xsort, const float *y, const float *B, size_t ldB,
-                const int *cand_b, const float *Bx, size_t ldBx, const double *Bo, size_t ldbo,
-                const double *ybo, const double *ybx, int n, int m, int head, int tail,
-                int min_span, double tol, double *hsse, int *hrow, int warps_per_block,
-                long long *launches)
+                const float *xsort, const float *bs, const float *bxs, const double *Bo,
+                size_t ldbo, const double *ybo, const double *ybx, const double *scal, int n,
+                int m, int head, int tail, int min_span, double tol, double *hsse, int *hrow,
+                int warps_per_block, long long *launches)
 {
     if (ntasks <= 0) {
         return;
@@ -1142,15 +1315,16 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
         throw Error(1, "the GPU hinge sweep supports at most " + std::to_string(mmax) +
                            " basis functions");
     }
+    const int ngrid = sweep_grid_rows(head, tail, min_span);
     const int comps = m + 1;
 #define LAUNCH_SWEEP(CPL, S)                                                                   \
     do {                                                                                       \
         CUDA_CHECK(cudaFuncSetAttribute(k_sweep<CPL, S>,                                       \
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,           \
                                         (int)smem));                                           \
-        k_sweep<CPL, S><<<ntasks, 32 * (warps + 2), smem, st>>>(                               \
-            tasks, perm, xsort, y, B, ldB, cand_b, Bx, ldBx, Bo, ldbo, ybo, ybx, n, m, head,   \
-            tail, min_span, tol, hsse, hrow);                                                  \
+        k_sweep<CPL, S><<<ntasks, 32 * (warps + 1), smem, st>>>(                               \
+            tasks, perm, xsort, bs, bxs, Bo, ldbo, ybo, ybx, scal, ngrid, n, m, head, tail,    \
+            min_span, tol, hsse, hrow);                                                        \
     } while (0)
 #define LAUNCH_CPL(CPL)            \
     do {                           \
@@ -1177,9 +1351,9 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
     *launches += 1;
 }
 
-void sort_columns(cudaStream_t st, const float *X, size_t ldX, const float *s, int n,
-                  const int *cols, int ncols, int *perm, float *xsort, DevBuf &keys,
-                  DevBuf &vals, DevBuf &tmp, long long *launches)
+void sort_columns(cudaStream_t st, const float *X, size_t ldX, const float *s, const float *y,
+                  int n, const int *cols, int ncols, int *perm, float *xsort, float *ysort,
+                  DevBuf &keys, DevBuf &vals, DevBuf &tmp, long long *launches)
 {
     keys.ensure(2 * sizeof(float) * (size_t)n);
     vals.ensure(sizeof(int) * (size_t)n);
@@ -1197,7 +1371,8 @@ void sort_columns(cudaStream_t st, const float *X, size_t ldX, const float *s, i
         size_t bytes = tmp.bytes;
         CUDA_CHECK(cub::DeviceRadixSort::SortPairsDescending(tmp.ptr, bytes, k_in, k_out,
                                                              vals.as<int>(), pc, n, 0, 32, st));
-        k_gather_scaled<<<nb, 256, 0, st>>>(X, ldX, s, n, c, pc, xsort + (size_t)c * n);
+        k_gather_scaled<<<nb, 256, 0, st>>>(X, ldX, s, y, n, c, pc, xsort + (size_t)c * n,
+                                            ysort + (size_t)c * n);
         LAUNCH_CHECK();
         *launches += 2;  // the radix sort's own kernels are not counted
     }

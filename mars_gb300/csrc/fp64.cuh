@@ -99,20 +99,40 @@ void scale_columns(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const 
 // and `candidates` candidates in the launch.
 int sweep_warps(int m, int candidates);
 
-// Hinge sweep in FP64 (marsalgo.cc:508-657), one warp per candidate; tasks
-// hold at most sweep_warps(m) candidates.
-void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *perm,
-                const float *xsort, const float *y, const float *B, size_t ldB,
-                const int *cand_b, const float *Bx, size_t ldBx, const double *Bo, size_t ldbo,
-                const double *ybo, const double *ybx, int n, int m, int head, int tail,
-                int min_span, double tol, double *hsse, int *hrow, int warps_per_block,
-                long long *launches);
+// Number of grid rows (cut candidates) of the sweep: rows head+1, head+1+min_span, ... < tail.
+int sweep_grid_rows(int head, int tail, int min_span);
 
-// Stable descending argsort of X columns (marsalgo.cc:33-39) and the scaled
-// sorted values xsort[i] = X[perm[i]] * s.
-void sort_columns(cudaStream_t st, const float *X, size_t ldX, const float *s, int n,
-                  const int *cols, int ncols, int *perm, float *xsort, DevBuf &keys,
-                  DevBuf &vals, DevBuf &tmp, long long *launches);
+// The sweep's inputs in the descending order of each candidate's input
+// column: bs[j * n + i] = B[perm_x[i], cand_b[j]] and bxs[j * n + i] =
+// f32(Bx[perm_x[i], j] * scale_j), for sorted rows i < rows.
+void gather_parents(cudaStream_t st, const int *perm, const float *B, size_t ldB,
+                    const int *cand_x, const int *cand_b, int n, int rows, int P, float *bs,
+                    long long *launches);
+void gather_candidates(cudaStream_t st, const int *perm, const float *Bx, size_t ldBx,
+                       const int *cand_x, const double *s, double tol, int n, int rows, int P,
+                       float *bxs, long long *launches);
+
+// Scalar recurrences of the hinge sweep (k0, k1, w at every grid row) for the
+// candidates of `tasks` (at most 32 per task, one input column each), from the
+// sorted parents bs and the sorted y; scal holds (candidates,
+// sweep_grid_rows, 3) doubles.
+void hinge_scalars(cudaStream_t st, const SweepTask *tasks, int ntasks, const float *xsort,
+                   const float *ysort, const float *bs, int n, int head, int tail, int min_span,
+                   double *scal, long long *launches);
+
+// Hinge sweep in FP64 (marsalgo.cc:508-657), one warp per candidate; tasks
+// hold at most sweep_warps(m) candidates; scal from hinge_scalars.
+void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *perm,
+                const float *xsort, const float *bs, const float *bxs, const double *Bo,
+                size_t ldbo, const double *ybo, const double *ybx, const double *scal, int n,
+                int m, int head, int tail, int min_span, double tol, double *hsse, int *hrow,
+                int warps_per_block, long long *launches);
+
+// Stable descending argsort of X columns (marsalgo.cc:33-39), the scaled
+// sorted values xsort[i] = X[perm[i]] * s and the sorted target ysort[i] = y[perm[i]].
+void sort_columns(cudaStream_t st, const float *X, size_t ldX, const float *s, const float *y,
+                  int n, const int *cols, int ncols, int *perm, float *xsort, float *ysort,
+                  DevBuf &keys, DevBuf &vals, DevBuf &tmp, long long *launches);
 
 // Scatter per-candidate results into the (rows, m) outputs.
 void assemble_outputs(cudaStream_t st, int P, const int *cand_x, const int *cand_b, int m,
