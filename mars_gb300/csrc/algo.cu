@@ -5,11 +5,15 @@
 // in one call and the basis lives only in device memory.
 #include "../../include/mars_gpu.h"
 #include "common.cuh"
+#include "fast.cuh"
 #include "fp64.cuh"
 #include "host_exact.h"
 
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
+#include <limits>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -121,11 +125,13 @@ struct mars_gpu_algo {
     // Host copy of the basis, kept in the reference's exact arithmetic.
     HostBasis hb;
     // Resident state.
-    DevBuf X, s, y, B, Bo, BoC, ybo_d, perm, xsort, ysort;
+    DevBuf X, s, y, B, Bo, BoF, BoC, ybo_d, perm, xsort, ysort;
+    std::vector<int32_t> perm_h;  // host copy of the sorted permutations (exact re-decision)
     std::vector<char> sorted;
     // Per-eval scratch (grow-only).
     DevBuf Bx, T, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks, stasks, scal;
     DevBuf bsort, bxsort;  // per candidate: parent and normalised column in sorted order
+    DevBuf fTp, fT, fmom, hflag;  // fast pass: split-K partials, T, parent moments, sweep flags
     DevBuf sort_keys, sort_vals, sort_tmp;
 
     ~mars_gpu_algo()
@@ -175,13 +181,14 @@ void span_mark_end(mars_gpu_algo *a)
 }
 
 
-// Column c of the f64 row-major basis copy from the f32 column (exact widening).
+// Column c of the row-major basis copies (f64, exact widening, and f32) from the f32 column.
 __global__ void k_col_to_rows(const float *__restrict__ col, int n, double *__restrict__ Bo,
-                              size_t ldbo, int c)
+                              float *__restrict__ BoF, size_t ldbo, int c)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         Bo[(size_t)i * ldbo + c] = (double)col[i];
+        BoF[(size_t)i * ldbo + c] = col[i];
     }
 }
 
@@ -230,12 +237,14 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     a->BoC.ensure(sizeof(float) * n * max_terms);
     a->Bo.ensure(sizeof(double) * n * a->ldbo);
     CUDA_CHECK(cudaMemsetAsync(a->Bo.ptr, 0, sizeof(double) * n * a->ldbo, a->st));
+    a->BoF.ensure(sizeof(float) * n * a->ldbo);
+    CUDA_CHECK(cudaMemsetAsync(a->BoF.ptr, 0, sizeof(float) * n * a->ldbo, a->st));
     CUDA_CHECK(cudaMemcpyAsync(a->B.ptr, a->hb.B.data(), sizeof(float) * n,
                                cudaMemcpyHostToDevice, a->st));
     CUDA_CHECK(cudaMemcpyAsync(a->BoC.ptr, a->hb.BoC.data(), sizeof(float) * n,
                                cudaMemcpyHostToDevice, a->st));
-    k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(a->BoC.as<float>(), (int)n,
-                                                                a->Bo.as<double>(), a->ldbo, 0);
+    k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(
+        a->BoC.as<float>(), (int)n, a->Bo.as<double>(), a->BoF.as<float>(), a->ldbo, 0);
     LAUNCH_CHECK();
     a->ybo_d.ensure(sizeof(double) * max_terms);
     CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.ptr, &a->ybo[0], sizeof(double), cudaMemcpyHostToDevice,
@@ -290,6 +299,19 @@ void ensure_sorted(mars_gpu_algo *a, const std::vector<int> &cols)
                  a->ysort.as<float>(), a->sort_keys, a->sort_vals, a->sort_tmp,
                  &a->stats.kernel_launches);
     a->timer.end(PH_SORT, t0);
+    if (a->precision == MARS_GPU_PREC_MIXED) {
+        // the host re-decision walks the same sorted order
+        if (a->perm_h.size() != np) {
+            a->perm_h.assign(np, 0);
+        }
+        for (int c : todo) {
+            CUDA_CHECK(cudaMemcpyAsync(a->perm_h.data() + (size_t)c * a->n,
+                                       a->perm.as<int>() + (size_t)c * a->n,
+                                       sizeof(int32_t) * a->n, cudaMemcpyDeviceToHost, a->st));
+            a->stats.d2h_bytes += (long long)(sizeof(int32_t) * a->n);
+        }
+        sync(a);
+    }
     for (int c : todo) {
         a->sorted[c] = 1;
     }
@@ -400,6 +422,233 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
     a->stats.knot_evals += (long long)Pc * sweep_grid_rows(head, tail, min_span);
 }
 
+// Mixed precision (MARS_GPU_PREC_MIXED). Every candidate is ranked by the
+// FP32 / FP64-carry fast pass on the GPU; the best-ranked ones -- the top
+// MARS_GPU_MIXED_TOPK (default 16) by linear and by hinge delta SSE, and any
+// within MARS_GPU_MIXED_BAND (default 5%) of the best fast value -- are
+// re-evaluated on the host cores in the reference's exact FP64 order
+// (host_exact.cpp), and the decisions come from those exact values: the
+// re-decided candidates carry their exact delta SSE and knot, every other one
+// its fast value, held strictly below the best exact value so the first
+// maximum (mars.py:342-343) is always an exactly evaluated candidate.
+void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<int> &cb,
+                int rows, int min_span, int head, int tail, bool linear_only, double *lin,
+                double *hin, double *cut)
+{
+    const int n = (int)a->n, m = (int)a->m, P = (int)cx.size();
+    const size_t cnt = (size_t)rows * m;
+    for (size_t e = 0; e < cnt; ++e) {
+        lin[e] = 0.0;
+        hin[e] = 0.0;
+        cut[e] = std::numeric_limits<double>::quiet_NaN();
+    }
+    if (P == 0) {
+        return;
+    }
+    const int ks = fast_ksplit(n);
+    const double budget = env_double("MARS_GPU_BLOCK_GB", 32.0) * 1e9;
+    const double ngrid = linear_only ? 0.0 : (double)sweep_grid_rows(head, tail, min_span);
+    (void)ngrid;
+    const double per = 4.0 * n + (linear_only ? 0.0 : 8.0 * n) + 4.0 * m * (ks + 1) + 64.0;
+    size_t cap = (size_t)std::max(1.0, budget / per);
+    cap = std::min<size_t>(cap, 262144);
+    const auto blocks = block_candidates(cx, cap);
+    size_t maxPc = 0;
+    for (auto &b : blocks) {
+        maxPc = std::max<size_t>(maxPc, b.second - b.first);
+    }
+    a->Bx.ensure(sizeof(float) * a->n * maxPc);
+    a->svec.ensure(sizeof(double) * maxPc);
+    a->ybx.ensure(sizeof(double) * maxPc);
+    a->hsse.ensure(sizeof(double) * 2 * maxPc);  // two sweep directions
+    a->hrow.ensure(sizeof(int) * 2 * maxPc);
+    a->fTp.ensure(sizeof(float) * (size_t)ks * maxPc * m);
+    a->fT.ensure(sizeof(float) * maxPc * m);
+    a->fmom.ensure(sizeof(double) * 3 * maxPc);
+    a->hflag.ensure(sizeof(int) * 2 * maxPc);
+    if (!linear_only) {
+        a->bsort.ensure(sizeof(float) * a->n * maxPc);
+        a->bxsort.ensure(sizeof(float) * a->n * maxPc);
+    }
+    a->cand.ensure(sizeof(int) * 2 * (size_t)P);
+    int *cx_all = a->cand.as<int>(), *cb_all = cx_all + P;
+    CUDA_CHECK(cudaMemcpyAsync(cx_all, cx.data(), sizeof(int) * P, cudaMemcpyHostToDevice, a->st));
+    CUDA_CHECK(cudaMemcpyAsync(cb_all, cb.data(), sizeof(int) * P, cudaMemcpyHostToDevice, a->st));
+    a->stats.h2d_bytes += (long long)(sizeof(int) * 2 * (size_t)P);
+
+    std::vector<double> fybx(P), fh(P, 0.0), fh2(2 * (size_t)P, 0.0), fs(P), fmom(3 * (size_t)P);
+    std::vector<int> frow(P, -1), frow2(2 * (size_t)P, -1), fflag(2 * (size_t)P, 0);
+    for (auto &b : blocks) {
+        const int c0 = b.first, Pc = b.second - b.first;
+        const int *cx_d = cx_all + c0, *cb_d = cb_all + c0;
+        a->stats.project_flops += 4.0 * (double)n * (double)m * (double)Pc;
+        cudaEvent_t t0 = a->timer.begin();
+        FillSrc src{a->B.as<float>(), a->n, a->X.as<float>(), a->n, a->s.as<float>(), cx_d, cb_d};
+        FastScratch ws{a->fTp.as<float>(), a->fT.as<float>(), a->Bx.as<float>(),
+                       a->svec.as<double>(), a->ybx.as<double>(), a->fmom.as<double>()};
+        fast_project(a->st, src, a->BoC.as<float>(), n, m, Pc, a->y.as<float>(), a->tol, ws,
+                     &a->stats.kernel_launches);
+        a->timer.end(PH_PROJECT, t0);
+        if (!linear_only) {
+            t0 = a->timer.begin();
+            // all n rows: the mirror half reads the end span too
+            gather_parents(a->st, a->perm.as<int>(), a->B.as<float>(), a->n, cx_d, cb_d, n, n,
+                           Pc, a->bsort.as<float>(), &a->stats.kernel_launches);
+            gather_candidates(a->st, a->perm.as<int>(), a->Bx.as<float>(), a->n, cx_d,
+                              a->svec.as<double>(), a->tol, n, n, Pc, a->bxsort.as<float>(),
+                              &a->stats.kernel_launches);
+            std::vector<FastTaskRec> tasks;
+            const int warps = fast_sweep_warps(m, 2 * Pc);
+            for (int q = 0; q < Pc;) {
+                int e = q;
+                while (e < Pc && cx[c0 + e] == cx[c0 + q]) {
+                    ++e;
+                }
+                a->stats.sweep_bytes += (double)n * (12.0 + 4.0 * m + 8.0 * (e - q));
+                for (int t = q; t < e; t += warps) {
+                    for (int dir = 0; dir < 2; ++dir) {
+                        tasks.push_back({cx[c0 + q], t, std::min(warps, e - t), dir});
+                    }
+                }
+                q = e;
+            }
+            a->tasks.ensure(sizeof(FastTaskRec) * tasks.size());
+            CUDA_CHECK(cudaMemcpyAsync(a->tasks.ptr, tasks.data(),
+                                       sizeof(FastTaskRec) * tasks.size(), cudaMemcpyHostToDevice,
+                                       a->st));
+            a->stats.h2d_bytes += (long long)(sizeof(FastTaskRec) * tasks.size());
+            fast_sweep(a->st, a->tasks.as<FastTaskRec>(), (int)tasks.size(), a->perm.as<int>(),
+                       a->xsort.as<float>(), a->ysort.as<float>(), a->bsort.as<float>(),
+                       a->bxsort.as<float>(), a->BoF.as<float>(), a->ldbo,
+                       a->ybo_d.as<double>(), a->ybx.as<double>(), a->fmom.as<double>(), n, m,
+                       head, tail, min_span, a->tol, env_double("MARS_GPU_MIXED_CUT_REL", 1e-7),
+                       a->hsse.as<double>(), a->hrow.as<int>(), a->hflag.as<int>(), warps,
+                       &a->stats.kernel_launches);
+            a->timer.end(PH_SWEEP, t0);
+            a->stats.knot_evals += (long long)Pc * sweep_grid_rows(head, tail, min_span);
+            CUDA_CHECK(cudaMemcpyAsync(fh2.data() + 2 * (size_t)c0, a->hsse.ptr,
+                                       sizeof(double) * 2 * Pc, cudaMemcpyDeviceToHost, a->st));
+            CUDA_CHECK(cudaMemcpyAsync(frow2.data() + 2 * (size_t)c0, a->hrow.ptr,
+                                       sizeof(int) * 2 * Pc, cudaMemcpyDeviceToHost, a->st));
+            CUDA_CHECK(cudaMemcpyAsync(fflag.data() + 2 * (size_t)c0, a->hflag.ptr,
+                                       sizeof(int) * 2 * Pc, cudaMemcpyDeviceToHost, a->st));
+        }
+        CUDA_CHECK(cudaMemcpyAsync(fybx.data() + c0, a->ybx.ptr, sizeof(double) * Pc,
+                                   cudaMemcpyDeviceToHost, a->st));
+        CUDA_CHECK(cudaMemcpyAsync(fs.data() + c0, a->svec.ptr, sizeof(double) * Pc,
+                                   cudaMemcpyDeviceToHost, a->st));
+        CUDA_CHECK(cudaMemcpyAsync(fmom.data() + 3 * (size_t)c0, a->fmom.ptr,
+                                   sizeof(double) * 3 * Pc, cudaMemcpyDeviceToHost, a->st));
+        a->stats.d2h_bytes += (long long)((linear_only ? 40 : 72) * (size_t)Pc);
+        sync(a);
+    }
+    for (int j = 0; j < P && !linear_only; ++j) {  // the better of the two halves
+        const double f0 = frow2[2 * (size_t)j] >= 0 ? fh2[2 * (size_t)j] : -1.0;
+        const double f1 = frow2[2 * (size_t)j + 1] >= 0 ? fh2[2 * (size_t)j + 1] : -1.0;
+        const int d = f1 > f0 ? 1 : 0;
+        fh[j] = fh2[2 * (size_t)j + d];
+        frow[j] = frow2[2 * (size_t)j + d];
+    }
+
+    // contenders: top-K and the band, by the fast linear and hinge values
+    const auto t_host = std::chrono::steady_clock::now();
+    const int topk = std::max(1, (int)env_double("MARS_GPU_MIXED_TOPK", 16));
+    const double band = env_double("MARS_GPU_MIXED_BAND", 0.05);
+    std::vector<double> flin(P), fhin(P, 0.0);
+    for (int j = 0; j < P; ++j) {
+        flin[j] = fybx[j] * fybx[j];
+        if (!linear_only && frow[j] >= 0) {
+            fhin[j] = flin[j] + fh[j];
+        }
+    }
+    std::vector<char> contend(P, 0);
+    auto pick = [&](const std::vector<double> &v) {
+        std::vector<int> idx(P);
+        for (int j = 0; j < P; ++j) {
+            idx[j] = j;
+        }
+        const int k = std::min(topk, P);
+        std::partial_sort(idx.begin(), idx.begin() + k, idx.end(),
+                          [&](int x, int y) { return v[x] > v[y] || (v[x] == v[y] && x < y); });
+        const double top = v[idx[0]];
+        for (int q = 0; q < k; ++q) {
+            contend[idx[q]] = 1;
+        }
+        for (int j = 0; j < P; ++j) {
+            if (v[j] >= top * (1.0 - band)) {
+                contend[j] = 1;
+            }
+        }
+    };
+    pick(flin);
+    if (!linear_only) {
+        pick(fhin);
+        // Candidates whose reference evaluation is numerically unreliable --
+        // a candidate column almost in the span (projected norm below
+        // MARS_GPU_MIXED_DEGEN_REL, default 1e-6, of
+        // its raw norm: every cut cancels), or a cut flagged by the sweep --
+        // are re-decided too, since the reference's value there may be large.
+        const double degen = env_double("MARS_GPU_MIXED_DEGEN_REL", 1e-6);
+        for (int j = 0; j < P; ++j) {
+            if (fs[j] < degen * fmom[3 * (size_t)j + 2] || fflag[2 * (size_t)j] ||
+                fflag[2 * (size_t)j + 1]) {
+                contend[j] = 1;
+            }
+        }
+    }
+    std::vector<int> ex_x, ex_b, ex_j;
+    std::vector<const int32_t *> ex_perm;
+    for (int j = 0; j < P; ++j) {
+        if (contend[j]) {
+            ex_j.push_back(j);
+            ex_x.push_back(cx[j]);
+            ex_b.push_back(cb[j]);
+            ex_perm.push_back(linear_only ? nullptr : a->perm_h.data() + (size_t)cx[j] * a->n);
+        }
+    }
+    std::vector<ExactResult> ex;
+    const int threads = std::max(1u, std::thread::hardware_concurrency());
+    exact_candidates(a->hb, ex_x, ex_b, ex_perm, min_span, head, tail, ex, threads);
+    a->stats.redecided += (long long)ex_j.size();
+
+    // assemble: exact values for the contenders, fast values held below them for the rest
+    double lbest = -std::numeric_limits<double>::infinity(), hbest = lbest;
+    std::vector<double> elin(ex.size()), ehin(ex.size(), 0.0);
+    for (size_t q = 0; q < ex.size(); ++q) {
+        elin[q] = ex[q].ybx * ex[q].ybx;
+        if (!linear_only && ex[q].hinge_pos >= 0) {
+            ehin[q] = elin[q] + ex[q].hinge_sse;
+        }
+        lbest = std::max(lbest, elin[q]);
+        hbest = std::max(hbest, ehin[q]);
+    }
+    const double lcap = std::nextafter(lbest, -std::numeric_limits<double>::infinity());
+    const double hcap = std::nextafter(hbest, -std::numeric_limits<double>::infinity());
+    const float *Xh = a->hb.X;
+    for (int j = 0; j < P; ++j) {
+        if (contend[j]) {
+            continue;
+        }
+        const size_t idx = (size_t)cx[j] * m + cb[j];
+        lin[idx] = std::min(flin[j], lcap);
+        if (!linear_only && frow[j] >= 0) {
+            hin[idx] = std::min(fhin[j], hcap);
+            cut[idx] = (double)Xh[(size_t)frow[j] + (size_t)cx[j] * a->hb.ldx];
+        }
+    }
+    for (size_t q = 0; q < ex.size(); ++q) {
+        const int j = ex_j[q];
+        const size_t idx = (size_t)cx[j] * m + cb[j];
+        lin[idx] = elin[q];
+        if (!linear_only && ex[q].hinge_pos >= 0) {
+            hin[idx] = ehin[q];
+            cut[idx] = (double)Xh[(size_t)ex[q].hinge_row + (size_t)cx[j] * a->hb.ldx];
+        }
+    }
+    a->phase_ms[PH_REDECIDE] +=
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_host).count();
+}
+
 void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, int min_span,
                int end_span, int linear_only, double *sse0, double *lin, double *hin, double *cut)
 {
@@ -428,6 +677,25 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
     }
     const int P = (int)cx.size();
     a->stats.candidates += P;
+    if (a->precision == MARS_GPU_PREC_MIXED) {
+        const int head = end_span;
+        const int tail = head < n ? n - head : 0;
+        if (P > 0 && !linear_only) {
+            ensure_sorted(a, cols);
+        }
+        eval_mixed(a, cx, cb, rows, min_span, head, tail, linear_only != 0, lin, hin, cut);
+        span_mark_end(a);
+        sync(a);
+        a->timer.resolve(a->phase_ms);
+        if (sse0) {
+            double s = 0.0;
+            for (double v : a->ybo) {
+                s = std::fma(v, v, s);
+            }
+            *sse0 = s;
+        }
+        return;
+    }
     const size_t cnt = (size_t)rows * m;
     a->out.ensure(sizeof(double) * 3 * std::max<size_t>(cnt, 1));
     double *o_lin = a->out.as<double>(), *o_hin = o_lin + cnt, *o_cut = o_hin + cnt;
@@ -524,7 +792,8 @@ double append_impl(mars_gpu_algo *a, char type, int xcol, int bcol, float h)
         CUDA_CHECK(cudaMemcpyAsync(a->BoC.as<float>() + m * n, a->hb.BoC.data() + m * n,
                                    sizeof(float) * n, cudaMemcpyHostToDevice, a->st));
         k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(
-            a->BoC.as<float>() + m * n, (int)n, a->Bo.as<double>(), a->ldbo, (int)m);
+            a->BoC.as<float>() + m * n, (int)n, a->Bo.as<double>(), a->BoF.as<float>(), a->ldbo,
+            (int)m);
         LAUNCH_CHECK();
         a->stats.kernel_launches += 1;
         CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.as<double>() + m, &a->hb.ybo[m], sizeof(double),
@@ -628,7 +897,9 @@ int mars_gpu_set_precision(mars_gpu_algo *a, int mode)
         verify(a != nullptr, "null handle");
         verify(mode == MARS_GPU_PREC_FP64 || mode == MARS_GPU_PREC_MIXED,
                "unknown precision mode");
-        verify(mode == MARS_GPU_PREC_FP64, "the mixed-precision path is not built yet");
+        if (mode == MARS_GPU_PREC_MIXED && a->precision != mode) {
+            a->sorted.assign(a->p, 0);  // re-sort so the host gets the permutations too
+        }
         a->precision = mode;
     });
 }

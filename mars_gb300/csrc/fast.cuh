@@ -1,0 +1,51 @@
+// Fast (ranking) pass of the mixed-precision forward pass: every candidate
+// scored in FP32 with FP64 carries; the decisions are then re-taken from the
+// exact FP64 values of the best-ranked candidates (host_exact.h).
+#pragma once
+
+#include "common.cuh"
+#include "fp64.cuh"
+
+namespace mgpu {
+
+struct FastScratch {
+    float *Tp;     // split-K partial T: [ksplit][P][m]
+    float *T;      // [P][m]
+    float *Bx;     // projected candidate columns, (n, P) column-major, ld n
+    double *s;     // [P] squared norms of the projected columns
+    double *ybx;   // [P] y . normalised column
+    double *mom;   // [3 P] sum b^2 x^k, k = 0..2 (parent b, input x); k = 2: raw norm of x b
+};
+
+// Split-K factor of the fast projection for n rows.
+int fast_ksplit(int n);
+
+// Bx = v - Bo (Bo^T v) twice (the second pass re-orthogonalises the residual
+// of the first), v = src (FillSrc), then s = ||Bx||^2 and
+// ybx = scale(s) * (Bx . y), and the parent moments mom. BoC: (n, m) column-major f32 (ld n).
+void fast_project(cudaStream_t st, const FillSrc &src, const float *BoC, int n, int m, int P,
+                  const float *y, double tol, const FastScratch &ws, long long *launches);
+
+// Chunked FP32 / FP64-carry hinge sweep of every candidate, in two halves:
+// tasks with dir 0 sweep from the top and score the cuts up to
+// fast_sweep_mid(), tasks with dir 1 sweep the mirror hinge from the bottom
+// and score the rest. Outputs per candidate j and direction:
+// hsse[2 j + dir] (the hinge part of the best score), hrow[2 j + dir], and
+// hflag[2 j + dir] = 1 when a cut of that half has den below cut_rel of the
+// reference's K (its f64 value there is unreliable). mom: from fast_project.
+// `tasks` are SweepTask-sized records {xcol, cand0, count, dir}; bs/bxs: sorted
+// parent and normalised candidate columns; BoR: (n, ldbo) row-major f32 basis
+// (ldbo a multiple of 4).
+int fast_sweep_warps(int m, int candidates);
+int fast_sweep_mid(int head, int tail, int n);  // in [0, n - 1]
+struct FastTaskRec {
+    int xcol, cand0, count, dir;
+};
+void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int *perm,
+                const float *xsort, const float *ysort, const float *bs, const float *bxs,
+                const float *BoR, size_t ldbo, const double *ybo, const double *ybx,
+                const double *mom, int n, int m, int head, int tail, int min_span, double tol,
+                double cut_rel, double *hsse, int *hrow, int *hflag, int warps_per_block,
+                long long *launches);
+
+}  // namespace mgpu

@@ -429,8 +429,9 @@ struct SweepSmem {
         o += 8 * (size_t)W * SW_SNAP * (m + 1);
         ybo = o;
         o += 8 * ((size_t)m + 1);
-        bo = o;  // [S][SW_ROWS][m] f64 rows of Bo
-        o += 8 * (size_t)S * SW_ROWS * m;
+        o = (o + 15) / 16 * 16;  // 16-byte cp.async destinations
+        bo = o;  // [S][SW_ROWS][mp] f64 rows of Bo, row stride mp = m rounded up to 2
+        o += 8 * (size_t)S * SW_ROWS * ((m + 1) / 2 * 2);
         cvt = o;  // [2][2W + 1][SW_ROWS] f64: B and Bx of each candidate, then the deltas
         o += 8 * 2 * (size_t)(2 * W + 1) * SW_ROWS;
         raw = o;  // [S][2W * SW_ROWS + SW_ROWS + 1] f32: B, Bx, then x from row i0 - 1
@@ -452,6 +453,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
     const int W = (blockDim.x >> 5) - 1;  // candidate warps
     const int NV = 2 * W + 1;
     const int RAW = 2 * W * SW_ROWS + SW_ROWS + 1;
+    const int U = (m + 1) / 2, MP = 2 * U;  // 16-byte units per Bo row, padded row stride
     const SweepSmem L(m, W, S);
     const int ldF = m + 1;
     double *snapbase = reinterpret_cast<double *>(sraw + L.snap);
@@ -489,12 +491,14 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
         const int sg = sq % S, i0 = sq * SW_ROWS;
         const int rows = min(SW_ROWS, tail - i0);
         const int k = pf_k;
-        double *bo = sbo + (size_t)sg * SW_ROWS * m;
-        for (int r = 0; r < rows; ++r) {
-            const int kr = __shfl_sync(0xffffffffu, k, r);
-            const double *src = Bo + (size_t)kr * ldbo;
-            for (int c = lane; c < m; c += 32) {
-                cp_async<8>(bo + r * m + c, src + c);
+        double *bo = sbo + (size_t)sg * SW_ROWS * MP;
+        // Bo rows, 16 bytes per lane, 32 / U rows per instruction (rows are
+        // 16-byte aligned: the row stride ldbo is a multiple of 4)
+        for (int e0 = 0; e0 < SW_ROWS * U; e0 += 32) {
+            const int e = e0 + lane, r = e / U, u = e - r * U;
+            const int kr = __shfl_sync(0xffffffffu, k, r < SW_ROWS ? r : 0);
+            if (r < rows) {
+                cp_async<16>(bo + r * MP + 2 * u, Bo + (size_t)kr * ldbo + 2 * u);
             }
         }
         // B, Bx (sorted per candidate) and x: coalesced, lanes over rows
@@ -607,13 +611,13 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
             const double *bw = cv + warp * SW_ROWS;
             const double *xw = cv + (W + warp) * SW_ROWS;
             const double *dv = cv + 2 * W * SW_ROWS;
-            const double *rowb = sbo + (size_t)sg * SW_ROWS * m;
+            const double *rowb = sbo + (size_t)sg * SW_ROWS * MP;
             long ng = next_grid;
             int slot = nsnap;
             for (int r = 0; r < rows; ++r) {
                 const int i = i0 + r;
                 const double bk = bw[r], bxk = xw[r];
-                const double *rowp = rowb + r * m;
+                const double *rowp = rowb + r * MP;
                 const double di = dv[r];  // 0 for the first row
 #pragma unroll
                 for (int q = 0; q < CPL; ++q) {
