@@ -424,8 +424,9 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
 
 // Mixed precision (MARS_GPU_PREC_MIXED). Every candidate is ranked by the
 // FP32 / FP64-carry fast pass on the GPU; the best-ranked ones -- the top
-// MARS_GPU_MIXED_TOPK (default 16) by linear and by hinge delta SSE, and any
-// within MARS_GPU_MIXED_BAND (default 5%) of the best fast value -- are
+// MARS_GPU_MIXED_TOPK (default 4) by linear and by hinge delta SSE, and any
+// within MARS_GPU_MIXED_BAND (default 2%) of the best fast value -- and the
+// numerically unreliable ones (below) are
 // re-evaluated on the host cores in the reference's exact FP64 order
 // (host_exact.cpp), and the decisions come from those exact values: the
 // re-decided candidates carry their exact delta SSE and knot, every other one
@@ -552,8 +553,8 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
 
     // contenders: top-K and the band, by the fast linear and hinge values
     const auto t_host = std::chrono::steady_clock::now();
-    const int topk = std::max(1, (int)env_double("MARS_GPU_MIXED_TOPK", 16));
-    const double band = env_double("MARS_GPU_MIXED_BAND", 0.05);
+    const int topk = std::max(1, (int)env_double("MARS_GPU_MIXED_TOPK", 4));
+    const double band = env_double("MARS_GPU_MIXED_BAND", 0.02);
     std::vector<double> flin(P), fhin(P, 0.0);
     for (int j = 0; j < P; ++j) {
         flin[j] = fybx[j] * fybx[j];
@@ -607,8 +608,61 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         }
     }
     std::vector<ExactResult> ex;
-    const int threads = std::max(1u, std::thread::hardware_concurrency());
-    exact_candidates(a->hb, ex_x, ex_b, ex_perm, min_span, head, tail, ex, threads);
+    const int host_max = (int)env_double("MARS_GPU_MIXED_HOST_MAX", 128);
+    if ((int)ex_j.size() <= host_max) {
+        // few contenders: the host cores, whose serial f64 chains are ~50x
+        // shorter in latency than the GPU's
+        const int threads = std::max(1u, std::thread::hardware_concurrency());
+        exact_candidates(a->hb, ex_x, ex_b, ex_perm, min_span, head, tail, ex, threads);
+    } else {
+        // many contenders: the FP64 GPU path over them (its time hardly depends
+        // on the candidate count)
+        const int C = (int)ex_j.size();
+        a->cand.ensure(sizeof(int) * 2 * (size_t)C);
+        a->Bx.ensure(sizeof(float) * a->n * C);
+        a->svec.ensure(sizeof(double) * C);
+        a->ybx.ensure(sizeof(double) * C);
+        a->hsse.ensure(sizeof(double) * C);
+        a->hrow.ensure(sizeof(int) * C);
+        if (!linear_only) {
+            a->bsort.ensure(sizeof(float) * a->n * C);
+            a->bxsort.ensure(sizeof(float) * a->n * C);
+        }
+        a->T.ensure(sizeof(double) * std::max<size_t>(1, (size_t)m * C));
+        a->snew.ensure(sizeof(double) * C);
+        a->fired.ensure(sizeof(int) * C);
+        a->nfired.ensure(sizeof(int) * 4);
+        if (!linear_only) {
+            a->scal.ensure(sizeof(double) * 3 *
+                           std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
+        }
+        int *ecx = a->cand.as<int>(), *ecb = ecx + C;
+        CUDA_CHECK(cudaMemcpyAsync(ecx, ex_x.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
+                                   a->st));
+        CUDA_CHECK(cudaMemcpyAsync(ecb, ex_b.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
+                                   a->st));
+        a->stats.h2d_bytes += (long long)(sizeof(int) * 2 * (size_t)C);
+        eval_block_fp64(a, C, ecx, ecb, ex_x, 0, min_span, head, tail, linear_only);
+        std::vector<double> eybx(C), ehs(C, 0.0);
+        std::vector<int> ehr(C, -1);
+        CUDA_CHECK(cudaMemcpyAsync(eybx.data(), a->ybx.ptr, sizeof(double) * C,
+                                   cudaMemcpyDeviceToHost, a->st));
+        if (!linear_only) {
+            CUDA_CHECK(cudaMemcpyAsync(ehs.data(), a->hsse.ptr, sizeof(double) * C,
+                                       cudaMemcpyDeviceToHost, a->st));
+            CUDA_CHECK(cudaMemcpyAsync(ehr.data(), a->hrow.ptr, sizeof(int) * C,
+                                       cudaMemcpyDeviceToHost, a->st));
+        }
+        a->stats.d2h_bytes += (long long)(20 * (size_t)C);
+        sync(a);
+        ex.resize(C);
+        for (int q = 0; q < C; ++q) {
+            ex[q].ybx = eybx[q];
+            ex[q].hinge_sse = ehs[q];
+            ex[q].hinge_row = ehr[q];
+            ex[q].hinge_pos = ehr[q] >= 0 ? 0 : -1;
+        }
+    }
     a->stats.redecided += (long long)ex_j.size();
 
     // assemble: exact values for the contenders, fast values held below them for the rest

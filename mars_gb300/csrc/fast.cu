@@ -199,10 +199,11 @@ __global__ void __launch_bounds__(256) k_parent_moments(FillSrc src, int n, doub
 
 // ---------------------------------------------------------------------------
 // Chunked sweep. Block = one input column, one direction and up to W
-// candidates (warps 0..W-1, lane = component) plus a loader warp (warp W)
-// that stages each chunk: the gathered f32 Bo rows (16 bytes per lane) and,
-// lanes over rows, the sorted parent and candidate values, y and x; then the
-// f32 deltas and their f64 running sums within the chunk.
+// candidates (warps 0..W-1, lane = component) plus two loader warps that stage
+// each chunk with cp.async: warp W the gathered f32 Bo rows (16 bytes per
+// lane), warp W+1, lanes over rows, the sorted parent and candidate values, y
+// and x, then the f32 deltas and their f64 running sums within the chunk
+// (copies in flight are limited per warp, so the staging is split).
 //
 // Directions. Forward tasks sweep the descending order from the top and score
 // the cuts of its first half. Near the bottom the hinge (x - t)+ b differs
@@ -274,7 +275,7 @@ struct FastSweepSmem {
 };
 
 template <int CPL, int S>
-__global__ void __launch_bounds__(32 * (FS_MAXW + 1), 1)
+__global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
     k_fast_sweep(const FastTask *__restrict__ tasks, const int *__restrict__ perm,
                  const float *__restrict__ xsort, const float *__restrict__ ysort,
                  const float *__restrict__ bs, const float *__restrict__ bxs,
@@ -284,7 +285,7 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 1), 1)
                  double *__restrict__ hsse, int *__restrict__ hrow, int *__restrict__ hflag)
 {
     extern __shared__ __align__(16) unsigned char sm[];
-    const int W = (blockDim.x >> 5) - 1;
+    const int W = (blockDim.x >> 5) - 2;  // candidate warps; then the two loaders
     const int NC = m + 3;  // basis columns, candidate, y, b
     const int U = (m + 3) / 4, MP = 4 * U;  // 16-byte units per Bo row, padded row stride
     const int RAW = (2 * W + 1) * FS_ROWS + FS_ROWS + 1;
@@ -312,7 +313,8 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 1), 1)
     const bool rev = task.dir != 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool cwarp = warp < task.count;
-    const bool lwarp = warp == W;
+    const bool lwarp = warp == W;      // loader of the Bo rows
+    const bool rwarp = warp == W + 1;  // loader of the per-candidate arrays, y, x
     const int *pk = perm + (size_t)task.xcol * n;
     const float *xs = xsort + (size_t)task.xcol * n;
     const float *ys = ysort + (size_t)task.xcol * n;
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 1), 1)
             pf_k = pk[idx(s)];
         }
     };
-    auto issue = [&](int sq) {
+    auto issue_bo = [&](int sq) {
         const int sg = sq % S, s0 = sq * FS_ROWS;
         const int rows = min(FS_ROWS, len - s0);
         const int k = pf_k;
@@ -363,6 +365,10 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 1), 1)
                 cp_async<16>(bo + r * MP + 4 * u, BoR + (size_t)kr * ldbo + 4 * u);
             }
         }
+    };
+    auto issue_raw = [&](int sq) {
+        const int sg = sq % S, s0 = sq * FS_ROWS;
+        const int rows = min(FS_ROWS, len - s0);
         float *rw = sraw4 + (size_t)sg * RAW;
         const bool ok = lane < rows;
         const int i = ok ? idx(s0 + lane) : 0;
@@ -382,14 +388,11 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 1), 1)
         const int h = sq & 1, s = sq * FS_ROWS + lane;
         const bool ok = s < len && s > 0;
         const float d = ok ? (rev ? xr[lane + 1] - xr[lane] : xr[lane] - xr[lane + 1]) : 0.f;
-        double run = (double)d;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const double u = __shfl_up_sync(0xffffffffu, run, o);
-            if (lane >= o) {
-                run += u;
-            }
-        }
+        // running sum of the chunk's deltas through this row: telescoped, the
+        // f64 difference of the x at the chunk's base and at the row
+        const float base = sq == 0 ? xr[1] : xr[0];
+        const double run = rev ? (double)xr[lane + 1] - (double)base
+                               : (double)base - (double)xr[lane + 1];
         dsm[h * FS_ROWS + lane] = d;
         dpre[h * FS_ROWS + lane] = run;
     };
@@ -499,10 +502,19 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 1), 1)
 #pragma unroll
         for (int u = 0; u < S - 1; ++u) {
             if (u < nstages) {
-                issue(u);
+                issue_bo(u);
             }
             cp_async_commit();
             prefetch(u + 1);
+        }
+        cp_async_wait<S - 2>();
+    } else if (rwarp) {
+#pragma unroll
+        for (int u = 0; u < S - 1; ++u) {
+            if (u < nstages) {
+                issue_raw(u);
+            }
+            cp_async_commit();
         }
         cp_async_wait<S - 2>();
         __syncwarp();
@@ -539,27 +551,45 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 1), 1)
             }
             const float *rw = sraw4 + (size_t)sg * RAW;
             const float *bw = rw + warp * FS_ROWS;
-            const float *xw = rw + (W + warp) * FS_ROWS;
-            const float *yw = rw + 2 * W * FS_ROWS;
             const float *dv = dsm + h * FS_ROWS;
             const float *rowb = sbo + (size_t)sg * FS_ROWS * MP;
             long ng = next_grid;
             int slot = nsnap;
-            for (int r = 0; r < rows; ++r) {
-                const int s = s0 + r;
-                const float bk = bw[r], bxk = xw[r], yk = yw[r], d = dv[r];
-                const float *rowp = rowb + r * MP;
+            // Per lane, where its x comes from: the Bo row (c < m) or one of the
+            // per-row candidate arrays (candidate column, y, parent); the same
+            // address arithmetic for every row, no per-row selects.
+            int xoff[CPL];
+            bool xrow[CPL];
 #pragma unroll
-                for (int u = 0; u < CPL; ++u) {
-                    const int c = lane + 32 * u;
-                    const float bv = rowp[min(c, m - 1)];
-                    const float xv = c < m ? bv : c == m ? bxk : c == m + 1 ? yk : c == cb ? bk : 0.f;
-                    const float klc = fmaf(d * d, q[u], fmaf(2.0f * d, e[u], kl));
-                    kl = c == cb ? klc : kl;
-                    e[u] = fmaf(d, q[u], e[u]);
-                    q[u] = fmaf(bk, xv, q[u]);
+            for (int u = 0; u < CPL; ++u) {
+                const int c = lane + 32 * u;
+                xrow[u] = c < m;
+                xoff[u] = c < m ? c
+                                : c == m ? (W + warp) * FS_ROWS
+                                         : c == m + 1 ? 2 * W * FS_ROWS : warp * FS_ROWS;
+            }
+            int r = 0;
+            while (r < rows) {
+                // rows up to and including the next grid row of this stage run
+                // without a branch; the snapshot follows
+                const bool grid_here = ng <= last_step && ng < (long)s0 + rows;
+                const int rend = grid_here ? (int)(ng - s0) + 1 : rows;
+#pragma unroll 4
+                for (; r < rend; ++r) {
+                    const float bk = bw[r], d = dv[r];
+                    const float *rowp = rowb + r * MP;
+#pragma unroll
+                    for (int u = 0; u < CPL; ++u) {
+                        const int c = lane + 32 * u;
+                        const float xv = xrow[u] ? rowp[xoff[u]] : (c < NC ? rw[xoff[u] + r] : 0.f);
+                        const float klc = fmaf(d * d, q[u], fmaf(2.0f * d, e[u], kl));
+                        kl = c == cb ? klc : kl;
+                        e[u] = fmaf(d, q[u], e[u]);
+                        q[u] = fmaf(bk, xv, q[u]);
+                    }
                 }
-                if (s == ng && s <= last_step) {
+                if (grid_here) {
+                    const int rg = rend - 1;
                     ng += min_span;
                     float *es = myE + (size_t)slot * NC;
 #pragma unroll
@@ -573,10 +603,10 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 1), 1)
                         }
                     }
                     if (lane == 0 && warp == 0) {
-                        srow[slot] = idx(s);
+                        srow[slot] = idx(s0 + rg);
                         sCh[slot] = nhist;
-                        sD[slot] = dpre[h * FS_ROWS + r];
-                        sXv[slot] = rw[(2 * W + 1) * FS_ROWS + 1 + r];
+                        sD[slot] = dpre[h * FS_ROWS + rg];
+                        sXv[slot] = rw[(2 * W + 1) * FS_ROWS + 1 + rg];
                     }
                     ++slot;
                 }
@@ -597,10 +627,16 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 1), 1)
             kl = 0.f;
         } else if (lwarp) {
             if (sq + S - 1 < nstages) {
-                issue(sq + S - 1);
+                issue_bo(sq + S - 1);
             }
             cp_async_commit();
             prefetch(sq + S);
+            cp_async_wait<S - 2>();
+        } else if (rwarp) {
+            if (sq + S - 1 < nstages) {
+                issue_raw(sq + S - 1);
+            }
+            cp_async_commit();
             cp_async_wait<S - 2>();
             __syncwarp();
             if (sq + 1 < nstages) {
@@ -718,7 +754,7 @@ void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int
         CUDA_CHECK(cudaFuncSetAttribute(k_fast_sweep<CPL, S>,                                  \
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,           \
                                         (int)smem));                                           \
-        k_fast_sweep<CPL, S><<<ntasks, 32 * (warps + 1), smem, st>>>(                          \
+        k_fast_sweep<CPL, S><<<ntasks, 32 * (warps + 2), smem, st>>>(                          \
             reinterpret_cast<const FastTask *>(tasks), perm, xsort, ysort, bs, bxs, BoR, ldbo, \
             ybo, ybx, mom, n, m, head, tail, mid, min_span, tol, cut_rel, hsse, hrow, hflag);  \
     } while (0)

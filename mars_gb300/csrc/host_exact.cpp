@@ -331,7 +331,19 @@ ExactResult exact_candidate(const HostBasis &hb, int xcol, int bcol, const int32
     double b2 = b_k * b_k;
     size_t next_grid = (size_t)head + 1;
     double best = 0.0;
+    // The rows are visited in sorted order, i.e. at random in memory: fetch
+    // the ones PF steps ahead so that their misses overlap.
+    constexpr size_t PF = 16;
     for (size_t i = 1; i < (size_t)tail; ++i) {
+        if (i + PF < (size_t)tail) {
+            const size_t kp = (size_t)k[i + PF];
+            __builtin_prefetch(Bo + kp * ld);
+            __builtin_prefetch(Bo + kp * ld + 16);
+            __builtin_prefetch(b + kp);
+            __builtin_prefetch(bx.data() + kp);
+            __builtin_prefetch(hb.y.data() + kp);
+            __builtin_prefetch(x.data() + kp);
+        }
         b_k = b[k[i]];
         bx_k = bx[k[i]];
         y_k = hb.y[k[i]];
