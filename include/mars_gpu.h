@@ -4,8 +4,9 @@
  *  Plain C types only (pointers, sizes, status codes): no CUDA or torch types
  *  cross this boundary, and no C++ exception escapes it. Every entry point
  *  returns MARS_GPU_OK (0) or a nonzero status; mars_gpu_last_error() then
- *  holds a message (per calling thread). Host pointers in, host pointers out:
- *  the library owns all device memory.
+ *  holds a message (per calling thread). The fit API takes host arrays and the
+ *  library owns its device memory; the kernel-level entry points marked
+ *  "DEVICE arrays" take caller-owned device memory and a stream.
  *
  *  A handle is the device-resident state of one fit (the reference's
  *  MarsAlgo plus its mars::cuda::Context). Calls on one handle must not
@@ -27,6 +28,7 @@
  *    mars_gpu_orthonormalize   mars::orthonormalize    kernels.h:52-62
  *                              mars::cuda::orthonormalize  cuda/mars_cuda.h:127-131
  *    mars_gpu_orthonormalize_col  mars::orthonormalize_col  kernels.h:91-96
+ *    mars_gpu_expand(_backward)   mars.expand (numpy)        mars.py:423-450
  */
 #ifndef MARS_GPU_H
 #define MARS_GPU_H
@@ -53,7 +55,8 @@ extern "C" {
 
 /* Arithmetic used for candidate evaluation. */
 #define MARS_GPU_PREC_FP64 0  /* plain FP64 forward pass */
-#define MARS_GPU_PREC_MIXED 1 /* FP32/tensor-core fast path, near-ties re-decided in FP64 */
+#define MARS_GPU_PREC_MIXED 1 /* FP32 / FP64-carry fast pass; the best-ranked and the
+                                  numerically unreliable candidates re-decided in FP64 */
 
 typedef struct mars_gpu_algo mars_gpu_algo;
 
@@ -102,7 +105,7 @@ MARS_GPU_API int mars_gpu_nbasis(const mars_gpu_algo *algo, int *out);
 MARS_GPU_API int mars_gpu_yvar(const mars_gpu_algo *algo, double *out);
 MARS_GPU_API int mars_gpu_dsse(const mars_gpu_algo *algo, double *out);
 
-/* Select MARS_GPU_PREC_FP64 or MARS_GPU_PREC_MIXED (the default). */
+/* Select MARS_GPU_PREC_FP64 (the default) or MARS_GPU_PREC_MIXED. */
 MARS_GPU_API int mars_gpu_set_precision(mars_gpu_algo *algo, int mode);
 
 /*
@@ -189,6 +192,37 @@ MARS_GPU_API int mars_gpu_orthonormalize_col(size_t n, size_t m, double *v, cons
  *  threads, or on two streams whose work can run at the same time -- race and
  *  give wrong results.
  */
+/*
+ *  Differentiable expansion of a fitted model: the basis of mars.expand
+ *  (mars.py:423-450) with the prediction pred = B beta, and its backward pass.
+ *  No counterpart in the reference (its expand is numpy, without gradients).
+ *
+ *  Term j (0 <= j < M, in model order): kind[j] (MARS_GPU_TERM_*), parent[j]
+ *  (< j; ignored for the intercept), input[j] (X column), knot[j] (hinges),
+ *  beta[j]. B_0 = 1, B_j = B_parent * f_j(x_input), f = x, max(x - t, 0) or
+ *  max(t - x, 0). All arrays are DEVICE arrays; X is (N, *) column-major with
+ *  column stride ldx; stream is a cudaStream_t (NULL: the default stream).
+ *
+ *  mars_gpu_expand: pred (N, optional) and B ((N, M) column-major, stride ldb,
+ *  optional). mars_gpu_expand_backward: given g = dL/dpred (N), accumulates
+ *  dL/dX into dX ((N, *) column-major, stride lddx, optional; the caller zeroes
+ *  it) and writes dL/dbeta and dL/dknot (M doubles each; the knot derivative of
+ *  a non-hinge term is 0; subgradient 0 at a kink). workspace holds
+ *  mars_gpu_expand_workspace(N, M) bytes. 1 <= M <= 128.
+ */
+#define MARS_GPU_TERM_INTERCEPT 0
+#define MARS_GPU_TERM_LINEAR 1
+#define MARS_GPU_TERM_PLUS 2
+#define MARS_GPU_TERM_MINUS 3
+MARS_GPU_API size_t mars_gpu_expand_workspace(size_t N, int M);
+MARS_GPU_API int mars_gpu_expand(const int *kind, const int *parent, const int *input,
+                    const float *knot, const float *beta, int M, const float *X, size_t ldx,
+                    size_t N, float *pred, float *B, size_t ldb, void *stream);
+MARS_GPU_API int mars_gpu_expand_backward(const int *kind, const int *parent, const int *input,
+                             const float *knot, const float *beta, int M, const float *X,
+                             size_t ldx, size_t N, const float *g, float *dX, size_t lddx,
+                             double *dbeta, double *dknot, void *workspace, void *stream);
+
 #define MARS_GPU_NOALLOC_MAX_CANDIDATES 4096
 #define MARS_GPU_NOALLOC_MAX_COEFS 262144
 MARS_GPU_API int mars_gpu_orthonormalize_noalloc(size_t n, size_t m, size_t p, const float *B,
