@@ -51,6 +51,10 @@ WORKLOADS = {
     "precision_stress": "precision_stress n=1000000 p=100 AR(1) rho=0.9 + 5 near-duplicates, "
                         "max_terms=63 tail_span=0 (config 3)",
     "plain_fit": "plain_fit n=10000 p=2 linear_only max_terms=17 (config 1)",
+    "batched": "256 independent fits, n log-uniform 1e3..2e5, p uniform 5..50, 4 random hinges "
+               "+ N(0,1) noise, max_terms=21, tail_span=0 (config 4)",
+    "expand": "differentiable prediction of a fitted hinge_search model (31 terms) on "
+              "1,000,000 rows: forward + backward (config 5)",
 }
 
 
@@ -336,10 +340,100 @@ def run_reference(args):
     return 0
 
 
+def run_batched(args):
+    """Config 4: fits/s over 256 independent fits driven concurrently."""
+    from mars_gb300 import batch, marslib, workloads
+
+    marslib.load()
+    probs = [(X, y, None, kw) for X, y, kw in workloads.batched_fits(count=256, seed=0)]
+    for _ in range(max(args.warmup, 0)):
+        batch.fit_many(probs[:8], threads=8, precision=args.precision)
+    clocks = Clocks()
+    clocks.start()
+    t0 = time.perf_counter()
+    walls = []
+    for _ in range(args.steps):
+        _, per = batch.fit_many(probs, threads=16, precision=args.precision)
+        walls.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+    clk = clocks.stop()
+    per = sorted(per)
+    total = sum(walls) / args.steps
+    line = {"metric": "fits/s (256 independent fits)", "value": len(probs) / total,
+            "unit": "fits/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "mixed",
+            "precision": args.precision, "data": "synthetic",
+            "config": {"workload": WORKLOADS["batched"], "concurrency": "16 host threads, "
+                       "one handle and stream per fit"},
+            "per_fit_s": {"p50": per[len(per) // 2], "p99": per[min(len(per) - 1,
+                                                                  int(0.99 * len(per)))]},
+            "clocks": clk}
+    if not args.no_cpu_baseline:
+        sample = probs[:4]
+        t0 = time.perf_counter()
+        for X, y, _, kw in sample:
+            cpu_fit(X, y, kw, cpu_threads())
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(sample) / dt, "unit": "fits/s",
+                                "cores": cpu_threads(), "kind": "port",
+                                "sample": "the first 4 of the 256 fits, one after another"}
+    print(json.dumps(line))
+    return 0
+
+
+def run_expand(args):
+    """Config 5: rows/s of forward + backward of the differentiable prediction."""
+    import torch
+
+    from mars_gb300 import diff, mars, marslib, workloads
+
+    marslib.load()
+    X, y, kw = workloads.hinge_search()
+    model = mars.fit(X, y, **kw)
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(0)
+    N = 1_000_000
+    Xb = torch.tensor(rng.standard_normal((N, X.shape[1])).astype(np.float32), device=dev)
+    Xb = Xb.t().contiguous().t()  # column-major
+    Xb.requires_grad_(True)
+    beta = torch.tensor(rng.uniform(-1, 1, len(model)).astype(np.float32), device=dev,
+                        requires_grad=True)
+    knots = torch.tensor(np.nan_to_num(np.asarray(model["hinge"], np.float32)), device=dev,
+                         requires_grad=True)
+
+    def step():
+        pred = diff.predict(Xb, model, beta, knots)
+        pred.sum().backward()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    line = {"metric": "rows/s (prediction forward + backward, grads in X, beta, knots)",
+            "value": N / (ms * 1e-3), "unit": "rows/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 gradient sums)",
+            "data": "synthetic", "config": {"workload": WORKLOADS["expand"],
+                                            "terms": len(model)}}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
+    if args.workload == "expand":
+        return run_expand(args)
     tdist = dist()
     from mars_gb300 import marslib
 

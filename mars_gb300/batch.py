@@ -1,0 +1,41 @@
+"""Many independent fits at once (bootstraps, several targets, per-group models).
+
+Each fit is its own handle with its own CUDA stream; ``fit_many`` drives up to
+``threads`` fits concurrently from a host thread pool. The C ABI releases the
+Python interpreter lock for every call (ctypes), so the fits' kernels overlap
+on the device while each fit's host-side decisions (mars.py's epoch loop, the
+reference-order append) proceed on its own thread. A single fit of modest n
+keeps only a few SMs busy with its dependent FP64 chains; concurrent fits fill
+the rest.
+"""
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+from . import marslib
+from .mars import forward_pass
+
+
+def fit_many(problems, threads=16, precision=None):
+    """Fit every (X, y, w, kwargs) of ``problems`` (w may be None); returns
+    (models, seconds per fit) in the input order. ``precision``: 'fp64'
+    (default) or 'mixed' for every handle."""
+
+    class Lib:
+        __version__ = getattr(marslib, "__version__", "0.12")
+
+        @staticmethod
+        def MarsAlgo(*a):
+            o = marslib.MarsAlgo(*a)
+            if precision is not None:
+                o.set_precision(precision)
+            return o
+
+    def one(prob):
+        X, y, w, kw = prob
+        t0 = time.perf_counter()
+        model = forward_pass(Lib, X, y, w, **kw)
+        return model, time.perf_counter() - t0
+
+    with ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
+        out = list(ex.map(one, problems))
+    return [m for m, _ in out], [t for _, t in out]
