@@ -466,8 +466,8 @@ def main():
             agg = dict(st)
         else:
             for key in ("ms_project", "ms_sweep", "ms_dgks", "ms_normalize", "ms_append",
-                        "ms_sort", "ms_redecide", "project_flops", "sweep_bytes", "evals",
-                        "candidates", "redecided"):
+                        "ms_sort", "ms_redecide", "ms_gather", "ms_redecide_gpu", "project_flops",
+                        "sweep_bytes", "evals", "candidates", "redecided"):
                 agg[key] += st[key]
     if tdist is not None:
         tdist.barrier()
@@ -504,7 +504,8 @@ def main():
         "roofline": roofline(agg, args.workload, args.precision),
         "phase_ms_per_step": {k[3:]: agg[k] / args.steps for k in
                               ("ms_project", "ms_dgks", "ms_normalize", "ms_sweep",
-                               "ms_append", "ms_sort", "ms_redecide")},
+                               "ms_append", "ms_sort", "ms_redecide", "ms_gather",
+                               "ms_redecide_gpu")},
         "clocks": clk,
     }
     if args.precision == "mixed":

@@ -78,7 +78,16 @@ typedef struct {
     double ms_sweep;
     double ms_sort;
     double ms_append;
-    double ms_redecide;
+    double ms_redecide;         /* mixed mode: wall time of the exact re-decisions */
+    double ms_gather;           /* mixed mode: parents and candidates into sorted order */
+    double ms_redecide_gpu;     /* mixed mode: device time of re-decisions run on the GPU */
+    long long redecided_flagged; /* mixed mode: candidates re-decided for a flag (degenerate
+                                    column or unresolvable cut), whatever their rank */
+    long long speculated;       /* mixed mode: candidates evaluated exactly beside the fast
+                                   pass (the previous contenders, the new columns' candidates) */
+    long long redecided_spec;   /* mixed mode: re-decided candidates the speculation covered */
+    long long leftovers;        /* mixed mode: candidates evaluated exactly after the fast pass */
+    long long leftovers_flagged; /* ... of which carried a flag */
 } mars_gpu_stats;
 
 /* Message of the last failing call on this thread ("" if none). */

@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <string>
 #include <vector>
 
@@ -56,11 +57,23 @@ double env_double(const char *name, double dflt)
     return (v && *v) ? std::atof(v) : dflt;
 }
 
-enum Phase { PH_PROJECT, PH_DGKS, PH_NORMALIZE, PH_SWEEP, PH_SORT, PH_APPEND, PH_REDECIDE, PH_N };
+enum Phase {
+    PH_PROJECT,
+    PH_DGKS,
+    PH_NORMALIZE,
+    PH_SWEEP,
+    PH_SORT,
+    PH_APPEND,
+    PH_REDECIDE,
+    PH_GATHER,
+    PH_REDECIDE_GPU,
+    PH_N
+};
 
 // Device time per phase, resolved after the stream is synchronised.
 struct PhaseTimer {
     cudaStream_t st = nullptr;
+    int redirect = -1;  // when >= 0, every phase is booked to this one
     std::vector<cudaEvent_t> pool;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> open;
     size_t used = 0;
@@ -83,7 +96,7 @@ struct PhaseTimer {
     {
         cudaEvent_t e = get();
         CUDA_CHECK(cudaEventRecord(e, st));
-        open.push_back({phase, {b, e}});
+        open.push_back({redirect >= 0 ? redirect : phase, {b, e}});
     }
     void resolve(double *ms)
     {
@@ -100,6 +113,56 @@ struct PhaseTimer {
     {
         for (auto e : pool) {
             cudaEventDestroy(e);
+        }
+    }
+};
+
+// The streams, counters and scratch one FP64 evaluation runs on: the handle's
+// own, or the speculative re-decision's (SpecLane), which runs beside the fast
+// pass of the mixed mode.
+struct Fp64Ctx {
+    cudaStream_t st, st2;
+    cudaEvent_t ev_fork, ev_join;
+    PhaseTimer *timer;
+    mars_gpu_stats *stats;
+    DevBuf *Bx, *T, *svec, *snew, *ybx, *hsse, *hrow, *fired, *nfired, *tasks, *stasks, *scal,
+        *bsort, *bxsort, *cand;
+};
+
+struct SpecLane {
+    cudaStream_t st = nullptr, st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    PhaseTimer timer;
+    double phase_ms[PH_N] = {0};
+    mars_gpu_stats stats{};
+    DevBuf Bx, T, svec, snew, ybx, hsse, hrow, fired, nfired, tasks, stasks, scal, bsort, bxsort,
+        cand;
+    void init()
+    {
+        if (!st) {
+            CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            CUDA_CHECK(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+            CUDA_CHECK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+            CUDA_CHECK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+            timer.st = st;
+            timer.redirect = PH_REDECIDE_GPU;
+        }
+    }
+    Fp64Ctx ctx()
+    {
+        return {st,   st2,     ev_fork, ev_join, &timer, &stats,  &Bx,    &T,     &svec,   &snew,
+                &ybx, &hsse,   &hrow,   &fired,  &nfired, &tasks, &stasks, &scal, &bsort, &bxsort,
+                &cand};
+    }
+    ~SpecLane()
+    {
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamSynchronize(st2);
+            cudaStreamDestroy(st);
+            cudaStreamDestroy(st2);
+            cudaEventDestroy(ev_fork);
+            cudaEventDestroy(ev_join);
         }
     }
 };
@@ -133,6 +196,18 @@ struct mars_gpu_algo {
     DevBuf bsort, bxsort;  // per candidate: parent and normalised column in sorted order
     DevBuf fTp, fT, fmom, hflag;  // fast pass: split-K partials, T, parent moments, sweep flags
     DevBuf sort_keys, sort_vals, sort_tmp;
+    // Mixed mode: the exact re-decision speculated for the previous eval's
+    // contenders and for the columns appended since, beside the fast pass.
+    SpecLane spec;
+    std::vector<long long> prev_contend;  // sorted (xcol << 32 | bcol) keys
+    std::vector<long long> appended;      // (xcol << 32 | column) of appends since the last eval
+
+    Fp64Ctx ctx()
+    {
+        return {st,   st2,   ev_fork, ev_join, &timer, &stats,  &Bx,    &T,     &svec,   &snew,
+                &ybx, &hsse, &hrow,   &fired,  &nfired, &tasks, &stasks, &scal, &bsort, &bxsort,
+                &cand};
+    }
 
     ~mars_gpu_algo()
     {
@@ -317,19 +392,23 @@ void ensure_sorted(mars_gpu_algo *a, const std::vector<int> &cols)
     }
 }
 
-// The FP64 evaluation of candidates [0, Pc) (device arrays cx/cb). Fills
-// ybx, and hsse/hrow unless linear_only.
-void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
+// The FP64 evaluation of candidates [0, Pc) (device arrays cx/cb) on the
+// context c. Fills c's ybx, and hsse/hrow unless linear_only. count_work: add
+// the algorithmic FLOPs, bytes and knot evaluations to c's counters (not for
+// re-decisions, whose candidates the fast pass has counted).
+void eval_block_fp64(mars_gpu_algo *a, Fp64Ctx &c, int Pc, const int *cx_d, const int *cb_d,
                      const std::vector<int> &cx_h, int c0, int min_span, int head, int tail,
-                     bool linear_only)
+                     bool linear_only, bool count_work = true)
 {
     const int n = (int)a->n, m = (int)a->m;
-    float *Bx = a->Bx.as<float>();
+    float *Bx = c.Bx->as<float>();
     ProjectScratch ws;
-    ws.T = a->T.as<double>();
-    double *s = a->svec.as<double>();
+    ws.T = c.T->as<double>();
+    double *s = c.svec->as<double>();
 
-    a->stats.project_flops += 4.0 * (double)n * (double)m * (double)Pc;
+    if (count_work) {
+        c.stats->project_flops += 4.0 * (double)n * (double)m * (double)Pc;
+    }
     // The sweep's scalar recurrences need only the parents, y and the sorted
     // inputs: start them on the side stream, concurrent with the projection.
     if (!linear_only) {
@@ -344,52 +423,52 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
             }
             b = e;
         }
-        a->stasks.ensure(sizeof(SweepTask) * stasks.size());
-        CUDA_CHECK(cudaMemcpyAsync(a->stasks.ptr, stasks.data(),
+        c.stasks->ensure(sizeof(SweepTask) * stasks.size());
+        CUDA_CHECK(cudaMemcpyAsync(c.stasks->ptr, stasks.data(),
                                    sizeof(SweepTask) * stasks.size(), cudaMemcpyHostToDevice,
-                                   a->st));
-        a->stats.h2d_bytes += (long long)(sizeof(SweepTask) * stasks.size());
+                                   c.st));
+        c.stats->h2d_bytes += (long long)(sizeof(SweepTask) * stasks.size());
         // The gather is a wide, short kernel: on the handle's stream, so it does
         // not crowd out the single-wave chain kernels that the scalars overlap.
-        gather_parents(a->st, a->perm.as<int>(), a->B.as<float>(), a->n, cx_d, cb_d, n, tail, Pc,
-                       a->bsort.as<float>(), &a->stats.kernel_launches);
-        CUDA_CHECK(cudaEventRecord(a->ev_fork, a->st));
-        CUDA_CHECK(cudaStreamWaitEvent(a->st2, a->ev_fork, 0));
-        hinge_scalars(a->st2, a->stasks.as<SweepTask>(), (int)stasks.size(), a->xsort.as<float>(),
-                      a->ysort.as<float>(), a->bsort.as<float>(), n, head, tail, min_span,
-                      a->scal.as<double>(), &a->stats.kernel_launches);
-        CUDA_CHECK(cudaEventRecord(a->ev_join, a->st2));
+        gather_parents(c.st, a->perm.as<int>(), a->B.as<float>(), a->n, cx_d, cb_d, n, tail, Pc,
+                       c.bsort->as<float>(), &c.stats->kernel_launches);
+        CUDA_CHECK(cudaEventRecord(c.ev_fork, c.st));
+        CUDA_CHECK(cudaStreamWaitEvent(c.st2, c.ev_fork, 0));
+        hinge_scalars(c.st2, c.stasks->as<SweepTask>(), (int)stasks.size(), a->xsort.as<float>(),
+                      a->ysort.as<float>(), c.bsort->as<float>(), n, head, tail, min_span,
+                      c.scal->as<double>(), &c.stats->kernel_launches);
+        CUDA_CHECK(cudaEventRecord(c.ev_join, c.st2));
     }
-    cudaEvent_t t0 = a->timer.begin();
+    cudaEvent_t t0 = c.timer->begin();
     FillSrc src{a->B.as<float>(), a->n, a->X.as<float>(), a->n, a->s.as<float>(), cx_d, cb_d};
-    project_fp64(a->st, src, a->Bo.as<double>(), a->ldbo, n, m, Pc, nullptr, Bx, a->n, s, ws,
-                 &a->stats.kernel_launches);
-    a->timer.end(PH_PROJECT, t0);
+    project_fp64(c.st, src, a->Bo.as<double>(), a->ldbo, n, m, Pc, nullptr, Bx, a->n, s, ws,
+                 &c.stats->kernel_launches);
+    c.timer->end(PH_PROJECT, t0);
 
-    t0 = a->timer.begin();
-    dgks_gate(a->st, ws.T, m, Pc, s, a->tol, a->fired.as<int>(), a->nfired.as<int>(),
-              &a->stats.kernel_launches);
+    t0 = c.timer->begin();
+    dgks_gate(c.st, ws.T, m, Pc, s, a->tol, c.fired->as<int>(), c.nfired->as<int>(),
+              &c.stats->kernel_launches);
     int nf = 0;
-    CUDA_CHECK(cudaMemcpyAsync(&nf, a->nfired.ptr, sizeof(int), cudaMemcpyDeviceToHost, a->st));
-    sync(a);
+    CUDA_CHECK(cudaMemcpyAsync(&nf, c.nfired->ptr, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+    CUDA_CHECK(cudaStreamSynchronize(c.st));
     if (nf > 0) {
-        StoredSrc src2{Bx, a->n, a->fired.as<int>()};
-        project_fp64(a->st, src2, a->Bo.as<double>(), a->ldbo, n, m, nf, a->fired.as<int>(), Bx,
-                     a->n, a->snew.as<double>(), ws, &a->stats.kernel_launches);
-        scatter_s(a->st, a->fired.as<int>(), nf, a->snew.as<double>(), s,
-                  &a->stats.kernel_launches);
-        a->stats.dgks_fired += nf;
+        StoredSrc src2{Bx, a->n, c.fired->as<int>()};
+        project_fp64(c.st, src2, a->Bo.as<double>(), a->ldbo, n, m, nf, c.fired->as<int>(), Bx,
+                     a->n, c.snew->as<double>(), ws, &c.stats->kernel_launches);
+        scatter_s(c.st, c.fired->as<int>(), nf, c.snew->as<double>(), s,
+                  &c.stats->kernel_launches);
+        c.stats->dgks_fired += nf;
     }
-    a->timer.end(PH_DGKS, t0);
+    c.timer->end(PH_DGKS, t0);
 
-    t0 = a->timer.begin();
-    normalize_ybx(a->st, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), false,
-                  a->ybx.as<double>(), &a->stats.kernel_launches);
+    t0 = c.timer->begin();
+    normalize_ybx(c.st, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), false,
+                  c.ybx->as<double>(), &c.stats->kernel_launches);
     if (!linear_only) {
-        gather_candidates(a->st, a->perm.as<int>(), Bx, a->n, cx_d, s, a->tol, n, tail, Pc,
-                          a->bxsort.as<float>(), &a->stats.kernel_launches);
+        gather_candidates(c.st, a->perm.as<int>(), Bx, a->n, cx_d, s, a->tol, n, tail, Pc,
+                          c.bxsort->as<float>(), &c.stats->kernel_launches);
     }
-    a->timer.end(PH_NORMALIZE, t0);
+    c.timer->end(PH_NORMALIZE, t0);
 
     if (linear_only) {
         return;
@@ -401,26 +480,89 @@ void eval_block_fp64(mars_gpu_algo *a, int Pc, const int *cx_d, const int *cb_d,
         while (e < Pc && cx_h[c0 + e] == cx_h[c0 + b]) {
             ++e;
         }
-        a->stats.sweep_bytes += (double)tail * (12.0 + 4.0 * m + 8.0 * (e - b));
+        if (count_work) {
+            c.stats->sweep_bytes += (double)tail * (12.0 + 4.0 * m + 8.0 * (e - b));
+        }
         for (int t = b; t < e; t += warps) {
             tasks.push_back({cx_h[c0 + b], t, std::min(warps, e - t)});
         }
         b = e;
     }
-    a->tasks.ensure(sizeof(SweepTask) * tasks.size());
-    CUDA_CHECK(cudaMemcpyAsync(a->tasks.ptr, tasks.data(), sizeof(SweepTask) * tasks.size(),
-                               cudaMemcpyHostToDevice, a->st));
-    a->stats.h2d_bytes += (long long)(sizeof(SweepTask) * tasks.size());
-    CUDA_CHECK(cudaStreamWaitEvent(a->st, a->ev_join, 0));
-    t0 = a->timer.begin();
-    sweep_fp64(a->st, a->tasks.as<SweepTask>(), (int)tasks.size(), a->perm.as<int>(),
-               a->xsort.as<float>(), a->bsort.as<float>(), a->bxsort.as<float>(),
-               a->Bo.as<double>(), a->ldbo, a->ybo_d.as<double>(), a->ybx.as<double>(),
-               a->scal.as<double>(), n, m, head, tail, min_span, a->tol, a->hsse.as<double>(),
-               a->hrow.as<int>(), warps, &a->stats.kernel_launches);
-    a->timer.end(PH_SWEEP, t0);
-    a->stats.knot_evals += (long long)Pc * sweep_grid_rows(head, tail, min_span);
+    c.tasks->ensure(sizeof(SweepTask) * tasks.size());
+    CUDA_CHECK(cudaMemcpyAsync(c.tasks->ptr, tasks.data(), sizeof(SweepTask) * tasks.size(),
+                               cudaMemcpyHostToDevice, c.st));
+    c.stats->h2d_bytes += (long long)(sizeof(SweepTask) * tasks.size());
+    CUDA_CHECK(cudaStreamWaitEvent(c.st, c.ev_join, 0));
+    t0 = c.timer->begin();
+    sweep_fp64(c.st, c.tasks->as<SweepTask>(), (int)tasks.size(), a->perm.as<int>(),
+               a->xsort.as<float>(), c.bsort->as<float>(), c.bxsort->as<float>(),
+               a->Bo.as<double>(), a->ldbo, a->ybo_d.as<double>(), c.ybx->as<double>(),
+               c.scal->as<double>(), n, m, head, tail, min_span, a->tol, c.hsse->as<double>(),
+               c.hrow->as<int>(), warps, &c.stats->kernel_launches);
+    c.timer->end(PH_SWEEP, t0);
+    if (count_work) {
+        c.stats->knot_evals += (long long)Pc * sweep_grid_rows(head, tail, min_span);
+    }
 }
+
+// The exact FP64 evaluation of the candidates sx/sb on the speculative lane
+// (its own streams and scratch); results to the host vectors.
+void run_spec(mars_gpu_algo *a, const std::vector<int> &sx, const std::vector<int> &sb,
+              int min_span, int head, int tail, std::vector<ExactResult> &out)
+{
+    SpecLane &L = a->spec;
+    Fp64Ctx c = L.ctx();
+    const int C = (int)sx.size();
+    const size_t n = a->n, m = a->m;
+    L.cand.ensure(sizeof(int) * 2 * (size_t)C);
+    L.Bx.ensure(sizeof(float) * n * C);
+    L.svec.ensure(sizeof(double) * C);
+    L.ybx.ensure(sizeof(double) * C);
+    L.hsse.ensure(sizeof(double) * C);
+    L.hrow.ensure(sizeof(int) * C);
+    L.bsort.ensure(sizeof(float) * n * C);
+    L.bxsort.ensure(sizeof(float) * n * C);
+    L.T.ensure(sizeof(double) * std::max<size_t>(1, m * C));
+    L.snew.ensure(sizeof(double) * C);
+    L.fired.ensure(sizeof(int) * C);
+    L.nfired.ensure(sizeof(int) * 4);
+    L.scal.ensure(sizeof(double) * 3 *
+                  std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
+    int *ecx = L.cand.as<int>(), *ecb = ecx + C;
+    CUDA_CHECK(cudaMemcpyAsync(ecx, sx.data(), sizeof(int) * C, cudaMemcpyHostToDevice, L.st));
+    CUDA_CHECK(cudaMemcpyAsync(ecb, sb.data(), sizeof(int) * C, cudaMemcpyHostToDevice, L.st));
+    L.stats.h2d_bytes += (long long)(sizeof(int) * 2 * (size_t)C);
+    eval_block_fp64(a, c, C, ecx, ecb, sx, 0, min_span, head, tail, false, false);
+    std::vector<double> ybx(C), hs(C);
+    std::vector<int> hr(C);
+    CUDA_CHECK(cudaMemcpyAsync(ybx.data(), L.ybx.ptr, sizeof(double) * C, cudaMemcpyDeviceToHost,
+                               L.st));
+    CUDA_CHECK(cudaMemcpyAsync(hs.data(), L.hsse.ptr, sizeof(double) * C, cudaMemcpyDeviceToHost,
+                               L.st));
+    CUDA_CHECK(cudaMemcpyAsync(hr.data(), L.hrow.ptr, sizeof(int) * C, cudaMemcpyDeviceToHost,
+                               L.st));
+    L.stats.d2h_bytes += (long long)(20 * (size_t)C);
+    CUDA_CHECK(cudaStreamSynchronize(L.st));
+    L.timer.resolve(L.phase_ms);
+    out.resize(C);
+    for (int q = 0; q < C; ++q) {
+        out[q].ybx = ybx[q];
+        out[q].hinge_sse = hs[q];
+        out[q].hinge_row = hr[q];
+        out[q].hinge_pos = hr[q] >= 0 ? 0 : -1;
+    }
+}
+
+// Joins the speculative evaluation on every exit path of eval_mixed.
+struct SpecJoin {
+    std::thread th;
+    ~SpecJoin()
+    {
+        if (th.joinable()) {
+            th.join();
+        }
+    }
+};
 
 // Mixed precision (MARS_GPU_PREC_MIXED). Every candidate is ranked by the
 // FP32 / FP64-carry fast pass on the GPU; the best-ranked ones -- the top
@@ -477,6 +619,57 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
     CUDA_CHECK(cudaMemcpyAsync(cb_all, cb.data(), sizeof(int) * P, cudaMemcpyHostToDevice, a->st));
     a->stats.h2d_bytes += (long long)(sizeof(int) * 2 * (size_t)P);
 
+    // Speculative exact re-decision (MARS_GPU_MIXED_SPEC=1; off by default),
+    // beside the fast pass: the previous eval's contenders (an unresolvable cut
+    // or a degenerate column mostly stays so from one step to the next) and the
+    // candidates whose parent is a column appended since. Contenders it covers
+    // need no evaluation afterwards. It pays only when the contenders it misses
+    // are rare: each step that has any costs a full exact pass after the fast
+    // pass, and the concurrent FP64 kernels slow the fast pass down.
+    // MARS_GPU_MIXED_RANK_ONLY=1: return the fast values as they are, with no
+    // exact re-decision (to measure the fast pass's accuracy; not the
+    // reference's decisions).
+    const bool rank_only = env_double("MARS_GPU_MIXED_RANK_ONLY", 0.0) != 0.0;
+    std::vector<int> sp_j;
+    if (!linear_only && !rank_only && env_double("MARS_GPU_MIXED_SPEC", 0.0) != 0.0) {
+        for (int j = 0; j < P; ++j) {
+            const long long key = ((long long)cx[j] << 32) | (long long)(unsigned)cb[j];
+            if (std::binary_search(a->prev_contend.begin(), a->prev_contend.end(), key) ||
+                std::find(a->appended.begin(), a->appended.end(), key) != a->appended.end()) {
+                sp_j.push_back(j);
+            }
+        }
+        const double per_c = 12.0 * n + 24.0 * sweep_grid_rows(head, tail, min_span) + 64.0 * m;
+        const size_t spmax = (size_t)std::max(
+            0.0, std::min(env_double("MARS_GPU_MIXED_SPEC_MAX", 1024.0), budget / per_c));
+        if (sp_j.size() > spmax) {
+            sp_j.resize(spmax);
+        }
+    }
+    a->appended.clear();
+    std::vector<ExactResult> sp_res;
+    std::exception_ptr sp_err;
+    SpecJoin sp_join;
+    if (!sp_j.empty()) {
+        std::vector<int> sx(sp_j.size()), sb(sp_j.size());
+        for (size_t q = 0; q < sp_j.size(); ++q) {
+            sx[q] = cx[sp_j[q]];
+            sb[q] = cb[sp_j[q]];
+        }
+        int dev = 0;
+        CUDA_CHECK(cudaGetDevice(&dev));
+        a->spec.init();
+        a->stats.speculated += (long long)sp_j.size();
+        sp_join.th = std::thread([a, dev, sx, sb, min_span, head, tail, &sp_res, &sp_err] {
+            try {
+                CUDA_CHECK(cudaSetDevice(dev));
+                run_spec(a, sx, sb, min_span, head, tail, sp_res);
+            } catch (...) {
+                sp_err = std::current_exception();
+            }
+        });
+    }
+
     std::vector<double> fybx(P), fh(P, 0.0), fh2(2 * (size_t)P, 0.0), fs(P), fmom(3 * (size_t)P);
     std::vector<int> frow(P, -1), frow2(2 * (size_t)P, -1), fflag(2 * (size_t)P, 0);
     for (auto &b : blocks) {
@@ -498,6 +691,8 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
             gather_candidates(a->st, a->perm.as<int>(), a->Bx.as<float>(), a->n, cx_d,
                               a->svec.as<double>(), a->tol, n, n, Pc, a->bxsort.as<float>(),
                               &a->stats.kernel_launches);
+            a->timer.end(PH_GATHER, t0);
+            t0 = a->timer.begin();
             std::vector<FastTaskRec> tasks;
             const int warps = fast_sweep_warps(m, 2 * Pc);
             for (int q = 0; q < Pc;) {
@@ -551,6 +746,25 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         frow[j] = frow2[2 * (size_t)j + d];
     }
 
+    if (rank_only) {
+        // cut: the fast knot, or NaN where the candidate carries a flag
+        const float *Xh = a->hb.X;
+        const double degen = env_double("MARS_GPU_MIXED_DEGEN_REL", 1e-6);
+        for (int j = 0; j < P; ++j) {
+            const size_t idx = (size_t)cx[j] * m + cb[j];
+            lin[idx] = fybx[j] * fybx[j];
+            if (!linear_only && frow[j] >= 0) {
+                hin[idx] = lin[idx] + fh[j];
+                cut[idx] = (double)Xh[(size_t)frow[j] + (size_t)cx[j] * a->hb.ldx];
+            }
+            if (!linear_only && (fs[j] < degen * fmom[3 * (size_t)j + 2] ||
+                                 fflag[2 * (size_t)j] || fflag[2 * (size_t)j + 1])) {
+                cut[idx] = std::numeric_limits<double>::quiet_NaN();
+            }
+        }
+        return;
+    }
+
     // contenders: top-K and the band, by the fast linear and hinge values
     const auto t_host = std::chrono::steady_clock::now();
     const int topk = std::max(1, (int)env_double("MARS_GPU_MIXED_TOPK", 4));
@@ -593,31 +807,98 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         for (int j = 0; j < P; ++j) {
             if (fs[j] < degen * fmom[3 * (size_t)j + 2] || fflag[2 * (size_t)j] ||
                 fflag[2 * (size_t)j + 1]) {
-                contend[j] = 1;
+                contend[j] = 2;
+                ++a->stats.redecided_flagged;
             }
         }
     }
-    std::vector<int> ex_x, ex_b, ex_j;
-    std::vector<const int32_t *> ex_perm;
-    for (int j = 0; j < P; ++j) {
-        if (contend[j]) {
-            ex_j.push_back(j);
-            ex_x.push_back(cx[j]);
-            ex_b.push_back(cb[j]);
-            ex_perm.push_back(linear_only ? nullptr : a->perm_h.data() + (size_t)cx[j] * a->n);
+    {
+        std::vector<long long> keys;
+        for (int j = 0; j < P; ++j) {
+            if (contend[j]) {
+                keys.push_back(((long long)cx[j] << 32) | (long long)(unsigned)cb[j]);
+            }
+        }
+        std::sort(keys.begin(), keys.end());
+        a->prev_contend.swap(keys);
+    }
+
+    // the speculation's results
+    if (sp_join.th.joinable()) {
+        sp_join.th.join();
+    }
+    if (sp_err) {
+        std::rethrow_exception(sp_err);
+    }
+    std::vector<int> sp_of(P, -1);
+    for (size_t q = 0; q < sp_j.size(); ++q) {
+        sp_of[sp_j[q]] = (int)q;
+    }
+    // A ranked (not flagged) contender whose fast values are both below
+    // (1 - band) of the best exact values already known cannot be the first
+    // maximum: its exact value is within the band of its fast value (the
+    // premise of the band itself). Every speculated candidate is exact anyway.
+    if (!sp_j.empty()) {
+        double elb = -std::numeric_limits<double>::infinity(), ehb = elb;
+        for (const ExactResult &r : sp_res) {
+            const double l = r.ybx * r.ybx;
+            elb = std::max(elb, l);
+            if (r.hinge_pos >= 0) {
+                ehb = std::max(ehb, l + r.hinge_sse);
+            }
+        }
+        for (int j = 0; j < P; ++j) {
+            if (contend[j] == 1 && sp_of[j] < 0 && flin[j] < (1.0 - band) * elb &&
+                (linear_only || fhin[j] < (1.0 - band) * ehb)) {
+                contend[j] = 0;
+            }
         }
     }
-    std::vector<ExactResult> ex;
-    const int host_max = (int)env_double("MARS_GPU_MIXED_HOST_MAX", 128);
-    if ((int)ex_j.size() <= host_max) {
-        // few contenders: the host cores, whose serial f64 chains are ~50x
+    std::vector<int> ex_j;
+    for (int j = 0; j < P; ++j) {
+        if (contend[j] || sp_of[j] >= 0) {
+            ex_j.push_back(j);
+        }
+    }
+    if (!sp_j.empty()) {
+        SpecLane &L = a->spec;
+        a->stats.kernel_launches += L.stats.kernel_launches;
+        a->stats.h2d_bytes += L.stats.h2d_bytes;
+        a->stats.d2h_bytes += L.stats.d2h_bytes;
+        a->stats.dgks_fired += L.stats.dgks_fired;
+        L.stats = mars_gpu_stats{};
+        for (int ph = 0; ph < PH_N; ++ph) {
+            a->phase_ms[ph] += L.phase_ms[ph];
+            L.phase_ms[ph] = 0.0;
+        }
+    }
+    std::vector<ExactResult> ex(ex_j.size());
+    std::vector<int> lo_q, lo_x, lo_b;  // leftovers: contenders the speculation missed
+    std::vector<const int32_t *> lo_perm;
+    for (size_t q = 0; q < ex_j.size(); ++q) {
+        const int j = ex_j[q];
+        if (sp_of[j] >= 0) {
+            ex[q] = sp_res[sp_of[j]];
+            a->stats.redecided_spec += contend[j] ? 1 : 0;
+        } else {
+            lo_q.push_back((int)q);
+            a->stats.leftovers_flagged += contend[j] == 2 ? 1 : 0;
+            lo_x.push_back(cx[j]);
+            lo_b.push_back(cb[j]);
+            lo_perm.push_back(linear_only ? nullptr : a->perm_h.data() + (size_t)cx[j] * a->n);
+        }
+    }
+    std::vector<ExactResult> lo;
+    const int threads = std::max(1u, std::thread::hardware_concurrency());
+    const int host_max = (int)env_double("MARS_GPU_MIXED_HOST_MAX", threads);
+    if ((int)lo_q.size() <= host_max) {
+        // few leftovers: the host cores, whose serial f64 chains are ~50x
         // shorter in latency than the GPU's
-        const int threads = std::max(1u, std::thread::hardware_concurrency());
-        exact_candidates(a->hb, ex_x, ex_b, ex_perm, min_span, head, tail, ex, threads);
+        exact_candidates(a->hb, lo_x, lo_b, lo_perm, min_span, head, tail, lo, threads);
     } else {
-        // many contenders: the FP64 GPU path over them (its time hardly depends
-        // on the candidate count)
-        const int C = (int)ex_j.size();
+        // many: the FP64 GPU path over them (its time hardly depends on the
+        // candidate count)
+        const int C = (int)lo_q.size();
         a->cand.ensure(sizeof(int) * 2 * (size_t)C);
         a->Bx.ensure(sizeof(float) * a->n * C);
         a->svec.ensure(sizeof(double) * C);
@@ -637,12 +918,18 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
                            std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
         }
         int *ecx = a->cand.as<int>(), *ecb = ecx + C;
-        CUDA_CHECK(cudaMemcpyAsync(ecx, ex_x.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
+        CUDA_CHECK(cudaMemcpyAsync(ecx, lo_x.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
                                    a->st));
-        CUDA_CHECK(cudaMemcpyAsync(ecb, ex_b.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
+        CUDA_CHECK(cudaMemcpyAsync(ecb, lo_b.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
                                    a->st));
         a->stats.h2d_bytes += (long long)(sizeof(int) * 2 * (size_t)C);
-        eval_block_fp64(a, C, ecx, ecb, ex_x, 0, min_span, head, tail, linear_only);
+        struct Redirect {
+            PhaseTimer &t;
+            ~Redirect() { t.redirect = -1; }
+        } guard{a->timer};
+        a->timer.redirect = PH_REDECIDE_GPU;
+        Fp64Ctx c = a->ctx();
+        eval_block_fp64(a, c, C, ecx, ecb, lo_x, 0, min_span, head, tail, linear_only, false);
         std::vector<double> eybx(C), ehs(C, 0.0);
         std::vector<int> ehr(C, -1);
         CUDA_CHECK(cudaMemcpyAsync(eybx.data(), a->ybx.ptr, sizeof(double) * C,
@@ -655,15 +942,21 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         }
         a->stats.d2h_bytes += (long long)(20 * (size_t)C);
         sync(a);
-        ex.resize(C);
+        lo.resize(C);
         for (int q = 0; q < C; ++q) {
-            ex[q].ybx = eybx[q];
-            ex[q].hinge_sse = ehs[q];
-            ex[q].hinge_row = ehr[q];
-            ex[q].hinge_pos = ehr[q] >= 0 ? 0 : -1;
+            lo[q].ybx = eybx[q];
+            lo[q].hinge_sse = ehs[q];
+            lo[q].hinge_row = ehr[q];
+            lo[q].hinge_pos = ehr[q] >= 0 ? 0 : -1;
         }
     }
-    a->stats.redecided += (long long)ex_j.size();
+    for (size_t q = 0; q < lo_q.size(); ++q) {
+        ex[lo_q[q]] = lo[q];
+    }
+    for (int j : ex_j) {
+        a->stats.redecided += contend[j] ? 1 : 0;
+    }
+    a->stats.leftovers += (long long)lo_q.size();
 
     // assemble: exact values for the contenders, fast values held below them for the rest
     double lbest = -std::numeric_limits<double>::infinity(), hbest = lbest;
@@ -799,7 +1092,9 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         for (auto &b : blocks) {
             const int c0 = b.first, Pc = b.second - b.first;
             const int *cx_d = cx_all + c0, *cb_d = cb_all + c0;
-            eval_block_fp64(a, Pc, cx_d, cb_d, cx, c0, min_span, head, tail, linear_only != 0);
+            Fp64Ctx c = a->ctx();
+            eval_block_fp64(a, c, Pc, cx_d, cb_d, cx, c0, min_span, head, tail,
+                            linear_only != 0);
             assemble_outputs(a->st, Pc, cx_d, cb_d, m, a->ybx.as<double>(), a->hsse.as<double>(),
                              a->hrow.as<int>(), a->X.as<float>(), a->n, linear_only != 0, o_lin,
                              o_hin, o_cut, &a->stats.kernel_launches);
@@ -853,6 +1148,7 @@ double append_impl(mars_gpu_algo *a, char type, int xcol, int bcol, float h)
         CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.as<double>() + m, &a->hb.ybo[m], sizeof(double),
                                    cudaMemcpyHostToDevice, a->st));
         a->stats.h2d_bytes += (long long)(sizeof(float) * n + sizeof(double));
+        a->appended.push_back(((long long)xcol << 32) | (long long)m);
         a->m = a->hb.m;
         a->ybo = a->hb.ybo;
     }
@@ -992,6 +1288,8 @@ int mars_gpu_get_stats(const mars_gpu_algo *a, mars_gpu_stats *out)
     out->ms_sort = a->phase_ms[PH_SORT];
     out->ms_append = a->phase_ms[PH_APPEND];
     out->ms_redecide = a->phase_ms[PH_REDECIDE];
+    out->ms_gather = a->phase_ms[PH_GATHER];
+    out->ms_redecide_gpu = a->phase_ms[PH_REDECIDE_GPU];
     out->ms_span = 0.0;
     if (a->span_started) {
         float t = 0.f;

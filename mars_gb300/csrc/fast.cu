@@ -6,16 +6,17 @@
 // block sums.
 //
 // Hinge sweep: the reference's recurrences (marsalgo.cc:576-649 with
-// covariates_impl :91-151) in chunks of FS_ROWS sorted rows: inside a chunk the
-// increments are FP32, across chunks the running values are carried in FP64:
+// covariates_impl :91-151) in chunks of sorted rows: inside a chunk the
+// increments are f32 (the running sums of products exact as f32 pairs),
+// across chunks the running values are carried as float-float pairs:
 //   g_c(i) = G_c + q_c(i)
 //   f_c(i) = F_c + G_c D(i) + e_c(i)      (D(i): sum of the chunk's deltas to row i)
-// with e_c += d q_c, q_c += b x_c in FP32. Besides the basis columns and the
+// with e_c += d q_c, q_c += b x_c. Besides the basis columns and the
 // candidate column, two more components carry the scalar recurrences: x = y
 // (g = vb, f = w) and x = b (g = b2, f = bd), and K = k0 + k1 follows as
 //   K(i) = K + 2 F_b D(i) + G_b D(i)^2 + kl(i),   kl += d^2 q_b + 2 d e_b.
-// A grid row stores only the FP32 increments; the scores are rebuilt in FP64
-// from the carries, 32 grid rows at a time (lane = grid row).
+// A grid row stores only the f32 increments; the scores are rebuilt from the
+// chunk's float-float anchors, 32 grid rows at a time (lane = grid row).
 #include "fast.cuh"
 
 #include <algorithm>
@@ -200,10 +201,10 @@ __global__ void __launch_bounds__(256) k_parent_moments(FillSrc src, int n, doub
 // ---------------------------------------------------------------------------
 // Chunked sweep. Block = one input column, one direction and up to W
 // candidates (warps 0..W-1, lane = component) plus two loader warps that stage
-// each chunk with cp.async: warp W the gathered f32 Bo rows (16 bytes per
-// lane), warp W+1, lanes over rows, the sorted parent and candidate values, y
-// and x, then the f32 deltas and their f64 running sums within the chunk
-// (copies in flight are limited per warp, so the staging is split).
+// each 32-row stage with cp.async: warp W the gathered f32 Bo rows (16 bytes
+// per lane), warp W+1, lanes over rows, the sorted parent and candidate
+// values, y and x, then the f32 deltas (copies in flight are limited per
+// warp, so the staging is split).
 //
 // Directions. Forward tasks sweep the descending order from the top and score
 // the cuts of its first half. Near the bottom the hinge (x - t)+ b differs
@@ -214,45 +215,99 @@ __global__ void __launch_bounds__(256) k_parent_moments(FillSrc src, int n, doub
 // recurrences on the reversed order, deltas x_cur - x_prev) and score the
 // cuts of the second half, where that mirror is small.
 //
-// Scoring, 32 grid rows at a time: first the per-chunk f64 sums
-// FF = sum F_c^2, FG = sum F_c G_c, GG = sum G_c^2, Fy = sum F_c yc_c,
-// Gy = sum G_c yc_c (one lane per chunk and sum), then per grid row (one lane
-// each), with f32 cross terms against f32 copies of the carries,
-//   ff = FF + 2D FG + D^2 GG + 2 (sum F_c e_c + D sum G_c e_c) + sum e_c^2
-//   fy = Fy + D Gy + sum e_c yc_c,   w = F_y + D G_y + e_y,
-//   K  = K + 2 F_b D + G_b D^2 + kl.
+// Arithmetic (no FP64 instruction: the FP64 pipe of this GPU issues one warp
+// instruction per 64 cycles per sub-partition). A chunk is FS_CHUNK stages
+// (64 rows). Inside a chunk, per component, e += d q in f32 and q += b x with
+// the f32 products summed exactly as an unevaluated pair (q_hi, q_lo) by
+// Knuth's two-sum: the rounding of a long f32 running sum, not of its
+// products, is what would otherwise dominate the error of den (measured on a
+// fit of n = 1e5: ~20x the error of the exact sum). At a chunk end
+// the carries (float-float pairs, Dekker's arithmetic) take the increments,
+//   K += Dc (2 F_b + G_b Dc) + kl,   F += G Dc + e,   G += q,
+// with Dc = x_base - x_end formed exactly. Scoring, 32 grid rows at a time:
+// per chunk, the float-float sums over the basis and candidate components
+//   FF = sum F_c^2, FG = sum F_c G_c, GG = sum G_c^2, Fy = sum F_c yc_c, Gy = sum G_c yc_c
+// (lane = chunk and sum) give the chunk's anchors, in which the large terms
+// cancel in float-float and only the differences are rounded to f32:
+//   A0 = K - FF, A1 = 2 (F_b - FG), A2 = G_b - GG, B0 = Fy - F_y, B1 = Gy - G_y;
+// then per grid row (lane = grid row), in f32, with D = x_base - x exact as a pair,
+//   den = A0 + D (A1 + D A2) + kl - 2 (Fe + D Ge) - ee,   uw = B0 + D B1 + ey - e_y,
+// Fe = sum F_c e_c, Ge = sum G_c e_c, ee = sum e_c^2, ey = sum yc_c e_c.
 // ---------------------------------------------------------------------------
-constexpr int FS_ROWS = 32, FS_SNAP = 32, FS_HIST = 6, FS_NSUM = 5, FS_MAXW = 8;
+constexpr int FS_ROWS = 32, FS_CHUNK = 2, FS_SNAP = 32, FS_HIST = 6, FS_NSUM = 5, FS_MAXW = 8;
 
 using FastTask = FastTaskRec;  // dir 0: forward (first half of the cuts), 1: mirror (second half)
 
+// Error-free transformations (Knuth's two-sum, Dekker's fast two-sum and
+// product with a fused multiply-add); the explicit _rn intrinsics keep the
+// compiler from contracting or reassociating them.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &err)
+{
+    s = __fadd_rn(a, b);
+    const float bv = __fsub_rn(s, a);
+    const float av = __fsub_rn(s, bv);
+    err = __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+}
+
+__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &err)
+{
+    s = __fadd_rn(a, b);
+    err = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// (ah, al) += (bh, bl)
+__device__ __forceinline__ void ff_add(float &ah, float &al, float bh, float bl)
+{
+    float s, e;
+    two_sum(ah, bh, s, e);
+    e = __fadd_rn(e, __fadd_rn(al, bl));
+    fast_two_sum(s, e, ah, al);
+}
+
+// (ph, pl) = (ah, al) (bh, bl)
+__device__ __forceinline__ void ff_mul(float ah, float al, float bh, float bl, float &ph,
+                                       float &pl)
+{
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    fast_two_sum(p, e, ph, pl);
+}
+
+// (ah - bh) + (al - bl) rounded to f32
+__device__ __forceinline__ float ff_diff(float ah, float al, float bh, float bl)
+{
+    float s, e;
+    two_sum(ah, -bh, s, e);
+    return __fadd_rn(s, __fadd_rn(e, __fsub_rn(al, bl)));
+}
+
 struct FastSweepSmem {
-    size_t hF, hG, hK, cst, sD, ybo, dpre, hFf, hGf, sE, sKL, sCh, srow, sXv, ycf, bo, raw, dsm,
-        total;
+    size_t hFh, hFl, hGh, hGl, hK, hXb, cA, csum, sE, sKL, sCh, srow, sXv, ycf, bo, raw, dsm,
+        zero, total;
     __host__ __device__ FastSweepSmem(int m, int W, int S)
     {
-        const int nc = m + 3;
+        const size_t ncs = (size_t)((m + 3) | 1);  // odd stride: conflict-free column reads
         size_t o = 0;
-        hF = o;  // [W][FS_HIST][nc] f64 carries at chunk starts
-        o += 8 * (size_t)W * FS_HIST * nc;
-        hG = o;
-        o += 8 * (size_t)W * FS_HIST * nc;
-        hK = o;  // [W][FS_HIST]
-        o += 8 * (size_t)W * FS_HIST;
-        cst = o;  // [W][FS_HIST][FS_NSUM] per-chunk f64 sums
-        o += 8 * (size_t)W * FS_HIST * FS_NSUM;
-        sD = o;  // [FS_SNAP] f64 D at the grid row
-        o += 8 * FS_SNAP;
-        ybo = o;  // [m + 1] f64 (component m: the candidate's ybx, per warp below)
-        o += 8 * ((size_t)m + 1);
-        dpre = o;  // [2][FS_ROWS] f64 running delta sums of a chunk
-        o += 8 * 2 * FS_ROWS;
-        hFf = o;  // [W][FS_HIST][nc] f32 copies of the carries
-        o += 4 * (size_t)W * FS_HIST * nc;
-        hGf = o;
-        o += 4 * (size_t)W * FS_HIST * nc;
-        sE = o;  // [W][FS_SNAP][nc] f32 increments e at grid rows
-        o += 4 * (size_t)W * FS_SNAP * nc;
+        hFh = o;  // [W][FS_HIST][ncs] carries at chunk starts, float-float
+        o += 4 * (size_t)W * FS_HIST * ncs;
+        hFl = o;
+        o += 4 * (size_t)W * FS_HIST * ncs;
+        hGh = o;
+        o += 4 * (size_t)W * FS_HIST * ncs;
+        hGl = o;
+        o += 4 * (size_t)W * FS_HIST * ncs;
+        hK = o;  // [W][FS_HIST][2]
+        o += 4 * (size_t)W * FS_HIST * 2;
+        hXb = o;  // [FS_HIST] x at the chunk's base
+        o += 4 * FS_HIST;
+        cA = o;  // [W][FS_HIST][FS_NSUM] f32 anchors A0, A1, A2, B0, B1
+        o += 4 * (size_t)W * FS_HIST * FS_NSUM;
+        csum = o;  // [W][FS_HIST][FS_NSUM][2] float-float chunk sums
+        o += 4 * (size_t)W * FS_HIST * FS_NSUM * 2;
+        sE = o;  // [W][FS_SNAP][ncs] f32 increments e at grid rows
+        o += 4 * (size_t)W * FS_SNAP * ncs;
         sKL = o;  // [W][FS_SNAP]
         o += 4 * (size_t)W * FS_SNAP;
         sCh = o;  // [FS_SNAP] chunk history index of the grid row
@@ -261,8 +316,8 @@ struct FastSweepSmem {
         o += 4 * FS_SNAP;
         sXv = o;  // [FS_SNAP] f32 x (the knot) of the grid row
         o += 4 * FS_SNAP;
-        ycf = o;  // [W][m + 1] f32 y coefficients (ybo, then ybx)
-        o += 4 * (size_t)W * (m + 1);
+        ycf = o;  // [W][m + 1][2] float-float y coefficients (ybo, then ybx)
+        o += 8 * (size_t)W * (m + 1);
         o = (o + 15) / 16 * 16;  // 16-byte cp.async destinations
         bo = o;  // [S][FS_ROWS][mp] f32, row stride mp = m rounded up to 4
         o += 4 * (size_t)S * FS_ROWS * ((m + 3) / 4 * 4);
@@ -270,12 +325,14 @@ struct FastSweepSmem {
         o += 4 * (size_t)S * ((2 * W + 1) * FS_ROWS + FS_ROWS + 1);
         dsm = o;  // [2][FS_ROWS] f32 deltas
         o += 4 * 2 * FS_ROWS;
+        zero = o;  // one f32 zero
+        o += 4;
         total = (o + 15) / 16 * 16;
     }
 };
 
 template <int CPL, int S>
-__global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
+__global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
     k_fast_sweep(const FastTask *__restrict__ tasks, const int *__restrict__ perm,
                  const float *__restrict__ xsort, const float *__restrict__ ysort,
                  const float *__restrict__ bs, const float *__restrict__ bxs,
@@ -287,18 +344,18 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
     extern __shared__ __align__(16) unsigned char sm[];
     const int W = (blockDim.x >> 5) - 2;  // candidate warps; then the two loaders
     const int NC = m + 3;  // basis columns, candidate, y, b
+    const int NCS = NC | 1;
     const int U = (m + 3) / 4, MP = 4 * U;  // 16-byte units per Bo row, padded row stride
     const int RAW = (2 * W + 1) * FS_ROWS + FS_ROWS + 1;
     const FastSweepSmem L(m, W, S);
-    double *hF = reinterpret_cast<double *>(sm + L.hF);
-    double *hG = reinterpret_cast<double *>(sm + L.hG);
-    double *hK = reinterpret_cast<double *>(sm + L.hK);
-    double *cst = reinterpret_cast<double *>(sm + L.cst);
-    double *sD = reinterpret_cast<double *>(sm + L.sD);
-    double *sybo = reinterpret_cast<double *>(sm + L.ybo);
-    double *dpre = reinterpret_cast<double *>(sm + L.dpre);
-    float *hFf = reinterpret_cast<float *>(sm + L.hFf);
-    float *hGf = reinterpret_cast<float *>(sm + L.hGf);
+    float *hFh = reinterpret_cast<float *>(sm + L.hFh);
+    float *hFl = reinterpret_cast<float *>(sm + L.hFl);
+    float *hGh = reinterpret_cast<float *>(sm + L.hGh);
+    float *hGl = reinterpret_cast<float *>(sm + L.hGl);
+    float *hK = reinterpret_cast<float *>(sm + L.hK);
+    float *hXb = reinterpret_cast<float *>(sm + L.hXb);
+    float *cA = reinterpret_cast<float *>(sm + L.cA);
+    float *csum = reinterpret_cast<float *>(sm + L.csum);
     float *sE = reinterpret_cast<float *>(sm + L.sE);
     float *sKL = reinterpret_cast<float *>(sm + L.sKL);
     int *sCh = reinterpret_cast<int *>(sm + L.sCh);
@@ -308,6 +365,10 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
     float *sbo = reinterpret_cast<float *>(sm + L.bo);
     float *sraw4 = reinterpret_cast<float *>(sm + L.raw);
     float *dsm = reinterpret_cast<float *>(sm + L.dsm);
+    float *zero = reinterpret_cast<float *>(sm + L.zero);
+    if (threadIdx.x == 0) {
+        *zero = 0.f;
+    }
 
     const FastTask task = tasks[blockIdx.x];
     const bool rev = task.dir != 0;
@@ -320,12 +381,12 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
     const float *ys = ysort + (size_t)task.xcol * n;
     const float *bsb = bs + (size_t)task.cand0 * n;
     const float *bxb = bxs + (size_t)task.cand0 * n;
-    for (int c = threadIdx.x; c < m; c += blockDim.x) {
-        sybo[c] = ybo[c];
-    }
     for (int e = threadIdx.x; e < W * (m + 1); e += blockDim.x) {
         const int w = e / (m + 1), c = e % (m + 1);
-        sycf[e] = (float)(c < m ? ybo[c] : (w < task.count ? ybx[task.cand0 + w] : 0.0));
+        const double v = c < m ? ybo[c] : (w < task.count ? ybx[task.cand0 + w] : 0.0);
+        const float hi = (float)v;
+        sycf[2 * e] = hi;
+        sycf[2 * e + 1] = (float)(v - (double)hi);
     }
     __syncthreads();
 
@@ -382,106 +443,126 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
             cp_async4(rw + (2 * W + 1) * FS_ROWS, xs + (s0 > 0 ? idx(s0 - 1) : 0), s0 > 0);
         }
     };
-    // Stage sq (landed): f32 deltas and their f64 running sums (lanes = rows).
+    // Stage sq (landed): the f32 deltas of its rows (lanes = rows), formed as
+    // the reference forms them (marsalgo.cc:523-525).
     auto deltas = [&](int sq) {
         const float *xr = sraw4 + (size_t)(sq % S) * RAW + (2 * W + 1) * FS_ROWS;
         const int h = sq & 1, s = sq * FS_ROWS + lane;
         const bool ok = s < len && s > 0;
-        const float d = ok ? (rev ? xr[lane + 1] - xr[lane] : xr[lane] - xr[lane + 1]) : 0.f;
-        // running sum of the chunk's deltas through this row: telescoped, the
-        // f64 difference of the x at the chunk's base and at the row
-        const float base = sq == 0 ? xr[1] : xr[0];
-        const double run = rev ? (double)xr[lane + 1] - (double)base
-                               : (double)base - (double)xr[lane + 1];
-        dsm[h * FS_ROWS + lane] = d;
-        dpre[h * FS_ROWS + lane] = run;
+        dsm[h * FS_ROWS + lane] = ok ? (rev ? xr[lane + 1] - xr[lane] : xr[lane] - xr[lane + 1]) : 0.f;
     };
 
     const int wsel = cwarp ? warp : 0;
     const int mycand = task.cand0 + wsel;
-    double F[CPL], G[CPL], K = 0.0;
-    float e[CPL], q[CPL], kl = 0.f;
+    float Fh[CPL], Fl[CPL], Gh[CPL], Gl[CPL], qh[CPL], ql[CPL], e[CPL];
+    float Kh = 0.f, Kl = 0.f, kl = 0.f;  // K on the lane of the b component
 #pragma unroll
     for (int u = 0; u < CPL; ++u) {
-        F[u] = 0.0;
-        G[u] = 0.0;
-        e[u] = 0.f;
-        q[u] = 0.f;
+        Fh[u] = Fl[u] = Gh[u] = Gl[u] = qh[u] = ql[u] = e[u] = 0.f;
     }
-    double *myF = hF + (size_t)wsel * FS_HIST * NC;
-    double *myG = hG + (size_t)wsel * FS_HIST * NC;
-    float *myFf = hFf + (size_t)wsel * FS_HIST * NC;
-    float *myGf = hGf + (size_t)wsel * FS_HIST * NC;
-    double *myK = hK + (size_t)wsel * FS_HIST;
-    double *myC = cst + (size_t)wsel * FS_HIST * FS_NSUM;
-    float *myE = sE + (size_t)wsel * FS_SNAP * NC;
+    float *myFh = hFh + (size_t)wsel * FS_HIST * NCS;
+    float *myFl = hFl + (size_t)wsel * FS_HIST * NCS;
+    float *myGh = hGh + (size_t)wsel * FS_HIST * NCS;
+    float *myGl = hGl + (size_t)wsel * FS_HIST * NCS;
+    float *myK = hK + (size_t)wsel * FS_HIST * 2;
+    float *myC = csum + (size_t)wsel * FS_HIST * FS_NSUM * 2;
+    float *myA = cA + (size_t)wsel * FS_HIST * FS_NSUM;
+    float *myE = sE + (size_t)wsel * FS_SNAP * NCS;
     float *myKL = sKL + (size_t)wsel * FS_SNAP;
-    const float *myY = sycf + (size_t)wsel * (m + 1);
-    const double ybx_c = ybx[mycand];
-    const int cb = m + 2;  // the b component (K lives on its lane)
-    const double S0 = mom[3 * (size_t)mycand], S1 = mom[3 * (size_t)mycand + 1],
-                 S2 = mom[3 * (size_t)mycand + 2];
-    double best = 0.0;
+    const float *myY = sycf + (size_t)wsel * (m + 1) * 2;
+    const int cy = m + 1, cb = m + 2;  // the y and b components
+    const float S0 = (float)mom[3 * (size_t)mycand], S1 = (float)mom[3 * (size_t)mycand + 1],
+                S2 = (float)mom[3 * (size_t)mycand + 2];
+    const float tolf = (float)tol, cutf = (float)cut_rel;
+    float best = 0.f;
     int besti = -1;
     int flagged = 0;  // a cut the reference's f64 evaluation cannot resolve
-    int nsnap = 0, nhist = 0;  // block-uniform
+    int nsnap = 0, nhist = 0, cur = 0;  // block-uniform
+    float xbase = 0.f;                  // x at the current chunk's base (block-uniform)
 
     auto flush = [&]() {
         if (cwarp) {
-            // per-chunk f64 sums, lane = chunk * FS_NSUM + sum
+            // per-chunk float-float sums, lane = chunk * FS_NSUM + sum
+            // (0 FF, 1 FG, 2 GG, 3 Fy, 4 Gy) over the basis and candidate components
             if (lane < nhist * FS_NSUM) {
                 const int ch = lane / FS_NSUM, t = lane % FS_NSUM;
-                const double *Fh = myF + (size_t)ch * NC, *Gh = myG + (size_t)ch * NC;
-                double acc = 0.0;
+                const bool ag = t == 2 || t == 4, bf = t == 0, by = t >= 3;
+                const float *Ah = (ag ? myGh : myFh) + (size_t)ch * NCS;
+                const float *Al = (ag ? myGl : myFl) + (size_t)ch * NCS;
+                const float *Bh = (bf ? myFh : myGh) + (size_t)ch * NCS;
+                const float *Bl = (bf ? myFl : myGl) + (size_t)ch * NCS;
+                float sh = 0.f, sl = 0.f;
                 for (int c = 0; c <= m; ++c) {
-                    // t: 0 FF, 1 FG, 2 GG, 3 Fy, 4 Gy
-                    const double yc = c < m ? sybo[c] : ybx_c;
-                    const double a = (t == 2 || t == 4) ? Gh[c] : Fh[c];
-                    const double b = t == 0 ? Fh[c] : (t == 1 || t == 2) ? Gh[c] : yc;
-                    acc = fma(a, b, acc);
+                    const float bh = by ? myY[2 * c] : Bh[c], bl = by ? myY[2 * c + 1] : Bl[c];
+                    const float ah = Ah[c], al = Al[c];
+                    const float p = __fmul_rn(ah, bh);
+                    float pe = __fmaf_rn(ah, bh, -p);
+                    pe = __fmaf_rn(ah, bl, pe);
+                    pe = __fmaf_rn(al, bh, pe);
+                    float s, err;
+                    two_sum(sh, p, s, err);
+                    sl = __fadd_rn(sl, __fadd_rn(err, pe));
+                    sh = s;
                 }
-                myC[ch * FS_NSUM + t] = acc;
+                myC[(ch * FS_NSUM + t) * 2] = sh;
+                myC[(ch * FS_NSUM + t) * 2 + 1] = sl;
             }
             __syncwarp();
-            double sse = -1.0;
+            if (lane < nhist) {
+                const int ch = lane;
+                const float *C = myC + ch * FS_NSUM * 2;
+                const float *Fc = myFh + (size_t)ch * NCS, *Fcl = myFl + (size_t)ch * NCS;
+                const float *Gc = myGh + (size_t)ch * NCS, *Gcl = myGl + (size_t)ch * NCS;
+                float *A = myA + ch * FS_NSUM;
+                A[0] = ff_diff(myK[2 * ch], myK[2 * ch + 1], C[0], C[1]);
+                A[1] = 2.0f * ff_diff(Fc[cb], Fcl[cb], C[2], C[3]);
+                A[2] = ff_diff(Gc[cb], Gcl[cb], C[4], C[5]);
+                A[3] = ff_diff(C[6], C[7], Fc[cy], Fcl[cy]);
+                A[4] = ff_diff(C[8], C[9], Gc[cy], Gcl[cy]);
+            }
+            __syncwarp();
+            float sse = -1.f;
             int row = 0x7fffffff;
             if (lane < nsnap) {
                 const int ch = sCh[lane];
-                const double D = sD[lane];
-                const float *Ff = myFf + (size_t)ch * NC, *Gf = myGf + (size_t)ch * NC;
-                const float *Eg = myE + (size_t)lane * NC;
+                const float xg = sXv[lane];
+                float Dh, Dl;
+                two_sum(hXb[ch], -xg, Dh, Dl);
+                if (rev) {
+                    Dh = -Dh;
+                    Dl = -Dl;
+                }
+                const float *Fc = myFh + (size_t)ch * NCS, *Gc = myGh + (size_t)ch * NCS;
+                const float *Eg = myE + (size_t)lane * NCS;
                 float Fe = 0.f, Ge = 0.f, ee = 0.f, ey = 0.f;
                 for (int c = 0; c <= m; ++c) {
                     const float ec = Eg[c];
-                    Fe = fmaf(Ff[c], ec, Fe);
-                    Ge = fmaf(Gf[c], ec, Ge);
+                    Fe = fmaf(Fc[c], ec, Fe);
+                    Ge = fmaf(Gc[c], ec, Ge);
                     ee = fmaf(ec, ec, ee);
-                    ey = fmaf(myY[c], ec, ey);
+                    ey = fmaf(myY[2 * c], ec, ey);
                 }
-                const double *C = myC + (size_t)ch * FS_NSUM;
-                const double *Fh = myF + (size_t)ch * NC, *Gh = myG + (size_t)ch * NC;
-                const double ff = C[0] + D * (2.0 * C[1] + D * C[2]) +
-                                  2.0 * ((double)Fe + D * (double)Ge) + (double)ee;
-                const double fy = C[3] + D * C[4] + (double)ey;
-                const double w = fma(Gh[m + 1], D, Fh[m + 1]) + (double)Eg[m + 1];
-                const double Kg = myK[ch] + D * (2.0 * Fh[cb] + D * Gh[cb]) + (double)myKL[lane];
-                const double uw = fy - w;
-                const double den = Kg - ff;
-                sse = den > tol ? (uw * uw) / (den + tol) : 0.0;
+                const float *A = myA + ch * FS_NSUM;
+                const float klg = myKL[lane];
+                const float t1 = fmaf(Dh, A[2], A[1]);
+                const float small = klg - 2.0f * fmaf(Dh, Ge, Fe) - ee;
+                const float den = fmaf(Dh, t1, A[0]) + fmaf(Dl, fmaf(2.0f * Dh, A[2], A[1]), small);
+                const float uw = fmaf(Dh, A[4], A[3]) + fmaf(Dl, A[4], ey - Eg[cy]);
+                sse = den > tolf ? (uw * uw) / (den + tolf) : 0.f;
                 row = srow[lane];
                 // The reference forms den as (k0 + k1) - ff with k0 + k1 the
                 // top-side K; when den is below cut_rel of it, that difference
                 // is near the level of its f64 rounding and its value may be
                 // anything: such a candidate is re-decided exactly.
-                const double t = (double)sXv[lane];
-                const double Kref = rev ? fmax(S2 - 2.0 * t * S1 + t * t * S0 - Kg, 0.0) : Kg;
-                if (den < cut_rel * Kref) {
+                const float Kg = myK[2 * ch] + Dh * (2.0f * Fc[cb] + Dh * Gc[cb]) + klg;
+                const float Kref = rev ? fmaxf(S2 - 2.0f * xg * S1 + xg * xg * S0 - Kg, 0.0f) : Kg;
+                if (den < cutf * Kref) {
                     flagged = 1;
                 }
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                const double s2 = __shfl_xor_sync(0xffffffffu, sse, o);
+                const float s2 = __shfl_xor_sync(0xffffffffu, sse, o);
                 const int r2 = __shfl_xor_sync(0xffffffffu, row, o);
                 if (s2 > sse || (s2 == sse && r2 < row)) {
                     sse = s2;
@@ -526,47 +607,87 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
     for (int sq = 0; sq < nstages; ++sq) {
         const int sg = sq % S, h = sq & 1, s0 = sq * FS_ROWS;
         const int rows = min(FS_ROWS, len - s0);
+        const bool cstart = sq % FS_CHUNK == 0;
+        const bool cend = sq % FS_CHUNK == FS_CHUNK - 1 || sq == nstages - 1;
+        const float *xr = sraw4 + (size_t)sg * RAW + (2 * W + 1) * FS_ROWS;
         int gcount = 0;
         for (long gr = next_grid; gr < s0 + rows && gr <= last_step; gr += min_span) {
             ++gcount;
         }
-        if (nsnap + gcount > FS_SNAP || nhist == FS_HIST) {
+        if (nsnap + gcount > FS_SNAP || (cstart && nhist == FS_HIST)) {
             flush();
             __syncthreads();  // snapshot and history slots are rewritten below
-        }
-        if (cwarp) {
-            // carries at the start of this chunk (f64, and f32 copies)
+            if (!cstart) {
+                // mid-chunk: the current chunk's carries become entry 0
+                if (cwarp) {
 #pragma unroll
-            for (int u = 0; u < CPL; ++u) {
-                const int c = lane + 32 * u;
-                if (c < NC) {
-                    myF[(size_t)nhist * NC + c] = F[u];
-                    myG[(size_t)nhist * NC + c] = G[u];
-                    myFf[(size_t)nhist * NC + c] = (float)F[u];
-                    myGf[(size_t)nhist * NC + c] = (float)G[u];
+                    for (int u = 0; u < CPL; ++u) {
+                        const int c = lane + 32 * u;
+                        if (c < NC) {
+                            myFh[c] = myFh[(size_t)cur * NCS + c];
+                            myFl[c] = myFl[(size_t)cur * NCS + c];
+                            myGh[c] = myGh[(size_t)cur * NCS + c];
+                            myGl[c] = myGl[(size_t)cur * NCS + c];
+                        }
+                    }
+                    if (lane == 0) {
+                        myK[0] = myK[2 * cur];
+                        myK[1] = myK[2 * cur + 1];
+                    }
                 }
-                if (c == cb) {
-                    myK[nhist] = K;
+                if (threadIdx.x == 0) {
+                    hXb[0] = hXb[cur];
+                }
+                cur = 0;
+                nhist = 1;
+                __syncthreads();
+            }
+        }
+        if (cstart) {
+            cur = nhist++;
+            if (cwarp) {
+                // carries at the start of this chunk
+#pragma unroll
+                for (int u = 0; u < CPL; ++u) {
+                    const int c = lane + 32 * u;
+                    if (c < NC) {
+                        myFh[(size_t)cur * NCS + c] = Fh[u];
+                        myFl[(size_t)cur * NCS + c] = Fl[u];
+                        myGh[(size_t)cur * NCS + c] = Gh[u];
+                        myGl[(size_t)cur * NCS + c] = Gl[u];
+                    }
+                    if (c == cb) {
+                        myK[2 * cur] = Kh;
+                        myK[2 * cur + 1] = Kl;
+                    }
                 }
             }
+            xbase = sq == 0 ? xr[1] : xr[0];
+            if (threadIdx.x == 0) {
+                hXb[cur] = xbase;
+            }
+        }
+        if (cwarp) {
             const float *rw = sraw4 + (size_t)sg * RAW;
             const float *bw = rw + warp * FS_ROWS;
             const float *dv = dsm + h * FS_ROWS;
             const float *rowb = sbo + (size_t)sg * FS_ROWS * MP;
             long ng = next_grid;
             int slot = nsnap;
-            // Per lane, where its x comes from: the Bo row (c < m) or one of the
-            // per-row candidate arrays (candidate column, y, parent); the same
-            // address arithmetic for every row, no per-row selects.
-            int xoff[CPL];
-            bool xrow[CPL];
+            // Per lane, where its x comes from: the Bo row (c < m, stride MP) or
+            // one of the per-row candidate arrays (candidate column, y, parent;
+            // stride 1); lanes past the components read the zero delta of the
+            // stage's first row with stride 0. One load per row and component.
+            const float *xsrc[CPL];
+            int xstr[CPL];
 #pragma unroll
             for (int u = 0; u < CPL; ++u) {
                 const int c = lane + 32 * u;
-                xrow[u] = c < m;
-                xoff[u] = c < m ? c
-                                : c == m ? (W + warp) * FS_ROWS
-                                         : c == m + 1 ? 2 * W * FS_ROWS : warp * FS_ROWS;
+                xsrc[u] = c < m ? rowb + c
+                                : c == m ? rw + (W + warp) * FS_ROWS
+                                         : c == m + 1 ? rw + 2 * W * FS_ROWS
+                                                      : c == m + 2 ? rw + warp * FS_ROWS : zero;
+                xstr[u] = c < m ? MP : c < NC ? 1 : 0;
             }
             int r = 0;
             while (r < rows) {
@@ -577,21 +698,23 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
 #pragma unroll 4
                 for (; r < rend; ++r) {
                     const float bk = bw[r], d = dv[r];
-                    const float *rowp = rowb + r * MP;
 #pragma unroll
                     for (int u = 0; u < CPL; ++u) {
                         const int c = lane + 32 * u;
-                        const float xv = xrow[u] ? rowp[xoff[u]] : (c < NC ? rw[xoff[u] + r] : 0.f);
-                        const float klc = fmaf(d * d, q[u], fmaf(2.0f * d, e[u], kl));
+                        const float xv = xsrc[u][r * xstr[u]];
+                        const float klc = kl + fmaf(d * d, qh[u], 2.0f * d * e[u]);
                         kl = c == cb ? klc : kl;
-                        e[u] = fmaf(d, q[u], e[u]);
-                        q[u] = fmaf(bk, xv, q[u]);
+                        e[u] = fmaf(d, qh[u], e[u]);
+                        float t, err;
+                        two_sum(qh[u], __fmul_rn(bk, xv), t, err);
+                        ql[u] = __fadd_rn(ql[u], err);
+                        qh[u] = t;
                     }
                 }
                 if (grid_here) {
                     const int rg = rend - 1;
                     ng += min_span;
-                    float *es = myE + (size_t)slot * NC;
+                    float *es = myE + (size_t)slot * NCS;
 #pragma unroll
                     for (int u = 0; u < CPL; ++u) {
                         const int c = lane + 32 * u;
@@ -604,27 +727,41 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
                     }
                     if (lane == 0 && warp == 0) {
                         srow[slot] = idx(s0 + rg);
-                        sCh[slot] = nhist;
-                        sD[slot] = dpre[h * FS_ROWS + rg];
-                        sXv[slot] = rw[(2 * W + 1) * FS_ROWS + 1 + rg];
+                        sCh[slot] = cur;
+                        sXv[slot] = xr[1 + rg];
                     }
                     ++slot;
                 }
             }
-            // carry to the next chunk start (f64)
-            const double Dc = dpre[h * FS_ROWS + rows - 1];
-#pragma unroll
-            for (int u = 0; u < CPL; ++u) {
-                const int c = lane + 32 * u;
-                if (c == cb) {
-                    K = K + Dc * (2.0 * F[u] + Dc * G[u]) + (double)kl;
+            if (cend) {
+                // carry to the next chunk: Dc = x_base - x_end exactly
+                float Dh, Dl;
+                two_sum(xbase, -xr[rows], Dh, Dl);
+                if (rev) {
+                    Dh = -Dh;
+                    Dl = -Dl;
                 }
-                F[u] = fma(G[u], Dc, F[u]) + (double)e[u];
-                G[u] = G[u] + (double)q[u];
-                e[u] = 0.f;
-                q[u] = 0.f;
+#pragma unroll
+                for (int u = 0; u < CPL; ++u) {
+                    const int c = lane + 32 * u;
+                    float th, tl;
+                    if (c == cb) {
+                        // K += Dc (2 F_b + G_b Dc) + kl, with the chunk-start F_b, G_b
+                        ff_mul(Gh[u], Gl[u], Dh, Dl, th, tl);
+                        ff_add(th, tl, 2.0f * Fh[u], 2.0f * Fl[u]);
+                        float vh, vl;
+                        ff_mul(th, tl, Dh, Dl, vh, vl);
+                        ff_add(Kh, Kl, vh, vl);
+                        ff_add(Kh, Kl, kl, 0.0f);
+                    }
+                    ff_mul(Gh[u], Gl[u], Dh, Dl, th, tl);
+                    ff_add(Fh[u], Fl[u], th, tl);
+                    ff_add(Fh[u], Fl[u], e[u], 0.0f);
+                    ff_add(Gh[u], Gl[u], qh[u], ql[u]);
+                    qh[u] = ql[u] = e[u] = 0.f;
+                }
+                kl = 0.f;
             }
-            kl = 0.f;
         } else if (lwarp) {
             if (sq + S - 1 < nstages) {
                 issue_bo(sq + S - 1);
@@ -644,7 +781,6 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
             }
         }
         nsnap += gcount;
-        nhist += 1;
         next_grid += (long)gcount * min_span;
         __syncthreads();
     }
@@ -653,7 +789,7 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
     }
     flagged = __any_sync(0xffffffffu, flagged);
     if (cwarp && lane == 0) {
-        hsse[(size_t)mycand * 2 + task.dir] = best;
+        hsse[(size_t)mycand * 2 + task.dir] = (double)best;
         hrow[(size_t)mycand * 2 + task.dir] = besti >= 0 ? pk[besti] : -1;
         hflag[(size_t)mycand * 2 + task.dir] = flagged;
     }
@@ -723,10 +859,14 @@ void fast_project(cudaStream_t st, const FillSrc &src, const float *BoC, int n, 
 
 static size_t fast_sweep_smem(int m, int w, int stages) { return FastSweepSmem(m, w, stages).total; }
 
+// Two blocks per SM when their shared memory allows (the kernel is bounded to
+// 96 registers for that); fewer candidate warps per block when the tasks are few.
+constexpr size_t FS_SMEM_2 = 113 * 1024;
+
 int fast_sweep_warps(int m, int candidates)
 {
     int w = candidates <= 4 * 152 ? 4 : FS_MAXW;
-    while (w > 1 && fast_sweep_smem(m, w, 2) > 200 * 1024) {
+    while (w > 1 && fast_sweep_smem(m, w, 2) > FS_SMEM_2) {
         --w;
     }
     return w;
@@ -744,7 +884,7 @@ void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int
     }
     const int warps = warps_per_block;
     verify(warps >= 1 && warps <= FS_MAXW, "sweep block size out of range", 2);
-    const int stages = fast_sweep_smem(m, warps, 4) <= 200 * 1024 ? 4 : 2;
+    const int stages = fast_sweep_smem(m, warps, 4) <= FS_SMEM_2 ? 4 : 2;
     const size_t smem = fast_sweep_smem(m, warps, stages);
     verify(smem <= 227 * 1024, "too many basis functions for the fast hinge sweep");
     const int nc = m + 3;

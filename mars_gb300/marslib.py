@@ -42,6 +42,13 @@ class Stats(ctypes.Structure):
         ("ms_sort", ctypes.c_double),
         ("ms_append", ctypes.c_double),
         ("ms_redecide", ctypes.c_double),
+        ("ms_gather", ctypes.c_double),
+        ("ms_redecide_gpu", ctypes.c_double),
+        ("redecided_flagged", ctypes.c_longlong),
+        ("speculated", ctypes.c_longlong),
+        ("redecided_spec", ctypes.c_longlong),
+        ("leftovers", ctypes.c_longlong),
+        ("leftovers_flagged", ctypes.c_longlong),
     ]
 
     def as_dict(self):
