@@ -121,49 +121,66 @@ struct PhaseTimer {
 // own, or the speculative re-decision's (SpecLane), which runs beside the fast
 // pass of the mixed mode.
 struct Fp64Ctx {
-    cudaStream_t st, st2;
-    cudaEvent_t ev_fork, ev_join;
+    cudaStream_t st, st2, st3;
+    cudaEvent_t ev_fork, ev_join, ev_s, ev_ybx;
     PhaseTimer *timer;
     mars_gpu_stats *stats;
     DevBuf *Bx, *T, *svec, *snew, *ybx, *hsse, *hrow, *fired, *nfired, *tasks, *stasks, *scal,
-        *bsort, *bxsort, *cand;
+        *bsort, *bxsort, *cand, *part;
+};
+
+// Streams and events of one FP64 context: the main stream, the side stream of
+// the hinge scalars and the one of the ybx chain, with their fork/join events.
+struct Fp64Streams {
+    cudaStream_t st = nullptr, st2 = nullptr, st3 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_s = nullptr, ev_ybx = nullptr;
+    void create()
+    {
+        CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        CUDA_CHECK(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+        CUDA_CHECK(cudaStreamCreateWithFlags(&st3, cudaStreamNonBlocking));
+        CUDA_CHECK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        CUDA_CHECK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+        CUDA_CHECK(cudaEventCreateWithFlags(&ev_s, cudaEventDisableTiming));
+        CUDA_CHECK(cudaEventCreateWithFlags(&ev_ybx, cudaEventDisableTiming));
+    }
+    ~Fp64Streams()
+    {
+        for (cudaStream_t x : {st, st2, st3}) {
+            if (x) {
+                cudaStreamSynchronize(x);
+                cudaStreamDestroy(x);
+            }
+        }
+        for (cudaEvent_t e : {ev_fork, ev_join, ev_s, ev_ybx}) {
+            if (e) {
+                cudaEventDestroy(e);
+            }
+        }
+    }
 };
 
 struct SpecLane {
-    cudaStream_t st = nullptr, st2 = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    Fp64Streams ss;
     PhaseTimer timer;
     double phase_ms[PH_N] = {0};
     mars_gpu_stats stats{};
     DevBuf Bx, T, svec, snew, ybx, hsse, hrow, fired, nfired, tasks, stasks, scal, bsort, bxsort,
-        cand;
+        cand, part;
     void init()
     {
-        if (!st) {
-            CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-            CUDA_CHECK(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
-            CUDA_CHECK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-            CUDA_CHECK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-            timer.st = st;
+        if (!ss.st) {
+            ss.create();
+            timer.st = ss.st;
             timer.redirect = PH_REDECIDE_GPU;
         }
     }
     Fp64Ctx ctx()
     {
-        return {st,   st2,     ev_fork, ev_join, &timer, &stats,  &Bx,    &T,     &svec,   &snew,
-                &ybx, &hsse,   &hrow,   &fired,  &nfired, &tasks, &stasks, &scal, &bsort, &bxsort,
-                &cand};
-    }
-    ~SpecLane()
-    {
-        if (st) {
-            cudaStreamSynchronize(st);
-            cudaStreamSynchronize(st2);
-            cudaStreamDestroy(st);
-            cudaStreamDestroy(st2);
-            cudaEventDestroy(ev_fork);
-            cudaEventDestroy(ev_join);
-        }
+        return {ss.st,  ss.st2, ss.st3, ss.ev_fork, ss.ev_join, ss.ev_s, ss.ev_ybx,
+                &timer, &stats, &Bx,    &T,         &svec,      &snew,   &ybx,
+                &hsse,  &hrow,  &fired, &nfired,    &tasks,     &stasks, &scal,
+                &bsort, &bxsort, &cand, &part};
     }
 };
 
@@ -174,11 +191,11 @@ struct mars_gpu_algo {
     double tol = 0, yvar = 0;
     int precision = MARS_GPU_PREC_FP64;
     std::vector<double> ybo;
+    // The handle's stream (st), with side streams for the hinge-sweep scalar
+    // recurrences, which run concurrently with the projection, and for the
+    // ybx chain, which runs concurrently with the sweep (fork/join events).
+    Fp64Streams ss;
     cudaStream_t st = nullptr;
-    // Side stream for the hinge-sweep scalar recurrences, which run
-    // concurrently with the projection (fork/join events below).
-    cudaStream_t st2 = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     PhaseTimer timer;
     double phase_ms[PH_N] = {0};
     cudaEvent_t span_begin = nullptr, span_end = nullptr;
@@ -192,7 +209,7 @@ struct mars_gpu_algo {
     std::vector<int32_t> perm_h;  // host copy of the sorted permutations (exact re-decision)
     std::vector<char> sorted;
     // Per-eval scratch (grow-only).
-    DevBuf Bx, T, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks, stasks, scal;
+    DevBuf Bx, T, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks, stasks, scal, part;
     DevBuf bsort, bxsort;  // per candidate: parent and normalised column in sorted order
     DevBuf fTp, fT, fmom, hflag;  // fast pass: split-K partials, T, parent moments, sweep flags
     DevBuf sort_keys, sort_vals, sort_tmp;
@@ -204,27 +221,14 @@ struct mars_gpu_algo {
 
     Fp64Ctx ctx()
     {
-        return {st,   st2,   ev_fork, ev_join, &timer, &stats,  &Bx,    &T,     &svec,   &snew,
-                &ybx, &hsse, &hrow,   &fired,  &nfired, &tasks, &stasks, &scal, &bsort, &bxsort,
-                &cand};
+        return {ss.st,  ss.st2, ss.st3, ss.ev_fork, ss.ev_join, ss.ev_s, ss.ev_ybx,
+                &timer, &stats, &Bx,    &T,         &svec,      &snew,   &ybx,
+                &hsse,  &hrow,  &fired, &nfired,    &tasks,     &stasks, &scal,
+                &bsort, &bxsort, &cand, &part};
     }
 
     ~mars_gpu_algo()
     {
-        if (st) {
-            cudaStreamSynchronize(st);
-            cudaStreamDestroy(st);
-        }
-        if (st2) {
-            cudaStreamSynchronize(st2);
-            cudaStreamDestroy(st2);
-        }
-        if (ev_fork) {
-            cudaEventDestroy(ev_fork);
-        }
-        if (ev_join) {
-            cudaEventDestroy(ev_join);
-        }
         if (span_begin) {
             cudaEventDestroy(span_begin);
         }
@@ -285,10 +289,8 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     a->yvar = a->hb.yvar;
     a->ybo = a->hb.ybo;
     std::memset(&a->stats, 0, sizeof(a->stats));
-    CUDA_CHECK(cudaStreamCreateWithFlags(&a->st, cudaStreamNonBlocking));
-    CUDA_CHECK(cudaStreamCreateWithFlags(&a->st2, cudaStreamNonBlocking));
-    CUDA_CHECK(cudaEventCreateWithFlags(&a->ev_fork, cudaEventDisableTiming));
-    CUDA_CHECK(cudaEventCreateWithFlags(&a->ev_join, cudaEventDisableTiming));
+    a->ss.create();
+    a->st = a->ss.st;
     CUDA_CHECK(cudaEventCreate(&a->span_begin));
     CUDA_CHECK(cudaEventCreate(&a->span_end));
     a->timer.st = a->st;
@@ -462,9 +464,17 @@ void eval_block_fp64(mars_gpu_algo *a, Fp64Ctx &c, int Pc, const int *cx_d, cons
     c.timer->end(PH_DGKS, t0);
 
     t0 = c.timer->begin();
-    normalize_ybx(c.st, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), false,
-                  c.ybx->as<double>(), &c.stats->kernel_launches);
-    if (!linear_only) {
+    if (linear_only) {
+        normalize_ybx(c.st, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), false,
+                      c.ybx->as<double>(), &c.stats->kernel_launches);
+    } else {
+        // The ybx chain on its own stream: the sweep stores the partial scores
+        // and sweep_score finishes them once ybx is known.
+        CUDA_CHECK(cudaEventRecord(c.ev_s, c.st));
+        CUDA_CHECK(cudaStreamWaitEvent(c.st3, c.ev_s, 0));
+        normalize_ybx(c.st3, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), false,
+                      c.ybx->as<double>(), &c.stats->kernel_launches);
+        CUDA_CHECK(cudaEventRecord(c.ev_ybx, c.st3));
         gather_candidates(c.st, a->perm.as<int>(), Bx, a->n, cx_d, s, a->tol, n, tail, Pc,
                           c.bxsort->as<float>(), &c.stats->kernel_launches);
     }
@@ -498,7 +508,11 @@ void eval_block_fp64(mars_gpu_algo *a, Fp64Ctx &c, int Pc, const int *cx_d, cons
                a->xsort.as<float>(), c.bsort->as<float>(), c.bxsort->as<float>(),
                a->Bo.as<double>(), a->ldbo, a->ybo_d.as<double>(), c.ybx->as<double>(),
                c.scal->as<double>(), n, m, head, tail, min_span, a->tol, c.hsse->as<double>(),
-               c.hrow->as<int>(), warps, &c.stats->kernel_launches);
+               c.hrow->as<int>(), warps, &c.stats->kernel_launches, c.part->as<double>());
+    CUDA_CHECK(cudaStreamWaitEvent(c.st, c.ev_ybx, 0));
+    sweep_score(c.st, c.part->as<double>(), Pc, cx_d, a->perm.as<int>(), c.ybx->as<double>(), n,
+                head, tail, min_span, a->tol, c.hsse->as<double>(), c.hrow->as<int>(),
+                &c.stats->kernel_launches);
     c.timer->end(PH_SWEEP, t0);
     if (count_work) {
         c.stats->knot_evals += (long long)Pc * sweep_grid_rows(head, tail, min_span);
@@ -528,21 +542,24 @@ void run_spec(mars_gpu_algo *a, const std::vector<int> &sx, const std::vector<in
     L.nfired.ensure(sizeof(int) * 4);
     L.scal.ensure(sizeof(double) * 3 *
                   std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
+    L.part.ensure(sizeof(double) * 4 *
+                  std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
     int *ecx = L.cand.as<int>(), *ecb = ecx + C;
-    CUDA_CHECK(cudaMemcpyAsync(ecx, sx.data(), sizeof(int) * C, cudaMemcpyHostToDevice, L.st));
-    CUDA_CHECK(cudaMemcpyAsync(ecb, sb.data(), sizeof(int) * C, cudaMemcpyHostToDevice, L.st));
+    const cudaStream_t st = L.ss.st;
+    CUDA_CHECK(cudaMemcpyAsync(ecx, sx.data(), sizeof(int) * C, cudaMemcpyHostToDevice, st));
+    CUDA_CHECK(cudaMemcpyAsync(ecb, sb.data(), sizeof(int) * C, cudaMemcpyHostToDevice, st));
     L.stats.h2d_bytes += (long long)(sizeof(int) * 2 * (size_t)C);
     eval_block_fp64(a, c, C, ecx, ecb, sx, 0, min_span, head, tail, false, false);
     std::vector<double> ybx(C), hs(C);
     std::vector<int> hr(C);
     CUDA_CHECK(cudaMemcpyAsync(ybx.data(), L.ybx.ptr, sizeof(double) * C, cudaMemcpyDeviceToHost,
-                               L.st));
+                               st));
     CUDA_CHECK(cudaMemcpyAsync(hs.data(), L.hsse.ptr, sizeof(double) * C, cudaMemcpyDeviceToHost,
-                               L.st));
+                               st));
     CUDA_CHECK(cudaMemcpyAsync(hr.data(), L.hrow.ptr, sizeof(int) * C, cudaMemcpyDeviceToHost,
-                               L.st));
+                               st));
     L.stats.d2h_bytes += (long long)(20 * (size_t)C);
-    CUDA_CHECK(cudaStreamSynchronize(L.st));
+    CUDA_CHECK(cudaStreamSynchronize(st));
     L.timer.resolve(L.phase_ms);
     out.resize(C);
     for (int q = 0; q < C; ++q) {
@@ -916,6 +933,8 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         if (!linear_only) {
             a->scal.ensure(sizeof(double) * 3 *
                            std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
+            a->part.ensure(sizeof(double) * 4 *
+                           std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
         }
         int *ecx = a->cand.as<int>(), *ecb = ecx + C;
         CUDA_CHECK(cudaMemcpyAsync(ecx, lo_x.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
@@ -1060,7 +1079,7 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         const double ngrid = linear_only ? 0.0 : (double)sweep_grid_rows(head, tail, min_span);
         const double sorted_b = linear_only ? 0.0 : 8.0 * n;  // bsort + bxsort
         size_t cap = (size_t)std::max(
-            1.0, budget / (4.0 * n + sorted_b + 24.0 * ngrid + 64.0 * m + 64.0));
+            1.0, budget / (4.0 * n + sorted_b + 56.0 * ngrid + 64.0 * m + 64.0));
         cap = std::min<size_t>(cap, 262144);
         const auto blocks = block_candidates(cx, cap);
         size_t maxPc = 0;
@@ -1076,6 +1095,8 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         a->hrow.ensure(sizeof(int) * maxPc);
         if (!linear_only) {
             a->scal.ensure(sizeof(double) * 3 *
+                           std::max<size_t>(1, maxPc * (size_t)sweep_grid_rows(head, tail, min_span)));
+            a->part.ensure(sizeof(double) * 4 *
                            std::max<size_t>(1, maxPc * (size_t)sweep_grid_rows(head, tail, min_span)));
             a->bsort.ensure(sizeof(float) * a->n * maxPc);
             a->bxsort.ensure(sizeof(float) * a->n * maxPc);

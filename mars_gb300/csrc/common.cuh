@@ -23,6 +23,22 @@ inline void cuda_check(cudaError_t e, const char *what, const char *file, int li
 #define CUDA_CHECK(x) ::mgpu::cuda_check((x), #x, __FILE__, __LINE__)
 #define LAUNCH_CHECK() ::mgpu::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
 
+// Allows a kernel the device's whole opt-in dynamic shared memory. The
+// attribute is per kernel and process-wide: setting it to each launch's own
+// size would race with concurrent handles launching the same kernel with
+// another size, so every caller sets the same (largest) value.
+template <class K>
+void allow_max_smem(K kernel)
+{
+    int dev = 0, v = 0;
+    CUDA_CHECK(cudaGetDevice(&dev));
+    CUDA_CHECK(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    CUDA_CHECK(cudaFuncGetAttributes(&fa, kernel));  // less the kernel's static shared memory
+    CUDA_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    v - (int)fa.sharedSizeBytes));
+}
+
 inline size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
 inline size_t round_up(size_t a, size_t b) { return ceil_div(a, b) * b; }
 

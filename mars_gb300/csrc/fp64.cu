@@ -447,7 +447,8 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
             const float *__restrict__ bxs, const double *__restrict__ Bo, size_t ldbo,
             const double *__restrict__ ybo, const double *__restrict__ ybx,
             const double *__restrict__ scal, int ngrid, int n, int m, int head, int tail,
-            int min_span, double tol, double *__restrict__ hsse, int *__restrict__ hrow)
+            int min_span, double tol, double *__restrict__ hsse, int *__restrict__ hrow,
+            double *__restrict__ part)
 {
     extern __shared__ __align__(16) unsigned char sraw[];
     const int W = (blockDim.x >> 5) - 1;  // candidate warps
@@ -527,7 +528,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
     };
 
     const int mycand = task.cand0 + (cwarp ? warp : 0);
-    const double ybx_c = ybx[mycand];
+    const double ybx_c = part ? 0.0 : ybx[mycand];
     const double *mysc = scal + (size_t)mycand * ngrid * 3;
     double *snap = snapbase + (size_t)(cwarp ? warp : 0) * SW_SNAP * ldF;
     double f[CPL], g[CPL];
@@ -556,10 +557,19 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
                     fy = fma(fs[c], sybo[c], fy);
                 }
                 ff = fma(fs[m], fs[m], ff);
-                fy = fma(fs[m], ybx_c, fy);
-                const double uw = fy - w;
                 const double den = (k0 + k1) - ff;
-                sse = den > tol ? (uw * uw) / (den + tol) : 0.0;
+                if (part) {
+                    double *o = part + ((size_t)mycand * ngrid +
+                                        (size_t)((row - (head + 1)) / min_span)) * 4;
+                    o[0] = fy;
+                    o[1] = fs[m];
+                    o[2] = w;
+                    o[3] = den;
+                } else {
+                    fy = fma(fs[m], ybx_c, fy);
+                    const double uw = fy - w;
+                    sse = den > tol ? (uw * uw) / (den + tol) : 0.0;
+                }
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -662,9 +672,69 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
     if (nsnap > 0) {
         flush();
     }
-    if (cwarp && lane == 0) {
+    if (cwarp && lane == 0 && !part) {
         hsse[mycand] = best;
         hrow[mycand] = besti >= 0 ? pk[besti] : -1;
+    }
+}
+
+constexpr int SS_THREADS = 256;
+
+__global__ void __launch_bounds__(SS_THREADS)
+    k_sweep_score(const double *__restrict__ part, int ngrid, const int *__restrict__ cand_x,
+                  const int *__restrict__ perm, const double *__restrict__ ybx, int n, int head,
+                  int min_span, double tol, double *__restrict__ hsse, int *__restrict__ hrow)
+{
+    __shared__ double rs[SS_THREADS / 32];
+    __shared__ int rg[SS_THREADS / 32];
+    const int j = blockIdx.x;
+    const double yb = ybx[j];
+    const double *pj = part + (size_t)j * ngrid * 4;
+    double best = -1.0;
+    int bg = 0x7fffffff;
+    for (int g = threadIdx.x; g < ngrid; g += SS_THREADS) {
+        const double *q = pj + (size_t)g * 4;
+        const double fy = fma(q[1], yb, q[0]);
+        const double uw = fy - q[2];
+        const double den = q[3];
+        const double sse = den > tol ? (uw * uw) / (den + tol) : 0.0;
+        if (sse > best) {  // g increases along a thread's loop: ties keep the first
+            best = sse;
+            bg = g;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double s2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const int g2 = __shfl_xor_sync(0xffffffffu, bg, o);
+        if (s2 > best || (s2 == best && g2 < bg)) {
+            best = s2;
+            bg = g2;
+        }
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        rs[warp] = best;
+        rg[warp] = bg;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        best = rs[0];
+        bg = rg[0];
+        for (int w = 1; w < SS_THREADS / 32; ++w) {
+            if (rs[w] > best || (rs[w] == best && rg[w] < bg)) {
+                best = rs[w];
+                bg = rg[w];
+            }
+        }
+        // the reference keeps the first strictly positive maximum
+        if (best > 0.0) {
+            hsse[j] = best;
+            hrow[j] = perm[(size_t)cand_x[j] * n + head + 1 + (size_t)bg * min_span];
+        } else {
+            hsse[j] = 0.0;
+            hrow[j] = -1;
+        }
     }
 }
 
@@ -1116,9 +1186,7 @@ void tgemm_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, int
     case K: {                                                                                \
         const size_t smem = TgemmSmem<BoT, K, Src::kRaw>::total;                             \
         if (smem > 48 * 1024) {                                                              \
-            CUDA_CHECK(cudaFuncSetAttribute(k_tgemm<Src, BoT, K>,                            \
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,     \
-                                            (int)smem));                                     \
+            allow_max_smem(k_tgemm<Src, BoT, K>);                                            \
         }                                                                                    \
         k_tgemm<Src, BoT, K><<<dim3(gx, gy), TG_THREADS, smem, st>>>(src, Bo, ldbo, n, m, P, T); \
         break;                                                                               \
@@ -1166,8 +1234,7 @@ void project_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, i
     const int rb = (int)ceil_div(n, PJ_THREADS);
     const size_t smem = sizeof(double) * PJ_COLS * std::max(m, 1);
     if (smem > 48 * 1024) {
-        CUDA_CHECK(cudaFuncSetAttribute(k_project<Src, BoT>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_max_smem(k_project<Src, BoT>);
     }
     verify(ceil_div(P, PJ_COLS) <= 65535, "too many candidate columns for one launch", 2);
     k_project<Src, BoT><<<dim3(rb, (unsigned)ceil_div(P, PJ_COLS)), PJ_THREADS, smem, st>>>(
@@ -1302,7 +1369,7 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
                 const float *xsort, const float *bs, const float *bxs, const double *Bo,
                 size_t ldbo, const double *ybo, const double *ybx, const double *scal, int n,
                 int m, int head, int tail, int min_span, double tol, double *hsse, int *hrow,
-                int warps_per_block, long long *launches)
+                int warps_per_block, long long *launches, double *part)
 {
     if (ntasks <= 0) {
         return;
@@ -1323,12 +1390,10 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
     const int comps = m + 1;
 #define LAUNCH_SWEEP(CPL, S)                                                                   \
     do {                                                                                       \
-        CUDA_CHECK(cudaFuncSetAttribute(k_sweep<CPL, S>,                                       \
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,           \
-                                        (int)smem));                                           \
+        allow_max_smem(k_sweep<CPL, S>);                                                       \
         k_sweep<CPL, S><<<ntasks, 32 * (warps + 1), smem, st>>>(                               \
             tasks, perm, xsort, bs, bxs, Bo, ldbo, ybo, ybx, scal, ngrid, n, m, head, tail,    \
-            min_span, tol, hsse, hrow);                                                        \
+            min_span, tol, hsse, hrow, part);                                                  \
     } while (0)
 #define LAUNCH_CPL(CPL)            \
     do {                           \
@@ -1351,6 +1416,20 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
     }
 #undef LAUNCH_CPL
 #undef LAUNCH_SWEEP
+    LAUNCH_CHECK();
+    *launches += 1;
+}
+
+void sweep_score(cudaStream_t st, const double *part, int P, const int *cand_x,
+                 const int *perm, const double *ybx, int n, int head, int tail, int min_span,
+                 double tol, double *hsse, int *hrow, long long *launches)
+{
+    if (P <= 0) {
+        return;
+    }
+    const int ngrid = sweep_grid_rows(head, tail, min_span);
+    k_sweep_score<<<P, SS_THREADS, 0, st>>>(part, ngrid, cand_x, perm, ybx, n, head, min_span,
+                                            tol, hsse, hrow);
     LAUNCH_CHECK();
     *launches += 1;
 }

@@ -122,11 +122,24 @@ void hinge_scalars(cudaStream_t st, const SweepTask *tasks, int ntasks, const fl
 
 // Hinge sweep in FP64 (marsalgo.cc:508-657), one warp per candidate; tasks
 // hold at most sweep_warps(m) candidates; scal from hinge_scalars.
+// With part == nullptr it scores the cuts with ybx and writes hsse/hrow.
+// Otherwise ybx is not read: per candidate j and grid row g it stores
+// part[(j * ngrid + g) * 4 + {0..3}] = {fy before its last step (the
+// candidate component's), f_m, w, den}, and sweep_score finishes the scores
+// once ybx is known -- so the sweep need not wait for the ybx chain.
 void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *perm,
                 const float *xsort, const float *bs, const float *bxs, const double *Bo,
                 size_t ldbo, const double *ybo, const double *ybx, const double *scal, int n,
                 int m, int head, int tail, int min_span, double tol, double *hsse, int *hrow,
-                int warps_per_block, long long *launches);
+                int warps_per_block, long long *launches, double *part = nullptr);
+
+// The scores of the deferred sweep (the reference's: fy = fy_partial + f_m ybx
+// as the chain's last fused step, uw = fy - w, sse = den > tol ? uw^2 / (den +
+// tol) : 0) and the first maximum in row order, for candidates j < P (input
+// cand_x[j]).
+void sweep_score(cudaStream_t st, const double *part, int P, const int *cand_x,
+                 const int *perm, const double *ybx, int n, int head, int tail, int min_span,
+                 double tol, double *hsse, int *hrow, long long *launches);
 
 // Stable descending argsort of X columns (marsalgo.cc:33-39), the scaled
 // sorted values xsort[i] = X[perm[i]] * s and the sorted target ysort[i] = y[perm[i]].
