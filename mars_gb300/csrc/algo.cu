@@ -711,7 +711,16 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
             a->timer.end(PH_GATHER, t0);
             t0 = a->timer.begin();
             std::vector<FastTaskRec> tasks;
-            const int warps = fast_sweep_warps(m, 2 * Pc);
+            std::vector<int> groups;
+            for (int q = 0; q < Pc;) {
+                int e = q;
+                while (e < Pc && cx[c0 + e] == cx[c0 + q]) {
+                    ++e;
+                }
+                groups.push_back(e - q);
+                q = e;
+            }
+            const int warps = fast_sweep_warps(m, groups);
             for (int q = 0; q < Pc;) {
                 int e = q;
                 while (e < Pc && cx[c0 + e] == cx[c0 + q]) {

@@ -235,6 +235,7 @@ __global__ void __launch_bounds__(256) k_parent_moments(FillSrc src, int n, doub
 // Fe = sum F_c e_c, Ge = sum G_c e_c, ee = sum e_c^2, ey = sum yc_c e_c.
 // ---------------------------------------------------------------------------
 constexpr int FS_ROWS = 32, FS_CHUNK = 2, FS_SNAP = 32, FS_HIST = 6, FS_NSUM = 5, FS_MAXW = 8;
+constexpr int FS_RS = FS_ROWS + 1;  // stride of the staged per-row arrays: each in its own banks
 
 using FastTask = FastTaskRec;  // dir 0: forward (first half of the cuts), 1: mirror (second half)
 
@@ -321,8 +322,8 @@ struct FastSweepSmem {
         o = (o + 15) / 16 * 16;  // 16-byte cp.async destinations
         bo = o;  // [S][FS_ROWS][mp] f32, row stride mp = m rounded up to 4
         o += 4 * (size_t)S * FS_ROWS * ((m + 3) / 4 * 4);
-        raw = o;  // [S][(2W + 1) * FS_ROWS + FS_ROWS + 1] f32: B, Bx per candidate, y, x
-        o += 4 * (size_t)S * ((2 * W + 1) * FS_ROWS + FS_ROWS + 1);
+        raw = o;  // [S][(2W + 1) * FS_RS + FS_ROWS + 1] f32: B, Bx per candidate, y, x
+        o += 4 * (size_t)S * ((2 * W + 1) * FS_RS + FS_ROWS + 1);
         dsm = o;  // [2][FS_ROWS] f32 deltas
         o += 4 * 2 * FS_ROWS;
         zero = o;  // one f32 zero
@@ -346,7 +347,7 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
     const int NC = m + 3;  // basis columns, candidate, y, b
     const int NCS = NC | 1;
     const int U = (m + 3) / 4, MP = 4 * U;  // 16-byte units per Bo row, padded row stride
-    const int RAW = (2 * W + 1) * FS_ROWS + FS_ROWS + 1;
+    const int RAW = (2 * W + 1) * FS_RS + FS_ROWS + 1;
     const FastSweepSmem L(m, W, S);
     float *hFh = reinterpret_cast<float *>(sm + L.hFh);
     float *hFl = reinterpret_cast<float *>(sm + L.hFl);
@@ -397,13 +398,13 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
     const long g_last = tail - 1 >= head + 1
                             ? (long)head + 1 + (long)((tail - 1 - (head + 1)) / min_span) * min_span
                             : -1;
-    long next_grid, last_step;  // in processing steps
+    int next_grid, last_step;  // in processing steps
     if (!rev) {
-        next_grid = (long)head + 1;
-        last_step = g_last < 0 ? -1 : (g_last < (long)mid ? g_last : (long)mid);
+        next_grid = head + 1;
+        last_step = g_last < 0 ? -1 : (int)(g_last < (long)mid ? g_last : (long)mid);
     } else {
-        next_grid = g_last < 0 ? (long)len : (long)n - 1 - g_last;  // largest grid row first
-        last_step = g_last < 0 ? -1 : (long)n - 1 - (mid + 1);
+        next_grid = g_last < 0 ? len : (int)((long)n - 1 - g_last);  // largest grid row first
+        last_step = g_last < 0 ? -1 : n - 1 - (mid + 1);
     }
     const int nstages = (len + FS_ROWS - 1) / FS_ROWS;
 
@@ -434,19 +435,19 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
         const bool ok = lane < rows;
         const int i = ok ? idx(s0 + lane) : 0;
         for (int cw = 0; cw < task.count; ++cw) {
-            cp_async4(rw + cw * FS_ROWS + lane, bsb + (size_t)cw * n + i, ok);
-            cp_async4(rw + (W + cw) * FS_ROWS + lane, bxb + (size_t)cw * n + i, ok);
+            cp_async4(rw + cw * FS_RS + lane, bsb + (size_t)cw * n + i, ok);
+            cp_async4(rw + (W + cw) * FS_RS + lane, bxb + (size_t)cw * n + i, ok);
         }
-        cp_async4(rw + 2 * W * FS_ROWS + lane, ys + i, ok);
-        cp_async4(rw + (2 * W + 1) * FS_ROWS + 1 + lane, xs + i, ok);
+        cp_async4(rw + 2 * W * FS_RS + lane, ys + i, ok);
+        cp_async4(rw + (2 * W + 1) * FS_RS + 1 + lane, xs + i, ok);
         if (lane == 0) {
-            cp_async4(rw + (2 * W + 1) * FS_ROWS, xs + (s0 > 0 ? idx(s0 - 1) : 0), s0 > 0);
+            cp_async4(rw + (2 * W + 1) * FS_RS, xs + (s0 > 0 ? idx(s0 - 1) : 0), s0 > 0);
         }
     };
     // Stage sq (landed): the f32 deltas of its rows (lanes = rows), formed as
     // the reference forms them (marsalgo.cc:523-525).
     auto deltas = [&](int sq) {
-        const float *xr = sraw4 + (size_t)(sq % S) * RAW + (2 * W + 1) * FS_ROWS;
+        const float *xr = sraw4 + (size_t)(sq % S) * RAW + (2 * W + 1) * FS_RS;
         const int h = sq & 1, s = sq * FS_ROWS + lane;
         const bool ok = s < len && s > 0;
         dsm[h * FS_ROWS + lane] = ok ? (rev ? xr[lane + 1] - xr[lane] : xr[lane] - xr[lane + 1]) : 0.f;
@@ -609,9 +610,12 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
         const int rows = min(FS_ROWS, len - s0);
         const bool cstart = sq % FS_CHUNK == 0;
         const bool cend = sq % FS_CHUNK == FS_CHUNK - 1 || sq == nstages - 1;
-        const float *xr = sraw4 + (size_t)sg * RAW + (2 * W + 1) * FS_ROWS;
+        const float *xr = sraw4 + (size_t)sg * RAW + (2 * W + 1) * FS_RS;
+        // the grid rows of this stage, as bits of their offsets in it
         int gcount = 0;
-        for (long gr = next_grid; gr < s0 + rows && gr <= last_step; gr += min_span) {
+        unsigned gmask = 0u;
+        for (int gr = next_grid; gr < s0 + rows && gr <= last_step; gr += min_span) {
+            gmask |= 1u << (gr - s0);
             ++gcount;
         }
         if (nsnap + gcount > FS_SNAP || (cstart && nhist == FS_HIST)) {
@@ -668,52 +672,43 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
             }
         }
         if (cwarp) {
-            const float *rw = sraw4 + (size_t)sg * RAW;
-            const float *bw = rw + warp * FS_ROWS;
-            const float *dv = dsm + h * FS_ROWS;
-            const float *rowb = sbo + (size_t)sg * FS_ROWS * MP;
-            long ng = next_grid;
-            int slot = nsnap;
-            // Per lane, where its x comes from: the Bo row (c < m, stride MP) or
-            // one of the per-row candidate arrays (candidate column, y, parent;
-            // stride 1); lanes past the components read the zero delta of the
-            // stage's first row with stride 0. One load per row and component.
-            const float *xsrc[CPL];
-            int xstr[CPL];
+            // Offsets (in floats from the start of shared memory) of this
+            // stage's values: the parent b and delta d of each row, and per lane
+            // where its x comes from -- the Bo row (c < m, stride MP) or one of
+            // the per-row candidate arrays (candidate column, y, parent; stride
+            // 1); lanes past the components read the zero word (stride 0).
+            const float *smf = reinterpret_cast<const float *>(sm);
+            const int rwo = (int)(L.raw / 4) + sg * RAW;
+            const int bwo = rwo + warp * FS_RS;
+            const int dvo = (int)(L.dsm / 4) + h * FS_ROWS;
+            const int boo = (int)(L.bo / 4) + sg * FS_ROWS * MP;
+            int xo[CPL], xs[CPL];
 #pragma unroll
             for (int u = 0; u < CPL; ++u) {
                 const int c = lane + 32 * u;
-                xsrc[u] = c < m ? rowb + c
-                                : c == m ? rw + (W + warp) * FS_ROWS
-                                         : c == m + 1 ? rw + 2 * W * FS_ROWS
-                                                      : c == m + 2 ? rw + warp * FS_ROWS : zero;
-                xstr[u] = c < m ? MP : c < NC ? 1 : 0;
+                xo[u] = c < m ? boo + c
+                              : c == m ? rwo + (W + warp) * FS_RS
+                                       : c == m + 1 ? rwo + 2 * W * FS_RS
+                                                    : c == m + 2 ? bwo : (int)(L.zero / 4);
+                xs[u] = c < m ? MP : c < NC ? 1 : 0;
             }
-            int r = 0;
-            while (r < rows) {
-                // rows up to and including the next grid row of this stage run
-                // without a branch; the snapshot follows
-                const bool grid_here = ng <= last_step && ng < (long)s0 + rows;
-                const int rend = grid_here ? (int)(ng - s0) + 1 : rows;
-#pragma unroll 4
-                for (; r < rend; ++r) {
-                    const float bk = bw[r], d = dv[r];
+            int slot = nsnap;
+            auto row = [&](int r) {
+                const float bk = smf[bwo + r], d = smf[dvo + r];
+                const float d2 = d * d, dd = 2.0f * d;
 #pragma unroll
-                    for (int u = 0; u < CPL; ++u) {
-                        const int c = lane + 32 * u;
-                        const float xv = xsrc[u][r * xstr[u]];
-                        const float klc = kl + fmaf(d * d, qh[u], 2.0f * d * e[u]);
-                        kl = c == cb ? klc : kl;
-                        e[u] = fmaf(d, qh[u], e[u]);
-                        float t, err;
-                        two_sum(qh[u], __fmul_rn(bk, xv), t, err);
-                        ql[u] = __fadd_rn(ql[u], err);
-                        qh[u] = t;
-                    }
+                for (int u = 0; u < CPL; ++u) {
+                    const int c = lane + 32 * u;
+                    const float xv = smf[xo[u] + r * xs[u]];
+                    const float klc = kl + fmaf(d2, qh[u], dd * e[u]);
+                    kl = c == cb ? klc : kl;
+                    e[u] = fmaf(d, qh[u], e[u]);
+                    float t, err;
+                    two_sum(qh[u], __fmul_rn(bk, xv), t, err);
+                    ql[u] = __fadd_rn(ql[u], err);
+                    qh[u] = t;
                 }
-                if (grid_here) {
-                    const int rg = rend - 1;
-                    ng += min_span;
+                if (gmask & (1u << r)) {  // a grid row: snapshot of the increments
                     float *es = myE + (size_t)slot * NCS;
 #pragma unroll
                     for (int u = 0; u < CPL; ++u) {
@@ -726,11 +721,21 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
                         }
                     }
                     if (lane == 0 && warp == 0) {
-                        srow[slot] = idx(s0 + rg);
+                        srow[slot] = idx(s0 + r);
                         sCh[slot] = cur;
-                        sXv[slot] = xr[1 + rg];
+                        sXv[slot] = xr[1 + r];
                     }
                     ++slot;
+                }
+            };
+            if (rows == FS_ROWS) {
+#pragma unroll
+                for (int r = 0; r < FS_ROWS; ++r) {
+                    row(r);
+                }
+            } else {
+                for (int r = 0; r < rows; ++r) {
+                    row(r);
                 }
             }
             if (cend) {
@@ -781,7 +786,7 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
             }
         }
         nsnap += gcount;
-        next_grid += (long)gcount * min_span;
+        next_grid += gcount * min_span;
         __syncthreads();
     }
     if (nsnap > 0) {
@@ -859,11 +864,20 @@ static size_t fast_sweep_smem(int m, int w, int stages) { return FastSweepSmem(m
 // 96 registers for that); fewer candidate warps per block when the tasks are few.
 constexpr size_t FS_SMEM_2 = 113 * 1024;
 
-int fast_sweep_warps(int m, int candidates)
+int fast_sweep_warps(int m, const std::vector<int> &group_sizes)
 {
-    int w = candidates <= 4 * 152 ? 4 : FS_MAXW;
-    while (w > 1 && fast_sweep_smem(m, w, 2) > FS_SMEM_2) {
-        --w;
+    // the most candidates per block (loaders amortised) that still gives
+    // every SM two blocks, else the fewest
+    auto blocks = [&](int w) {
+        long b = 0;
+        for (int g : group_sizes) {
+            b += 2 * ((g + w - 1) / w);
+        }
+        return b;
+    };
+    int w = FS_MAXW;
+    while (w > 1 && (blocks(w) < 2 * 152 || fast_sweep_smem(m, w, 2) > FS_SMEM_2)) {
+        w = w > 4 ? 4 : w - 1;
     }
     return w;
 }

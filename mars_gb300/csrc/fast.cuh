@@ -6,6 +6,8 @@
 #include "common.cuh"
 #include "fp64.cuh"
 
+#include <vector>
+
 namespace mgpu {
 
 struct FastScratch {
@@ -36,7 +38,7 @@ void fast_project(cudaStream_t st, const FillSrc &src, const float *BoC, int n, 
 // `tasks` are SweepTask-sized records {xcol, cand0, count, dir}; bs/bxs: sorted
 // parent and normalised candidate columns; BoR: (n, ldbo) row-major f32 basis
 // (ldbo a multiple of 4).
-int fast_sweep_warps(int m, int candidates);
+int fast_sweep_warps(int m, const std::vector<int> &group_sizes);  // candidates per input column
 int fast_sweep_mid(int head, int tail, int n);  // in [0, n - 1]
 struct FastTaskRec {
     int xcol, cand0, count, dir;
