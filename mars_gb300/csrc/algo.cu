@@ -609,7 +609,7 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
     const double budget = env_double("MARS_GPU_BLOCK_GB", 32.0) * 1e9;
     const double ngrid = linear_only ? 0.0 : (double)sweep_grid_rows(head, tail, min_span);
     (void)ngrid;
-    const double per = 4.0 * n + (linear_only ? 0.0 : 8.0 * n) + 4.0 * m * (ks + 1) + 64.0;
+    const double per = 4.0 * n + 4.0 * m * (ks + 1) + 64.0;
     size_t cap = (size_t)std::max(1.0, budget / per);
     cap = std::min<size_t>(cap, 262144);
     const auto blocks = block_candidates(cx, cap);
@@ -626,10 +626,6 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
     a->fT.ensure(sizeof(float) * maxPc * m);
     a->fmom.ensure(sizeof(double) * 3 * maxPc);
     a->hflag.ensure(sizeof(int) * 2 * maxPc);
-    if (!linear_only) {
-        a->bsort.ensure(sizeof(float) * a->n * maxPc);
-        a->bxsort.ensure(sizeof(float) * a->n * maxPc);
-    }
     a->cand.ensure(sizeof(int) * 2 * (size_t)P);
     int *cx_all = a->cand.as<int>(), *cb_all = cx_all + P;
     CUDA_CHECK(cudaMemcpyAsync(cx_all, cx.data(), sizeof(int) * P, cudaMemcpyHostToDevice, a->st));
@@ -702,14 +698,6 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         a->timer.end(PH_PROJECT, t0);
         if (!linear_only) {
             t0 = a->timer.begin();
-            // all n rows: the mirror half reads the end span too
-            gather_parents(a->st, a->perm.as<int>(), a->B.as<float>(), a->n, cx_d, cb_d, n, n,
-                           Pc, a->bsort.as<float>(), &a->stats.kernel_launches);
-            gather_candidates(a->st, a->perm.as<int>(), a->Bx.as<float>(), a->n, cx_d,
-                              a->svec.as<double>(), a->tol, n, n, Pc, a->bxsort.as<float>(),
-                              &a->stats.kernel_launches);
-            a->timer.end(PH_GATHER, t0);
-            t0 = a->timer.begin();
             std::vector<FastTaskRec> tasks;
             std::vector<int> groups;
             for (int q = 0; q < Pc;) {
@@ -739,9 +727,10 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
                                        sizeof(FastTaskRec) * tasks.size(), cudaMemcpyHostToDevice,
                                        a->st));
             a->stats.h2d_bytes += (long long)(sizeof(FastTaskRec) * tasks.size());
+            const FastSweepCols cols{a->B.as<float>(), a->n,       cb_d,
+                                     a->Bx.as<float>(), a->n, a->svec.as<double>()};
             fast_sweep(a->st, a->tasks.as<FastTaskRec>(), (int)tasks.size(), a->perm.as<int>(),
-                       a->xsort.as<float>(), a->ysort.as<float>(), a->bsort.as<float>(),
-                       a->bxsort.as<float>(), a->BoF.as<float>(), a->ldbo,
+                       a->xsort.as<float>(), a->ysort.as<float>(), cols, a->BoF.as<float>(), a->ldbo,
                        a->ybo_d.as<double>(), a->ybx.as<double>(), a->fmom.as<double>(), n, m,
                        head, tail, min_span, a->tol, env_double("MARS_GPU_MIXED_CUT_REL", 1e-7),
                        a->hsse.as<double>(), a->hrow.as<int>(), a->hflag.as<int>(), warps,

@@ -336,7 +336,7 @@ template <int CPL, int S>
 __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
     k_fast_sweep(const FastTask *__restrict__ tasks, const int *__restrict__ perm,
                  const float *__restrict__ xsort, const float *__restrict__ ysort,
-                 const float *__restrict__ bs, const float *__restrict__ bxs,
+                 const FastSweepCols cols,
                  const float *__restrict__ BoR, size_t ldbo, const double *__restrict__ ybo,
                  const double *__restrict__ ybx, const double *__restrict__ mom, int n, int m,
                  int head, int tail, int mid, int min_span, double tol, double cut_rel,
@@ -380,8 +380,11 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
     const int *pk = perm + (size_t)task.xcol * n;
     const float *xs = xsort + (size_t)task.xcol * n;
     const float *ys = ysort + (size_t)task.xcol * n;
-    const float *bsb = bs + (size_t)task.cand0 * n;
-    const float *bxb = bxs + (size_t)task.cand0 * n;
+    // loader of the per-candidate arrays: lane q holds candidate q's parent
+    // column and normalisation
+    const int pcol = rwarp && lane < task.count ? cols.cand_b[task.cand0 + lane] : 0;
+    const float pscale =
+        rwarp && lane < task.count ? fast_scale(cols.s[task.cand0 + lane], tol) : 0.0f;
     for (int e = threadIdx.x; e < W * (m + 1); e += blockDim.x) {
         const int w = e / (m + 1), c = e % (m + 1);
         const double v = c < m ? ybo[c] : (w < task.count ? ybx[task.cand0 + w] : 0.0);
@@ -434,9 +437,12 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
         float *rw = sraw4 + (size_t)sg * RAW;
         const bool ok = lane < rows;
         const int i = ok ? idx(s0 + lane) : 0;
+        const int pi = ok ? pk[i] : 0;  // the row of sorted position i
         for (int cw = 0; cw < task.count; ++cw) {
-            cp_async4(rw + cw * FS_RS + lane, bsb + (size_t)cw * n + i, ok);
-            cp_async4(rw + (W + cw) * FS_RS + lane, bxb + (size_t)cw * n + i, ok);
+            const int bc = __shfl_sync(0xffffffffu, pcol, cw);
+            cp_async4(rw + cw * FS_RS + lane, cols.B + (size_t)bc * cols.ldB + pi, ok);
+            cp_async4(rw + (W + cw) * FS_RS + lane,
+                      cols.Bx + (size_t)(task.cand0 + cw) * cols.ldBx + pi, ok);
         }
         cp_async4(rw + 2 * W * FS_RS + lane, ys + i, ok);
         cp_async4(rw + (2 * W + 1) * FS_RS + 1 + lane, xs + i, ok);
@@ -446,11 +452,16 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
     };
     // Stage sq (landed): the f32 deltas of its rows (lanes = rows), formed as
     // the reference forms them (marsalgo.cc:523-525).
+    // and the candidate columns normalised in place, f32(Bx * scale).
     auto deltas = [&](int sq) {
-        const float *xr = sraw4 + (size_t)(sq % S) * RAW + (2 * W + 1) * FS_RS;
+        float *rwl = sraw4 + (size_t)(sq % S) * RAW;
+        const float *xr = rwl + (2 * W + 1) * FS_RS;
         const int h = sq & 1, s = sq * FS_ROWS + lane;
         const bool ok = s < len && s > 0;
         dsm[h * FS_ROWS + lane] = ok ? (rev ? xr[lane + 1] - xr[lane] : xr[lane] - xr[lane + 1]) : 0.f;
+        for (int cw = 0; cw < task.count; ++cw) {
+            rwl[(W + cw) * FS_RS + lane] *= __shfl_sync(0xffffffffu, pscale, cw);
+        }
     };
 
     const int wsel = cwarp ? warp : 0;
@@ -883,7 +894,7 @@ int fast_sweep_warps(int m, const std::vector<int> &group_sizes)
 }
 
 void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int *perm,
-                const float *xsort, const float *ysort, const float *bs, const float *bxs,
+                const float *xsort, const float *ysort, const FastSweepCols &cols,
                 const float *BoR, size_t ldbo, const double *ybo, const double *ybx,
                 const double *mom, int n, int m, int head, int tail, int min_span, double tol,
                 double cut_rel, double *hsse, int *hrow, int *hflag, int warps_per_block,
@@ -903,7 +914,7 @@ void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int
     do {                                                                                       \
         allow_max_smem(k_fast_sweep<CPL, S>);                                                  \
         k_fast_sweep<CPL, S><<<ntasks, 32 * (warps + 2), smem, st>>>(                          \
-            reinterpret_cast<const FastTask *>(tasks), perm, xsort, ysort, bs, bxs, BoR, ldbo, \
+            reinterpret_cast<const FastTask *>(tasks), perm, xsort, ysort, cols, BoR, ldbo,    \
             ybo, ybx, mom, n, m, head, tail, mid, min_span, tol, cut_rel, hsse, hrow, hflag);  \
     } while (0)
 #define LAUNCH_FS_CPL(CPL)      \

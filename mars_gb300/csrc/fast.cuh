@@ -35,16 +35,26 @@ void fast_project(cudaStream_t st, const FillSrc &src, const float *BoC, int n, 
 // hsse[2 j + dir] (the hinge part of the best score), hrow[2 j + dir], and
 // hflag[2 j + dir] = 1 when a cut of that half has den below cut_rel of the
 // reference's K (its f64 value there is unreliable). mom: from fast_project.
-// `tasks` are SweepTask-sized records {xcol, cand0, count, dir}; bs/bxs: sorted
-// parent and normalised candidate columns; BoR: (n, ldbo) row-major f32 basis
-// (ldbo a multiple of 4).
+// `tasks` are SweepTask-sized records {xcol, cand0, count, dir}; BoR: (n, ldbo)
+// row-major f32 basis (ldbo a multiple of 4).
 int fast_sweep_warps(int m, const std::vector<int> &group_sizes);  // candidates per input column
+// The sweep's per-candidate columns, read in each input's sorted order by the
+// sweep itself: the parent B[:, cand_b[j]] and the projected candidate column
+// Bx[:, j], normalised there by f32(1 / sqrt(s[j] + tol)).
+struct FastSweepCols {
+    const float *B;
+    size_t ldB;
+    const int *cand_b;
+    const float *Bx;
+    size_t ldBx;
+    const double *s;
+};
 int fast_sweep_mid(int head, int tail, int n);  // in [0, n - 1]
 struct FastTaskRec {
     int xcol, cand0, count, dir;
 };
 void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int *perm,
-                const float *xsort, const float *ysort, const float *bs, const float *bxs,
+                const float *xsort, const float *ysort, const FastSweepCols &cols,
                 const float *BoR, size_t ldbo, const double *ybo, const double *ybx,
                 const double *mom, int n, int m, int head, int tail, int min_span, double tol,
                 double cut_rel, double *hsse, int *hrow, int *hflag, int warps_per_block,
