@@ -49,7 +49,8 @@ WORKLOADS = {
     "hinge_search": "hinge_search n=100000 p=20 iid N(0,1), 6 hinges + 3 hinge products, "
                     "max_terms=31 max_degree=2 tail_span=0 (config 2)",
     "precision_stress": "precision_stress n=1000000 p=100 AR(1) rho=0.9 + 5 near-duplicates, "
-                        "max_terms=63 tail_span=0 (config 3)",
+                        "max_terms=63 max_degree=3 tail_span=0.02 (config 3; the reference's "
+                        "default tail span)",
     "plain_fit": "plain_fit n=10000 p=2 linear_only max_terms=17 (config 1)",
     "batched": "256 independent fits, n log-uniform 1e3..2e5, p uniform 5..50, 4 random hinges "
                "+ N(0,1) noise, max_terms=21, tail_span=0 (config 4)",
@@ -79,7 +80,9 @@ def workload(name):
     if name == "hinge_search":
         return workloads.hinge_search()
     if name == "precision_stress":
-        return workloads.precision_stress()
+        X, y, kw = workloads.precision_stress()
+        kw["tail_span"] = 0.02
+        return X, y, kw
     return workloads.plain_fit()
 
 

@@ -5,6 +5,8 @@
 // (fixed per-thread order, fixed block tree, fixed order across blocks).
 #include "fp64.cuh"
 
+#include <type_traits>
+
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
@@ -540,7 +542,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
     double best = 0.0;
     int besti = -1;
     int nsnap = 0;  // block-uniform
-    long next_grid = (long)head + 1;
+    int next_grid = head + 1;
 
     auto flush = [&]() {
         if (cwarp) {
@@ -609,7 +611,9 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
         const int sg = sq % S, h = sq & 1, i0 = sq * SW_ROWS;
         const int rows = min(SW_ROWS, tail - i0);
         int gcount = 0;
-        for (long gr = next_grid; gr < i0 + rows; gr += min_span) {
+        unsigned gmask = 0u;  // the grid rows of this stage
+        for (int gr = next_grid; gr < i0 + rows; gr += min_span) {
+            gmask |= 1u << (gr - i0);
             ++gcount;
         }
         if (nsnap + gcount > SW_SNAP) {
@@ -622,10 +626,8 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
             const double *xw = cv + (W + warp) * SW_ROWS;
             const double *dv = cv + 2 * W * SW_ROWS;
             const double *rowb = sbo + (size_t)sg * SW_ROWS * MP;
-            long ng = next_grid;
             int slot = nsnap;
-            for (int r = 0; r < rows; ++r) {
-                const int i = i0 + r;
+            auto step = [&](int r) {
                 const double bk = bw[r], bxk = xw[r];
                 const double *rowp = rowb + r * MP;
                 const double di = dv[r];  // 0 for the first row
@@ -637,8 +639,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
                     f[q] = fma(di, g[q], f[q]);
                     g[q] = fma(bk, xv, g[q]);
                 }
-                if (i == ng) {
-                    ng += min_span;
+                if (gmask & (1u << r)) {
                     double *fs = snap + (size_t)slot * ldF;
 #pragma unroll
                     for (int q = 0; q < CPL; ++q) {
@@ -648,9 +649,19 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
                         }
                     }
                     if (lane == 0 && warp == 0) {
-                        srow[slot] = i;
+                        srow[slot] = i0 + r;
                     }
                     ++slot;
+                }
+            };
+            if (rows == SW_ROWS) {  // a whole stage, unrolled
+#pragma unroll
+                for (int r = 0; r < SW_ROWS; ++r) {
+                    step(r);
+                }
+            } else {
+                for (int r = 0; r < rows; ++r) {
+                    step(r);
                 }
             }
         } else if (lwarp) {
@@ -666,7 +677,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
             }
         }
         nsnap += gcount;
-        next_grid += (long)gcount * min_span;
+        next_grid += gcount * min_span;
         __syncthreads();
     }
     if (nsnap > 0) {
@@ -825,52 +836,72 @@ __global__ void __launch_bounds__(SC_THREADS)
     const bool active = !lwarp && lane < task.count;
     double *out = scal + (size_t)(task.cand0 + (lane < task.count ? lane : 0)) * ngrid * 3;
     double v0 = 0.0, v1 = 0.0, v2 = 0.0;
-    long ng = (long)head + 1;
+    int ng = head + 1;
     int gi = 0;
+    // One stage of rows for the chains of warp role R (0: vb, w; 1: b2, bd,
+    // k1; 2: b2, k0); a whole stage is unrolled, the grid rows a bitmask.
+    auto stage = [&](auto role, int h, int i0, int rows, unsigned gmask) {
+        constexpr int R = decltype(role)::value;
+        const double *dv = sd[h], *ddv = sdd[h], *d2v = sd2[h];
+        auto step = [&](int r) {
+            const int i = i0 + r;
+            const double bk = db[h][r][lane];
+            if (R == 0) {  // v0 = vb, v1 = w
+                const double yk = dy[h][r];
+                if (i == 0) {
+                    v0 = bk * yk;
+                } else {
+                    v1 = fma(dv[r], v0, v1);
+                    v0 = fma(yk, bk, v0);
+                }
+            } else if (R == 1) {  // v0 = b2, v1 = bd, v2 = k1
+                if (i == 0) {
+                    v0 = bk * bk;
+                } else {
+                    v2 = fma(d2v[r], v1, v2);
+                    v1 = fma(dv[r], v0, v1);
+                    v0 = fma(bk, bk, v0);
+                }
+            } else {  // v0 = b2, v1 = k0
+                if (i == 0) {
+                    v0 = bk * bk;
+                } else {
+                    v1 = fma(ddv[r], v0, v1);
+                    v0 = fma(bk, bk, v0);
+                }
+            }
+            if (gmask & (1u << r)) {
+                out[(size_t)gi * 3 + (R == 0 ? 2 : R == 1 ? 1 : 0)] = R == 1 ? v2 : v1;
+                ++gi;
+            }
+        };
+        if (rows == SC_ROWS) {
+#pragma unroll
+            for (int r = 0; r < SC_ROWS; ++r) {
+                step(r);
+            }
+        } else {
+            for (int r = 0; r < rows; ++r) {
+                step(r);
+            }
+        }
+    };
     for (int sq = 0; sq < nstages; ++sq) {
         const int h = sq & 1, i0 = sq * SC_ROWS;
         const int rows = min(SC_ROWS, tail - i0);
+        unsigned gmask = 0u;
+        int gcount = 0;
+        for (int g = ng; g < i0 + rows; g += min_span) {
+            gmask |= 1u << (g - i0);
+            ++gcount;
+        }
         if (active) {
-            const double *dv = sd[h], *ddv = sdd[h], *d2v = sd2[h];
-            for (int r = 0; r < rows; ++r) {
-                const int i = i0 + r;
-                const double bk = db[h][r][lane];
-                if (warp == 0) {  // v0 = vb, v1 = w
-                    const double yk = dy[h][r];
-                    if (i == 0) {
-                        v0 = bk * yk;
-                    } else {
-                        v1 = fma(dv[r], v0, v1);
-                        v0 = fma(yk, bk, v0);
-                    }
-                } else if (warp == 1) {  // v0 = b2, v1 = bd, v2 = k1
-                    if (i == 0) {
-                        v0 = bk * bk;
-                    } else {
-                        v2 = fma(d2v[r], v1, v2);
-                        v1 = fma(dv[r], v0, v1);
-                        v0 = fma(bk, bk, v0);
-                    }
-                } else {  // v0 = b2, v1 = k0
-                    if (i == 0) {
-                        v0 = bk * bk;
-                    } else {
-                        v1 = fma(ddv[r], v0, v1);
-                        v0 = fma(bk, bk, v0);
-                    }
-                }
-                if (i == ng) {
-                    ng += min_span;
-                    double *o = out + (size_t)gi * 3;
-                    if (warp == 0) {
-                        o[2] = v1;
-                    } else if (warp == 1) {
-                        o[1] = v2;
-                    } else {
-                        o[0] = v1;
-                    }
-                    ++gi;
-                }
+            if (warp == 0) {
+                stage(std::integral_constant<int, 0>(), h, i0, rows, gmask);
+            } else if (warp == 1) {
+                stage(std::integral_constant<int, 1>(), h, i0, rows, gmask);
+            } else {
+                stage(std::integral_constant<int, 2>(), h, i0, rows, gmask);
             }
         } else if (lwarp) {
             if (sq + S - 1 < nstages) {
@@ -883,6 +914,7 @@ __global__ void __launch_bounds__(SC_THREADS)
                 convert(sq + 1);
             }
         }
+        ng += gcount * min_span;
         __syncthreads();
     }
 }
