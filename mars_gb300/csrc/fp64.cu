@@ -759,19 +759,34 @@ __global__ void __launch_bounds__(SS_THREADS)
 // column -- so they run here, concurrently with the projection, and the sweep
 // reads k0, k1, w at its grid rows.
 //
-// Block = one input column and up to 32 parents (lane = parent). A result of
-// GB300's FP64 pipe reaches a dependent FP64 instruction after ~86 cycles but
-// a shuffle or store only after a few hundred, so no value crosses lanes or
-// warps per row; instead the six chains are split over three warps, none of
-// them issuing more than three FMAs per row:
-//   warp 0: vb, w      warp 1: b2, bd, k1      warp 2: b2, k0
-// (b2 is computed twice, identically). Warp 3 stages the rows with coalesced
-// cp.async from the sorted copies (the parents' B per candidate, y and x per
-// input column) and converts them to f64 once, with the deltas.
+// Block = one input column and up to 32 parents (lane = parent). GB300's FP64
+// pipe takes one warp instruction per ~64 cycles per SM sub-partition, so no
+// warp (one per sub-partition) issues more than two FMAs per row:
+//   warp 0: vb, w      warp 1: b2, bd      warp 2: k0, k1
+// Warp 1 leaves b2 and bd of every row in shared memory; warp 2 runs one
+// stage (32 rows) behind and reads them there, long after they were written.
+// Warp 3 stages the rows with coalesced cp.async from the sorted copies (the
+// parents' B per candidate, y and x per input column) and converts them to
+// f64 once, with the deltas (kept three stages deep for the lagging warp).
 // Output per candidate and grid row g: scal[(cand * ngrid + g) * 3 + {0,1,2}] =
 // k0, k1, w.
 // ---------------------------------------------------------------------------
 constexpr int SC_ROWS = 32, SC_STAGES = 4, SC_THREADS = 128, SC_MAXP = 32;
+
+// Dynamic shared memory of k_hinge_scalars (byte offsets).
+struct ScSmem {
+    static constexpr size_t rb = 0;  // [S][MAXP][ROWS] f32, B of each parent, lanes over rows
+    static constexpr size_t ry = rb + 4 * SC_STAGES * SC_MAXP * SC_ROWS;  // [S][ROWS] f32
+    static constexpr size_t rx = ry + 4 * SC_STAGES * SC_ROWS;  // [S][ROWS + 1] f32
+    static constexpr size_t db = align16(rx + 4 * SC_STAGES * (SC_ROWS + 1));  // [2][ROWS][MAXP+1]
+    static constexpr size_t dy = db + 8 * 2 * SC_ROWS * (SC_MAXP + 1);  // [2][ROWS] f64
+    static constexpr size_t sd = dy + 8 * 2 * SC_ROWS;    // [3][ROWS] f64: d, then d^2, 2d
+    static constexpr size_t sdd = sd + 8 * 3 * SC_ROWS;
+    static constexpr size_t sd2 = sdd + 8 * 3 * SC_ROWS;
+    static constexpr size_t lb2 = sd2 + 8 * 3 * SC_ROWS;  // [2][ROWS][MAXP] f64, b2 after row r
+    static constexpr size_t lbd = lb2 + 8 * 2 * SC_ROWS * SC_MAXP;  // bd after row r
+    static constexpr size_t total = lbd + 8 * 2 * SC_ROWS * SC_MAXP;
+};
 
 __global__ void __launch_bounds__(SC_THREADS)
     k_hinge_scalars(const SweepTask *__restrict__ tasks, const float *__restrict__ xsort,
@@ -779,12 +794,17 @@ __global__ void __launch_bounds__(SC_THREADS)
                     int head, int tail, int min_span, int ngrid, double *__restrict__ scal)
 {
     constexpr int S = SC_STAGES;
-    __shared__ float rb[S][SC_MAXP][SC_ROWS];  // B of each parent, lanes over rows
-    __shared__ float ry[S][SC_ROWS];
-    __shared__ float rx[S][SC_ROWS + 1];  // x of rows i0 - 1 .. i0 + 31
-    __shared__ double db[2][SC_ROWS][SC_MAXP + 1];
-    __shared__ double dy[2][SC_ROWS];
-    __shared__ double sd[2][SC_ROWS], sdd[2][SC_ROWS], sd2[2][SC_ROWS];
+    extern __shared__ __align__(16) unsigned char scm[];
+    auto rb = reinterpret_cast<float(*)[SC_MAXP][SC_ROWS]>(scm + ScSmem::rb);
+    auto ry = reinterpret_cast<float(*)[SC_ROWS]>(scm + ScSmem::ry);
+    auto rx = reinterpret_cast<float(*)[SC_ROWS + 1]>(scm + ScSmem::rx);
+    auto db = reinterpret_cast<double(*)[SC_ROWS][SC_MAXP + 1]>(scm + ScSmem::db);
+    auto dy = reinterpret_cast<double(*)[SC_ROWS]>(scm + ScSmem::dy);
+    auto sd = reinterpret_cast<double(*)[SC_ROWS]>(scm + ScSmem::sd);
+    auto sdd = reinterpret_cast<double(*)[SC_ROWS]>(scm + ScSmem::sdd);
+    auto sd2 = reinterpret_cast<double(*)[SC_ROWS]>(scm + ScSmem::sd2);
+    auto lb2 = reinterpret_cast<double(*)[SC_ROWS][SC_MAXP]>(scm + ScSmem::lb2);
+    auto lbd = reinterpret_cast<double(*)[SC_ROWS][SC_MAXP]>(scm + ScSmem::lbd);
 
     const SweepTask task = tasks[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -806,16 +826,17 @@ __global__ void __launch_bounds__(SC_THREADS)
             cp_async4(&rx[sg][0], xs + (i0 > 0 ? i0 - 1 : 0), i0 > 0);
         }
     };
-    auto convert = [&](int sq) {  // stage sq (landed) -> f64 slot sq & 1, lanes over rows
-        const int sg = sq % S, h = sq & 1, i = sq * SC_ROWS + lane;
+    // stage sq (landed) -> f64: B and y in slot sq & 1, the deltas in slot sq % 3
+    auto convert = [&](int sq) {
+        const int sg = sq % S, h = sq & 1, h3 = sq % 3, i = sq * SC_ROWS + lane;
         for (int q = 0; q < task.count; ++q) {
             db[h][lane][q] = (double)rb[sg][q][lane];
         }
         dy[h][lane] = (double)ry[sg][lane];
         const double dl = i > 0 ? (double)(rx[sg][lane] - rx[sg][lane + 1]) : 0.0;
-        sd[h][lane] = dl;
-        sdd[h][lane] = dl * dl;
-        sd2[h][lane] = dl * 2;
+        sd[h3][lane] = dl;
+        sdd[h3][lane] = dl * dl;
+        sd2[h3][lane] = dl * 2;
     };
 
     if (lwarp) {
@@ -835,47 +856,62 @@ __global__ void __launch_bounds__(SC_THREADS)
     __syncthreads();
     const bool active = !lwarp && lane < task.count;
     double *out = scal + (size_t)(task.cand0 + (lane < task.count ? lane : 0)) * ngrid * 3;
-    double v0 = 0.0, v1 = 0.0, v2 = 0.0;
-    int ng = head + 1;
+    // role 0: v0 = vb, v1 = w; role 1: v0 = b2, v1 = bd; role 2: v0 = k0, v1 = k1,
+    // one stage behind roles 0 and 1, from the b2 and bd they leave per row
+    double v0 = 0.0, v1 = 0.0;
+    double pb2 = 0.0, pbd = 0.0;  // role 2: b2 and bd after the row before its stage
     int gi = 0;
-    // One stage of rows for the chains of warp role R (0: vb, w; 1: b2, bd,
-    // k1; 2: b2, k0); a whole stage is unrolled, the grid rows a bitmask.
-    auto stage = [&](auto role, int h, int i0, int rows, unsigned gmask) {
+    auto grid_mask = [&](int ng, int i0, int rows) {
+        unsigned mask = 0u;
+        for (int g = ng; g < i0 + rows; g += min_span) {
+            mask |= 1u << (g - i0);
+        }
+        return mask;
+    };
+    auto stage = [&](auto role, int sq, int rows, unsigned gmask) {
         constexpr int R = decltype(role)::value;
-        const double *dv = sd[h], *ddv = sdd[h], *d2v = sd2[h];
+        const int i0 = sq * SC_ROWS, h = sq & 1, h3 = sq % 3;
+        const double *dv = sd[h3], *ddv = sdd[h3], *d2v = sd2[h3];
         auto step = [&](int r) {
             const int i = i0 + r;
-            const double bk = db[h][r][lane];
-            if (R == 0) {  // v0 = vb, v1 = w
-                const double yk = dy[h][r];
+            if (R == 0) {  // vb, w
+                const double bk = db[h][r][lane], yk = dy[h][r];
                 if (i == 0) {
                     v0 = bk * yk;
                 } else {
                     v1 = fma(dv[r], v0, v1);
                     v0 = fma(yk, bk, v0);
                 }
-            } else if (R == 1) {  // v0 = b2, v1 = bd, v2 = k1
+            } else if (R == 1) {  // b2, bd
+                const double bk = db[h][r][lane];
                 if (i == 0) {
                     v0 = bk * bk;
                 } else {
-                    v2 = fma(d2v[r], v1, v2);
                     v1 = fma(dv[r], v0, v1);
                     v0 = fma(bk, bk, v0);
                 }
-            } else {  // v0 = b2, v1 = k0
-                if (i == 0) {
-                    v0 = bk * bk;
-                } else {
-                    v1 = fma(ddv[r], v0, v1);
-                    v0 = fma(bk, bk, v0);
+                lb2[h][r][lane] = v0;
+                lbd[h][r][lane] = v1;
+            } else {  // k0, k1 from the b2 and bd after the previous row
+                const double b2p = r == 0 ? pb2 : lb2[h][r - 1][lane];
+                const double bdp = r == 0 ? pbd : lbd[h][r - 1][lane];
+                if (i > 0) {
+                    v0 = fma(ddv[r], b2p, v0);
+                    v1 = fma(d2v[r], bdp, v1);
                 }
             }
-            if (gmask & (1u << r)) {
-                out[(size_t)gi * 3 + (R == 0 ? 2 : R == 1 ? 1 : 0)] = R == 1 ? v2 : v1;
+            if (R != 1 && (gmask & (1u << r))) {
+                double *o = out + (size_t)gi * 3;
+                if (R == 0) {
+                    o[2] = v1;
+                } else {
+                    o[0] = v0;
+                    o[1] = v1;
+                }
                 ++gi;
             }
         };
-        if (rows == SC_ROWS) {
+        if (rows == SC_ROWS) {  // a whole stage, unrolled
 #pragma unroll
             for (int r = 0; r < SC_ROWS; ++r) {
                 step(r);
@@ -885,25 +921,27 @@ __global__ void __launch_bounds__(SC_THREADS)
                 step(r);
             }
         }
-    };
-    for (int sq = 0; sq < nstages; ++sq) {
-        const int h = sq & 1, i0 = sq * SC_ROWS;
-        const int rows = min(SC_ROWS, tail - i0);
-        unsigned gmask = 0u;
-        int gcount = 0;
-        for (int g = ng; g < i0 + rows; g += min_span) {
-            gmask |= 1u << (g - i0);
-            ++gcount;
+        if (R == 2) {
+            pb2 = lb2[h][rows - 1][lane];
+            pbd = lbd[h][rows - 1][lane];
         }
+    };
+    int ng = head + 1, ng2 = head + 1;  // next grid row of stage sq, and of stage sq - 1
+    for (int sq = 0; sq <= nstages; ++sq) {
+        const int rows = sq < nstages ? min(SC_ROWS, tail - sq * SC_ROWS) : 0;
+        const unsigned gmask = sq < nstages ? grid_mask(ng, sq * SC_ROWS, rows) : 0u;
+        const int rows2 = sq > 0 ? min(SC_ROWS, tail - (sq - 1) * SC_ROWS) : 0;
+        const unsigned gmask2 = sq > 0 ? grid_mask(ng2, (sq - 1) * SC_ROWS, rows2) : 0u;
+        const int gc = __popc(gmask), gc2 = __popc(gmask2);
         if (active) {
-            if (warp == 0) {
-                stage(std::integral_constant<int, 0>(), h, i0, rows, gmask);
-            } else if (warp == 1) {
-                stage(std::integral_constant<int, 1>(), h, i0, rows, gmask);
-            } else {
-                stage(std::integral_constant<int, 2>(), h, i0, rows, gmask);
+            if (warp == 0 && sq < nstages) {
+                stage(std::integral_constant<int, 0>(), sq, rows, gmask);
+            } else if (warp == 1 && sq < nstages) {
+                stage(std::integral_constant<int, 1>(), sq, rows, gmask);
+            } else if (warp == 2 && sq > 0) {
+                stage(std::integral_constant<int, 2>(), sq - 1, rows2, gmask2);
             }
-        } else if (lwarp) {
+        } else if (lwarp && sq < nstages) {
             if (sq + S - 1 < nstages) {
                 issue(sq + S - 1);
             }
@@ -914,7 +952,8 @@ __global__ void __launch_bounds__(SC_THREADS)
                 convert(sq + 1);
             }
         }
-        ng += gcount * min_span;
+        ng += gc * min_span;
+        ng2 += gc2 * min_span;
         __syncthreads();
     }
 }
@@ -1390,9 +1429,10 @@ void hinge_scalars(cudaStream_t st, const SweepTask *tasks, int ntasks, const fl
     if (ntasks <= 0) {
         return;
     }
-    k_hinge_scalars<<<ntasks, SC_THREADS, 0, st>>>(tasks, xsort, ysort, bs, n, head, tail,
-                                                   min_span, sweep_grid_rows(head, tail, min_span),
-                                                   scal);
+    allow_max_smem(k_hinge_scalars);
+    k_hinge_scalars<<<ntasks, SC_THREADS, ScSmem::total, st>>>(
+        tasks, xsort, ysort, bs, n, head, tail, min_span, sweep_grid_rows(head, tail, min_span),
+        scal);
     LAUNCH_CHECK();
     *launches += 1;
 }
