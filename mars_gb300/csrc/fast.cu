@@ -163,7 +163,9 @@ __global__ void __launch_bounds__(256)
 
 // Per candidate j (parent b = B[:, cand_b[j]], input x = X[:, cand_x[j]] * s):
 // mom[3 j + k] = sum_i b_i^2 x_i^k, k = 0, 1, 2 (sum b^2 x^2 is also the raw
-// squared norm of the candidate column x b).
+// squared norm of the candidate column x b). They only set flag thresholds, so
+// FP32 per thread and FP64 across threads (an FP64 sum per row would make the
+// kernel FP64-pipe bound).
 __global__ void __launch_bounds__(256) k_parent_moments(FillSrc src, int n, double *__restrict__ mom)
 {
     __shared__ double red[3][8];
@@ -172,17 +174,15 @@ __global__ void __launch_bounds__(256) k_parent_moments(FillSrc src, int n, doub
     const float *bcol = src.B + (size_t)src.cand_b[j] * src.ldB;
     const float *xcol = src.X + (size_t)xc * src.ldX;
     const float sx = src.s[xc];
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    float f0 = 0.f, f1 = 0.f, f2 = 0.f;
     for (int i = t; i < n; i += 256) {
-        const double b = bcol[i], x = (double)(xcol[i] * sx);
-        const double b2 = b * b;
-        a0 += b2;
-        a1 += b2 * x;
-        a2 += b2 * x * x;
+        const float b = bcol[i], x = xcol[i] * sx;
+        const float b2 = b * b, b2x = b2 * x;
+        f0 += b2;
+        f1 += b2x;
+        f2 = fmaf(b2x, x, f2);
     }
-    a0 = warp_sum(a0);
-    a1 = warp_sum(a1);
-    a2 = warp_sum(a2);
+    double a0 = warp_sum((double)f0), a1 = warp_sum((double)f1), a2 = warp_sum((double)f2);
     if ((t & 31) == 0) {
         red[0][t >> 5] = a0;
         red[1][t >> 5] = a1;
