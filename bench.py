@@ -245,9 +245,9 @@ def traffic_ratio(precision, workload_name, kernel):
 
 def roofline(st, workload_name, precision):
     """The dominant kernel against its roofline. The hinge sweep is charged
-    with its algorithmic bytes against HBM bandwidth; in this implementation
-    it is bound by the FP64 pipe (the captures in profiles/), so the fraction
-    is small by construction."""
+    with its algorithmic bytes against HBM bandwidth. The FP64 sweep is bound
+    by the FP64 pipe and the fast sweep by the latency of its sequential row
+    walk (the captures in profiles/), so the fraction is small by construction."""
     hbm, bf16, src = peaks()
     phases = {"sweep": st["ms_sweep"], "project": st["ms_project"]}
     dom = max(phases, key=phases.get)
@@ -260,7 +260,10 @@ def roofline(st, workload_name, precision):
                 "unit": "GB/s", "frac": ach / hbm, "peak_source": src,
                 "algorithmic_bytes_per_launch": per_launch,
                 "traffic": None if ratio is None else ratio * per_launch,
-                "limiter": "FP64 pipe and FP64 dependency latency (ncu: DRAM < 1% of peak)"}
+                "limiter": ("FP64 pipe (ncu: 57% active) and FP64 dependency latency; DRAM < 1% "
+                            "of peak" if precision == "fp64" else
+                            "latency of each warp's sequential walk over the sorted rows "
+                            "(ncu: issue 32% active, no FP64, DRAM 6% of peak)")}
     ms = max(st["ms_project"], 1e-9)
     ach = st["project_flops"] / (ms * 1e-3) / 1e12
     return {"kernel": "projection", "bound": "tensor", "achieved": ach, "peak": bf16,
