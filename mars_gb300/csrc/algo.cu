@@ -464,12 +464,22 @@ void eval_block_fp64(mars_gpu_algo *a, Fp64Ctx &c, int Pc, const int *cx_d, cons
     c.timer->end(PH_DGKS, t0);
 
     t0 = c.timer->begin();
-    if (linear_only) {
+    // Few candidates (latency-bound chains): the ybx chain on its own stream,
+    // the sweep storing partial scores that sweep_score finishes once ybx is
+    // known. Many: the partial scores would cost more HBM traffic than the
+    // overlap saves, so ybx comes first and the sweep scores directly.
+    const double part_bytes =
+        32.0 * Pc * (linear_only ? 0.0 : (double)sweep_grid_rows(head, tail, min_span));
+    const bool defer = !linear_only && part_bytes <= env_double("MARS_GPU_DEFER_BYTES", 1e9);
+    if (!defer) {
         normalize_ybx(c.st, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), false,
                       c.ybx->as<double>(), &c.stats->kernel_launches);
+        if (!linear_only) {
+            gather_candidates(c.st, a->perm.as<int>(), Bx, a->n, cx_d, s, a->tol, n, tail, Pc,
+                              c.bxsort->as<float>(), &c.stats->kernel_launches);
+        }
     } else {
-        // The ybx chain on its own stream: the sweep stores the partial scores
-        // and sweep_score finishes them once ybx is known.
+        c.part->ensure(std::max<size_t>(8, (size_t)part_bytes));
         CUDA_CHECK(cudaEventRecord(c.ev_s, c.st));
         CUDA_CHECK(cudaStreamWaitEvent(c.st3, c.ev_s, 0));
         normalize_ybx(c.st3, Bx, a->n, n, Pc, s, a->tol, a->y.as<float>(), false,
@@ -508,11 +518,14 @@ void eval_block_fp64(mars_gpu_algo *a, Fp64Ctx &c, int Pc, const int *cx_d, cons
                a->xsort.as<float>(), c.bsort->as<float>(), c.bxsort->as<float>(),
                a->Bo.as<double>(), a->ldbo, a->ybo_d.as<double>(), c.ybx->as<double>(),
                c.scal->as<double>(), n, m, head, tail, min_span, a->tol, c.hsse->as<double>(),
-               c.hrow->as<int>(), warps, &c.stats->kernel_launches, c.part->as<double>());
-    CUDA_CHECK(cudaStreamWaitEvent(c.st, c.ev_ybx, 0));
-    sweep_score(c.st, c.part->as<double>(), Pc, cx_d, a->perm.as<int>(), c.ybx->as<double>(), n,
-                head, tail, min_span, a->tol, c.hsse->as<double>(), c.hrow->as<int>(),
-                &c.stats->kernel_launches);
+               c.hrow->as<int>(), warps, &c.stats->kernel_launches,
+               defer ? c.part->as<double>() : nullptr);
+    if (defer) {
+        CUDA_CHECK(cudaStreamWaitEvent(c.st, c.ev_ybx, 0));
+        sweep_score(c.st, c.part->as<double>(), Pc, cx_d, a->perm.as<int>(),
+                    c.ybx->as<double>(), n, head, tail, min_span, a->tol, c.hsse->as<double>(),
+                    c.hrow->as<int>(), &c.stats->kernel_launches);
+    }
     c.timer->end(PH_SWEEP, t0);
     if (count_work) {
         c.stats->knot_evals += (long long)Pc * sweep_grid_rows(head, tail, min_span);
@@ -541,8 +554,6 @@ void run_spec(mars_gpu_algo *a, const std::vector<int> &sx, const std::vector<in
     L.fired.ensure(sizeof(int) * C);
     L.nfired.ensure(sizeof(int) * 4);
     L.scal.ensure(sizeof(double) * 3 *
-                  std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
-    L.part.ensure(sizeof(double) * 4 *
                   std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
     int *ecx = L.cand.as<int>(), *ecb = ecx + C;
     const cudaStream_t st = L.ss.st;
@@ -931,8 +942,6 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         if (!linear_only) {
             a->scal.ensure(sizeof(double) * 3 *
                            std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
-            a->part.ensure(sizeof(double) * 4 *
-                           std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
         }
         int *ecx = a->cand.as<int>(), *ecb = ecx + C;
         CUDA_CHECK(cudaMemcpyAsync(ecx, lo_x.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
@@ -1077,7 +1086,7 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         const double ngrid = linear_only ? 0.0 : (double)sweep_grid_rows(head, tail, min_span);
         const double sorted_b = linear_only ? 0.0 : 8.0 * n;  // bsort + bxsort
         size_t cap = (size_t)std::max(
-            1.0, budget / (4.0 * n + sorted_b + 56.0 * ngrid + 64.0 * m + 64.0));
+            1.0, budget / (4.0 * n + sorted_b + 24.0 * ngrid + 64.0 * m + 64.0));
         cap = std::min<size_t>(cap, 262144);
         const auto blocks = block_candidates(cx, cap);
         size_t maxPc = 0;
@@ -1093,8 +1102,6 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         a->hrow.ensure(sizeof(int) * maxPc);
         if (!linear_only) {
             a->scal.ensure(sizeof(double) * 3 *
-                           std::max<size_t>(1, maxPc * (size_t)sweep_grid_rows(head, tail, min_span)));
-            a->part.ensure(sizeof(double) * 4 *
                            std::max<size_t>(1, maxPc * (size_t)sweep_grid_rows(head, tail, min_span)));
             a->bsort.ensure(sizeof(float) * a->n * maxPc);
             a->bxsort.ensure(sizeof(float) * a->n * maxPc);

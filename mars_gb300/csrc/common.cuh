@@ -5,6 +5,8 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 
@@ -23,20 +25,24 @@ inline void cuda_check(cudaError_t e, const char *what, const char *file, int li
 #define CUDA_CHECK(x) ::mgpu::cuda_check((x), #x, __FILE__, __LINE__)
 #define LAUNCH_CHECK() ::mgpu::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
 
-// Allows a kernel the device's whole opt-in dynamic shared memory. The
-// attribute is per kernel and process-wide: setting it to each launch's own
-// size would race with concurrent handles launching the same kernel with
-// another size, so every caller sets the same (largest) value.
+// Raises a kernel's dynamic shared-memory limit to at least `bytes`. The
+// attribute is per kernel and process-wide, so concurrent handles launching
+// the same kernel with different sizes would race if each set its own size;
+// here it only ever grows (under a lock), to the largest size asked so far.
+// Not to the device maximum: a larger limit can make the driver pick a larger
+// shared-memory carveout and leave the kernel less L1 cache.
 template <class K>
-void allow_max_smem(K kernel)
+void allow_smem(K kernel, size_t bytes)
 {
-    int dev = 0, v = 0;
-    CUDA_CHECK(cudaGetDevice(&dev));
-    CUDA_CHECK(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    cudaFuncAttributes fa;
-    CUDA_CHECK(cudaFuncGetAttributes(&fa, kernel));  // less the kernel's static shared memory
-    CUDA_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    v - (int)fa.sharedSizeBytes));
+    static std::mutex mu;
+    static std::map<const void *, size_t> set;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = set[reinterpret_cast<const void *>(kernel)];
+    if (bytes > cur) {
+        CUDA_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)bytes));
+        cur = bytes;
+    }
 }
 
 inline size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }

@@ -849,12 +849,12 @@ void fast_project(cudaStream_t st, const FillSrc &src, const float *BoC, int n, 
         const dim3 g2((unsigned)ceil_div(n, FP_ROWS), (unsigned)ceil_div(P, FP_COLS));
         if (pass == 0) {
             if (psmem > 48 * 1024) {
-                allow_max_smem(k_fast_project<FillSrc>);
+                allow_smem(k_fast_project<FillSrc>, psmem);
             }
             k_fast_project<FillSrc><<<g2, FP_THREADS, psmem, st>>>(src, BoC, n, m, P, ws.T, ws.Bx);
         } else {
             if (psmem > 48 * 1024) {
-                allow_max_smem(k_fast_project<StoredSrc>);
+                allow_smem(k_fast_project<StoredSrc>, psmem);
             }
             k_fast_project<StoredSrc><<<g2, FP_THREADS, psmem, st>>>(stored, BoC, n, m, P, ws.T,
                                                                    ws.Bx);
@@ -912,7 +912,7 @@ void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int
     const int mid = fast_sweep_mid(head, tail, n);
 #define LAUNCH_FS(CPL, S)                                                                      \
     do {                                                                                       \
-        allow_max_smem(k_fast_sweep<CPL, S>);                                                  \
+        allow_smem(k_fast_sweep<CPL, S>, smem);                                                \
         k_fast_sweep<CPL, S><<<ntasks, 32 * (warps + 2), smem, st>>>(                          \
             reinterpret_cast<const FastTask *>(tasks), perm, xsort, ysort, cols, BoR, ldbo,    \
             ybo, ybx, mom, n, m, head, tail, mid, min_span, tol, cut_rel, hsse, hrow, hflag);  \

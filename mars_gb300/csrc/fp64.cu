@@ -1257,7 +1257,7 @@ void tgemm_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, int
     case K: {                                                                                \
         const size_t smem = TgemmSmem<BoT, K, Src::kRaw>::total;                             \
         if (smem > 48 * 1024) {                                                              \
-            allow_max_smem(k_tgemm<Src, BoT, K>);                                            \
+            allow_smem(k_tgemm<Src, BoT, K>, smem);                                            \
         }                                                                                    \
         k_tgemm<Src, BoT, K><<<dim3(gx, gy), TG_THREADS, smem, st>>>(src, Bo, ldbo, n, m, P, T); \
         break;                                                                               \
@@ -1305,7 +1305,7 @@ void project_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, i
     const int rb = (int)ceil_div(n, PJ_THREADS);
     const size_t smem = sizeof(double) * PJ_COLS * std::max(m, 1);
     if (smem > 48 * 1024) {
-        allow_max_smem(k_project<Src, BoT>);
+        allow_smem(k_project<Src, BoT>, smem);
     }
     verify(ceil_div(P, PJ_COLS) <= 65535, "too many candidate columns for one launch", 2);
     k_project<Src, BoT><<<dim3(rb, (unsigned)ceil_div(P, PJ_COLS)), PJ_THREADS, smem, st>>>(
@@ -1429,7 +1429,7 @@ void hinge_scalars(cudaStream_t st, const SweepTask *tasks, int ntasks, const fl
     if (ntasks <= 0) {
         return;
     }
-    allow_max_smem(k_hinge_scalars);
+    allow_smem(k_hinge_scalars, ScSmem::total);
     k_hinge_scalars<<<ntasks, SC_THREADS, ScSmem::total, st>>>(
         tasks, xsort, ysort, bs, n, head, tail, min_span, sweep_grid_rows(head, tail, min_span),
         scal);
@@ -1462,7 +1462,7 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
     const int comps = m + 1;
 #define LAUNCH_SWEEP(CPL, S)                                                                   \
     do {                                                                                       \
-        allow_max_smem(k_sweep<CPL, S>);                                                       \
+        allow_smem(k_sweep<CPL, S>, smem);                                                     \
         k_sweep<CPL, S><<<ntasks, 32 * (warps + 1), smem, st>>>(                               \
             tasks, perm, xsort, bs, bxs, Bo, ldbo, ybo, ybx, scal, ngrid, n, m, head, tail,    \
             min_span, tol, hsse, hrow, part);                                                  \
