@@ -394,6 +394,24 @@ void ensure_sorted(mars_gpu_algo *a, const std::vector<int> &cols)
     }
 }
 
+// Bytes of per-step scratch one eval may use (MARS_GPU_BLOCK_GB, default 45 %
+// of the device's memory). A step whose candidates do not fit runs as several
+// blocks, and on the FP64 path every block pays the full latency of its serial
+// chains again, so the default is large.
+double block_budget()
+{
+    const char *v = std::getenv("MARS_GPU_BLOCK_GB");
+    if (v && *v) {
+        return std::atof(v) * 1e9;
+    }
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return 32e9;
+    }
+    return 0.45 * (double)tot;
+}
+
 // The FP64 evaluation of candidates [0, Pc) (device arrays cx/cb) on the
 // context c. Fills c's ybx, and hsse/hrow unless linear_only. count_work: add
 // the algorithmic FLOPs, bytes and knot evaluations to c's counters (not for
@@ -617,7 +635,7 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         return;
     }
     const int ks = fast_ksplit(n);
-    const double budget = env_double("MARS_GPU_BLOCK_GB", 32.0) * 1e9;
+    const double budget = block_budget();
     const double ngrid = linear_only ? 0.0 : (double)sweep_grid_rows(head, tail, min_span);
     (void)ngrid;
     const double per = 4.0 * n + 4.0 * m * (ks + 1) + 64.0;
@@ -1080,7 +1098,7 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
         if (!linear_only) {
             ensure_sorted(a, cols);
         }
-        const double budget = env_double("MARS_GPU_BLOCK_GB", 32.0) * 1e9;
+        const double budget = block_budget();
         // Candidate columns per block: the Bx scratch budget, and at most
         // 2^18 so every per-column grid dimension stays within 65535 blocks.
         const double ngrid = linear_only ? 0.0 : (double)sweep_grid_rows(head, tail, min_span);
