@@ -91,3 +91,47 @@ def test_mixed_matches_fp64_on_a_fit_with_default_tail(gpu):
         stats[prec] = hold["a"].stats()
     np.testing.assert_equal(paths["mixed"], paths["fp64"])
     assert stats["mixed"]["redecided"] < stats["mixed"]["candidates"] // 2
+
+
+@pytest.mark.parametrize("name", ["hinge_search_small", "precision_stress_small", "default_tail",
+                                  "batched_small_1"])
+def test_mixed_with_speculation_keeps_golden_path(name, gpu, monkeypatch):
+    """MARS_GPU_MIXED_SPEC=1: the previous contenders are evaluated exactly
+    beside the fast pass; the term path must not change."""
+    monkeypatch.setenv("MARS_GPU_PRECISION", "mixed")
+    monkeypatch.setenv("MARS_GPU_MIXED_SPEC", "1")
+    g = load_fit(name)
+    X, y, w, kw = cases.fit_case(name)
+    model = mars.fit(X, y, w, **kw)
+    assert_same_path(model, g)
+
+
+def test_rank_only_values_track_fp64(gpu, monkeypatch):
+    """MARS_GPU_MIXED_RANK_ONLY=1 returns the fast values as they are (NaN cut
+    where a candidate is flagged). Unflagged candidates within half of the best
+    exact hinge score agree with the FP64 values to 1e-3 relative."""
+    from mars_gb300 import marslib
+
+    X, y, w, kw = cases.fit_case("hinge_search_small")
+    if w is None:
+        w = np.ones(len(y), np.float32)
+    g = load_fit("hinge_search_small")
+    mt = kw.get("max_terms", 31)
+    out = {}
+    for mode in ("fp64", "rank"):
+        monkeypatch.setenv("MARS_GPU_MIXED_RANK_ONLY", "1" if mode == "rank" else "0")
+        a = marslib.MarsAlgo(X, y, w, mt)
+        a.set_precision("fp64" if mode == "fp64" else "mixed")
+        for r in g["model"][1:9]:
+            a.append(r["type"], int(r["input"]), int(r["basis"]),
+                     float("nan") if r["hinge"] is None else r["hinge"])
+        mask = np.ones((X.shape[1], a.nbasis()), bool)
+        out[mode] = a.eval(mask, 6, 1, False, 1)
+    _, l0, h0, _ = out["fp64"]
+    _, l1, h1, c1 = out["rank"]
+    flagged = np.isnan(c1)
+    assert flagged.sum() < flagged.size
+    ok = ~flagged & (h0 >= 0.5 * h0[~flagged].max())
+    assert ok.any()
+    np.testing.assert_allclose(h1[ok], h0[ok], rtol=1e-3)
+    np.testing.assert_allclose(l1, l0, rtol=1e-3, atol=1e-9 * l0.max())
