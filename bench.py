@@ -138,6 +138,9 @@ def gpu_fit(X, y, kw, precision):
     model = forward_pass(lib, X, y, None, **kw)
     wall = time.perf_counter() - t0
     st = lib.algo.stats()
+    # after the timed fit: max |Q^T Q - I| of the final basis (the basis only
+    # grows, so this is the largest over the fit's steps) and its FP64 RSS
+    st["orth_max"], st["rss"] = lib.algo.orth_error()
     return model, wall, st, lib.knot_evals
 
 
@@ -513,6 +516,7 @@ def main():
                                "ms_append", "ms_sort", "ms_redecide", "ms_gather",
                                "ms_redecide_gpu")},
         "clocks": clk,
+        "orthogonality": {"max_abs_QtQ_minus_I": st["orth_max"], "rss": st["rss"]},
     }
     if args.precision == "mixed":
         line["redecided_fraction"] = agg["redecided"] / max(1, agg["candidates"])
@@ -526,6 +530,9 @@ def main():
                         "value": line["knot_evals_per_step"] / statistics.mean(fp_spans),
                         "speedup": statistics.mean(fp_spans) / (t_dev / args.steps)}
         line["term_path_identical_to_fp64"] = path_of(model) == path_of(fp_model)
+        line["orthogonality"]["fp64_max_abs_QtQ_minus_I"] = st["orth_max"]
+        line["orthogonality"]["rss_rel_err_vs_fp64"] = (
+            abs(line["orthogonality"]["rss"] - st["rss"]) / max(abs(st["rss"]), 1e-300))
     golden = os.path.join(ROOT, "tests", "golden", args.workload + ".json")
     if os.path.isfile(golden):
         with open(golden) as f:
