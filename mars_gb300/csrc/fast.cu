@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(256) k_parent_moments(FillSrc src, int n, doub
 //   den = A0 + D (A1 + D A2) + kl - 2 (Fe + D Ge) - ee,   uw = B0 + D B1 + ey - e_y,
 // Fe = sum F_c e_c, Ge = sum G_c e_c, ee = sum e_c^2, ey = sum yc_c e_c.
 // ---------------------------------------------------------------------------
-constexpr int FS_ROWS = 32, FS_CHUNK = 2, FS_SNAP = 32, FS_HIST = 6, FS_NSUM = 5, FS_MAXW = 8;
+constexpr int FS_ROWS = 32, FS_CHUNK = 2, FS_SNAP = 32, FS_HIST = 4, FS_NSUM = 5, FS_MAXW = 8;
 constexpr int FS_RS = FS_ROWS + 1;  // stride of the staged per-row arrays: each in its own banks
 
 using FastTask = FastTaskRec;  // dir 0: forward (first half of the cuts), 1: mirror (second half)
@@ -871,26 +871,50 @@ void fast_project(cudaStream_t st, const FillSrc &src, const float *BoC, int n, 
 
 static size_t fast_sweep_smem(int m, int w, int stages) { return FastSweepSmem(m, w, stages).total; }
 
-// Two blocks per SM when their shared memory allows (the kernel is bounded to
-// 96 registers for that); fewer candidate warps per block when the tasks are few.
-constexpr size_t FS_SMEM_2 = 113 * 1024;
+// Resident blocks per SM for W candidate warps and S stages: shared memory
+// (228 KB per SM, 1 KB of it reserved per block) and registers (the kernel is
+// bounded to 96 per thread).
+static int fast_sweep_bps(int m, int w, int stages)
+{
+    const size_t sm = fast_sweep_smem(m, w, stages) + 1024;
+    const int by_smem = (int)((228 * 1024) / sm);
+    const int by_regs = 65536 / (96 * 32 * (w + 2));
+    return std::max(0, std::min(std::min(by_smem, by_regs), 32));
+}
+
+// The stage depth: four unless two lets more blocks reside.
+static int fast_sweep_stages(int m, int w)
+{
+    return fast_sweep_bps(m, w, 2) > fast_sweep_bps(m, w, 4) ? 2 : 4;
+}
 
 int fast_sweep_warps(int m, const std::vector<int> &group_sizes)
 {
-    // the most candidates per block (loaders amortised) that still gives
-    // every SM two blocks, else the fewest
-    auto blocks = [&](int w) {
-        long b = 0;
-        for (int g : group_sizes) {
-            b += 2 * ((g + w - 1) / w);
+    // Each candidate warp walks half the sorted rows one after another, so the
+    // launch takes about (waves of blocks) x (one walk): choose the block
+    // width with the fewest waves on 152 SMs, and among those the widest
+    // (fewer loader warps per candidate).
+    int best_w = 1;
+    long best_waves = -1;
+    for (int w : {FS_MAXW, 4, 2, 1}) {
+        if (fast_sweep_smem(m, w, 2) > 227 * 1024) {
+            continue;
         }
-        return b;
-    };
-    int w = FS_MAXW;
-    while (w > 1 && (blocks(w) < 2 * 152 || fast_sweep_smem(m, w, 2) > FS_SMEM_2)) {
-        w = w > 4 ? 4 : w - 1;
+        const int bps = fast_sweep_bps(m, w, fast_sweep_stages(m, w));
+        if (bps == 0) {
+            continue;
+        }
+        long blocks = 0;
+        for (int g : group_sizes) {
+            blocks += 2 * ((g + w - 1) / w);
+        }
+        const long waves = (blocks + 152L * bps - 1) / (152L * bps);
+        if (best_waves < 0 || waves < best_waves) {
+            best_waves = waves;
+            best_w = w;
+        }
     }
-    return w;
+    return best_w;
 }
 
 void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int *perm,
@@ -905,7 +929,7 @@ void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int
     }
     const int warps = warps_per_block;
     verify(warps >= 1 && warps <= FS_MAXW, "sweep block size out of range", 2);
-    const int stages = fast_sweep_smem(m, warps, 4) <= FS_SMEM_2 ? 4 : 2;
+    const int stages = fast_sweep_stages(m, warps);
     const size_t smem = fast_sweep_smem(m, warps, stages);
     verify(smem <= 227 * 1024, "too many basis functions for the fast hinge sweep");
     const int nc = m + 3;
