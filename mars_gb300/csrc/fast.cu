@@ -333,7 +333,7 @@ struct FastSweepSmem {
 };
 
 template <int CPL, int S>
-__global__ void __launch_bounds__(32 * (FS_MAXW + 2), 2)
+__global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
     k_fast_sweep(const FastTask *__restrict__ tasks, const int *__restrict__ perm,
                  const float *__restrict__ xsort, const float *__restrict__ ysort,
                  const FastSweepCols cols,
@@ -872,14 +872,29 @@ void fast_project(cudaStream_t st, const FillSrc &src, const float *BoC, int n, 
 static size_t fast_sweep_smem(int m, int w, int stages) { return FastSweepSmem(m, w, stages).total; }
 
 // Resident blocks per SM for W candidate warps and S stages: shared memory
-// (228 KB per SM, 1 KB of it reserved per block) and registers (the kernel is
-// bounded to 96 per thread).
+// (228 KB per SM, 1 KB of it reserved per block) and registers.
+static int fast_sweep_regs();
+
 static int fast_sweep_bps(int m, int w, int stages)
 {
     const size_t sm = fast_sweep_smem(m, w, stages) + 1024;
     const int by_smem = (int)((228 * 1024) / sm);
-    const int by_regs = 65536 / (96 * 32 * (w + 2));
+    const int by_regs = 65536 / (fast_sweep_regs() * 32 * (w + 2));
     return std::max(0, std::min(std::min(by_smem, by_regs), 32));
+}
+
+// Registers per thread of the sweep kernel (the instances differ little).
+static int fast_sweep_regs()
+{
+    static int regs = 0;
+    if (regs == 0) {
+        cudaFuncAttributes fa;
+        regs = cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4>) == cudaSuccess
+                   ? std::max(fa.numRegs, 32)
+                   : 168;
+        cudaGetLastError();
+    }
+    return regs;
 }
 
 // The stage depth: four unless two lets more blocks reside.
