@@ -45,10 +45,20 @@ def test_golden_term_path_gpu(name, precision, gpu, monkeypatch):
     assert_same_path(model, g)
 
 
+# How the FP64 sweep scores its cuts: "deferred" (partial scores stored, the ybx
+# chain beside the sweep; steps whose partial scores stay under
+# MARS_GPU_DEFER_BYTES) or "direct" (ybx first; the larger steps).
+SCORING = {"deferred": None, "direct": "0"}
+
+
+@pytest.mark.parametrize("scoring", sorted(SCORING))
 @pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("name", cases.EVAL_CASES)
-def test_eval_matches_oracle(name, precision, gpu, port):
+def test_eval_matches_oracle(name, precision, scoring, gpu, port, monkeypatch):
     import oracle
+
+    if SCORING[scoring] is not None:
+        monkeypatch.setenv("MARS_GPU_DEFER_BYTES", SCORING[scoring])
 
     X, y, w, appends, evals = cases.eval_case(name)
     a_gpu = gpu.MarsAlgo(X, y, w, cases.EVAL_MAX_TERMS)
@@ -70,6 +80,16 @@ def test_eval_matches_oracle(name, precision, gpu, port):
     mx, rss = a_gpu.orth_error()
     assert mx < 1e-5
     assert rss == pytest.approx(1 - a_gpu.dsse(), rel=1e-6)
+
+
+@pytest.mark.parametrize("name", ["hinge_search", "precision_stress_small", "weighted_nan"])
+def test_golden_term_path_direct_scoring(name, gpu, monkeypatch):
+    monkeypatch.setenv("MARS_GPU_PRECISION", "fp64")
+    monkeypatch.setenv("MARS_GPU_DEFER_BYTES", "0")
+    g = load_fit(name)
+    X, y, w, kw = cases.fit_case(name)
+    model = mars.fit(X, y, w, **kw)
+    assert_same_path(model, g)
 
 
 def test_delta_sse_gpu(be_gpu):
