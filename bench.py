@@ -349,6 +349,9 @@ def run_reference(args):
     return 0
 
 
+BATCH_THREADS = int(os.environ.get("MARS_BENCH_BATCH_THREADS", "16"))
+
+
 def run_batched(args):
     """Config 4: fits/s over 256 independent fits driven concurrently."""
     from mars_gb300 import batch, marslib, workloads
@@ -362,7 +365,7 @@ def run_batched(args):
     t0 = time.perf_counter()
     walls = []
     for _ in range(args.steps):
-        _, per = batch.fit_many(probs, threads=16, precision=args.precision)
+        _, per = batch.fit_many(probs, threads=BATCH_THREADS, precision=args.precision)
         walls.append(time.perf_counter() - t0)
         t0 = time.perf_counter()
     clk = clocks.stop()

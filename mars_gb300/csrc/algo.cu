@@ -173,6 +173,10 @@ struct SpecLane {
             ss.create();
             timer.st = ss.st;
             timer.redirect = PH_REDECIDE_GPU;
+            for (DevBuf *b : {&Bx, &T, &svec, &snew, &ybx, &hsse, &hrow, &fired, &nfired, &tasks,
+                              &stasks, &scal, &bsort, &bxsort, &cand, &part}) {
+                b->bind(ss.st);
+            }
         }
     }
     Fp64Ctx ctx()
@@ -291,6 +295,13 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     std::memset(&a->stats, 0, sizeof(a->stats));
     a->ss.create();
     a->st = a->ss.st;
+    for (DevBuf *b : {&a->X, &a->s, &a->y, &a->B, &a->Bo, &a->BoF, &a->BoC, &a->ybo_d, &a->perm,
+                      &a->xsort, &a->ysort, &a->Bx, &a->T, &a->svec, &a->snew, &a->ybx,
+                      &a->hsse, &a->hrow, &a->cand, &a->fired, &a->nfired, &a->out, &a->tasks,
+                      &a->stasks, &a->scal, &a->part, &a->bsort, &a->bxsort, &a->fTp, &a->fT,
+                      &a->fmom, &a->hflag, &a->sort_keys, &a->sort_vals, &a->sort_tmp}) {
+        b->bind(a->st);
+    }
     CUDA_CHECK(cudaEventCreate(&a->span_begin));
     CUDA_CHECK(cudaEventCreate(&a->span_end));
     a->timer.st = a->st;

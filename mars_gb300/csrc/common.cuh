@@ -48,18 +48,58 @@ void allow_smem(K kernel, size_t bytes)
 inline size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
 inline size_t round_up(size_t a, size_t b) { return ceil_div(a, b) * b; }
 
-// Grow-only device buffer.
+// The library's memory pool on the current device: stream-ordered
+// allocations, so that a fit's buffers come and go without the device-wide
+// synchronisation of cudaMalloc / cudaFree (which would stall every other
+// fit running concurrently). Up to 8 GB of freed memory stays cached in it.
+inline cudaMemPool_t device_pool()
+{
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    int dev = 0;
+    CUDA_CHECK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = pools.find(dev);
+    if (it != pools.end()) {
+        return it->second;
+    }
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool;
+    CUDA_CHECK(cudaMemPoolCreate(&pool, &props));
+    unsigned long long keep = 8ull << 30;
+    CUDA_CHECK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    pools[dev] = pool;
+    return pool;
+}
+
+// Grow-only device buffer. Bound to a stream (bind), it is allocated from
+// the library's pool and freed in that stream's order; unbound, with
+// cudaMalloc / cudaFree.
 struct DevBuf {
     void *ptr = nullptr;
     size_t bytes = 0;
+    cudaStream_t st = nullptr;
+    bool bound = false;
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
+    void bind(cudaStream_t s)
+    {
+        st = s;
+        bound = true;
+    }
     void release()
     {
         if (ptr) {
-            cudaFree(ptr);
+            if (bound) {
+                cudaFreeAsync(ptr, st);
+            } else {
+                cudaFree(ptr);
+            }
         }
         ptr = nullptr;
         bytes = 0;
@@ -73,7 +113,8 @@ struct DevBuf {
         if (want == 0) {
             return;
         }
-        cudaError_t e = cudaMalloc(&ptr, want);
+        cudaError_t e = bound ? cudaMallocFromPoolAsync(&ptr, want, device_pool(), st)
+                              : cudaMalloc(&ptr, want);
         if (e != cudaSuccess) {
             cudaGetLastError();  // clear the sticky-free allocation error
             ptr = nullptr;
