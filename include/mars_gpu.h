@@ -88,6 +88,8 @@ typedef struct {
     long long redecided_spec;   /* mixed mode: re-decided candidates the speculation covered */
     long long leftovers;        /* mixed mode: candidates evaluated exactly after the fast pass */
     long long leftovers_flagged; /* ... of which carried a flag */
+    long long evals_exact;      /* mixed mode: evals run on the exact path after a step that
+                                   re-decided most of its candidates */
 } mars_gpu_stats;
 
 /* Message of the last failing call on this thread ("" if none). */

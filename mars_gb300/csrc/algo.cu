@@ -222,6 +222,9 @@ struct mars_gpu_algo {
     SpecLane spec;
     std::vector<long long> prev_contend;  // sorted (xcol << 32 | bcol) keys
     std::vector<long long> appended;      // (xcol << 32 | column) of appends since the last eval
+    // Mixed mode: steps left to run on the exact path directly, after a step
+    // that re-decided most of its candidates anyway.
+    int mixed_skip = 0;
 
     Fp64Ctx ctx()
     {
@@ -1079,13 +1082,29 @@ void eval_impl(mars_gpu_algo *a, const bool *mask, int rows, int mask_stride, in
     }
     const int P = (int)cx.size();
     a->stats.candidates += P;
-    if (a->precision == MARS_GPU_PREC_MIXED) {
+    // Mixed mode runs the fast pass unless a recent step re-decided more than
+    // MARS_GPU_MIXED_FALLBACK (default half) of its candidates exactly: then
+    // the next MARS_GPU_MIXED_FALLBACK_STEPS (7) steps take the exact path
+    // directly (same decisions, no wasted fast pass), and the fast pass is
+    // tried again.
+    const bool use_fast = a->precision == MARS_GPU_PREC_MIXED && a->mixed_skip == 0;
+    if (a->precision == MARS_GPU_PREC_MIXED && !use_fast) {
+        --a->mixed_skip;
+        a->stats.evals_exact += 1;
+    }
+    if (use_fast) {
         const int head = end_span;
         const int tail = head < n ? n - head : 0;
         if (P > 0 && !linear_only) {
             ensure_sorted(a, cols);
         }
+        const long long before = a->stats.redecided;
         eval_mixed(a, cx, cb, rows, min_span, head, tail, linear_only != 0, lin, hin, cut);
+        if (P > 0 && !linear_only &&
+            (double)(a->stats.redecided - before) >
+                env_double("MARS_GPU_MIXED_FALLBACK", 0.5) * (double)P) {
+            a->mixed_skip = (int)env_double("MARS_GPU_MIXED_FALLBACK_STEPS", 7.0);
+        }
         span_mark_end(a);
         sync(a);
         a->timer.resolve(a->phase_ms);
@@ -1306,6 +1325,7 @@ int mars_gpu_set_precision(mars_gpu_algo *a, int mode)
             a->sorted.assign(a->p, 0);  // re-sort so the host gets the permutations too
         }
         a->precision = mode;
+        a->mixed_skip = 0;
     });
 }
 

@@ -49,6 +49,7 @@ class Stats(ctypes.Structure):
         ("redecided_spec", ctypes.c_longlong),
         ("leftovers", ctypes.c_longlong),
         ("leftovers_flagged", ctypes.c_longlong),
+        ("evals_exact", ctypes.c_longlong),
     ]
 
     def as_dict(self):

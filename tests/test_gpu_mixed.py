@@ -18,9 +18,14 @@ from tests.test_oracle import assert_same_path, load_fit
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("fallback", ["default", "never"])
 @pytest.mark.parametrize("name", cases.FIT_CASES)
-def test_mixed_golden_term_path(name, gpu, monkeypatch):
+def test_mixed_golden_term_path(name, fallback, gpu, monkeypatch):
+    """fallback 'never': every step through the fast pass, however many of
+    its candidates need an exact re-decision."""
     monkeypatch.setenv("MARS_GPU_PRECISION", "mixed")
+    if fallback == "never":
+        monkeypatch.setenv("MARS_GPU_MIXED_FALLBACK", "2")
     g = load_fit(name)
     X, y, w, kw = cases.fit_case(name)
     model = mars.fit(X, y, w, **kw)
