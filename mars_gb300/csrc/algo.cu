@@ -551,7 +551,7 @@ void eval_block_fp64(mars_gpu_algo *a, Fp64Ctx &c, int Pc, const int *cx_d, cons
                a->Bo.as<double>(), a->ldbo, a->ybo_d.as<double>(), c.ybx->as<double>(),
                c.scal->as<double>(), n, m, head, tail, min_span, a->tol, c.hsse->as<double>(),
                c.hrow->as<int>(), warps, &c.stats->kernel_launches,
-               defer ? c.part->as<double>() : nullptr);
+               defer ? c.part->as<double>() : nullptr, sweep_split(m, Pc));
     if (defer) {
         CUDA_CHECK(cudaStreamWaitEvent(c.st, c.ev_ybx, 0));
         sweep_score(c.st, c.part->as<double>(), Pc, cx_d, a->perm.as<int>(),

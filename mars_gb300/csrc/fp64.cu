@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
             const double *__restrict__ ybo, const double *__restrict__ ybx,
             const double *__restrict__ scal, int ngrid, int n, int m, int head, int tail,
             int min_span, double tol, double *__restrict__ hsse, int *__restrict__ hrow,
-            double *__restrict__ part)
+            double *__restrict__ part, int split)
 {
     extern __shared__ __align__(16) unsigned char sraw[];
     const int W = (blockDim.x >> 5) - 1;  // candidate warps
@@ -468,7 +468,11 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
 
     const SweepTask task = tasks[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bool cwarp = warp < task.count;
+    // `split` warps share a candidate, each with its own components (lane +
+    // 32 (sub + split q)): a candidate's FP64 FMAs per row are spread over as
+    // many sub-partitions. Sub-warp 0 scores the cuts.
+    const int wc = warp / split, sub = warp - wc * split;
+    const bool cwarp = warp < task.count * split;
     const bool lwarp = warp == W;
     const int *pk = perm + (size_t)task.xcol * n;
     const float *xs = xsort + (size_t)task.xcol * n;
@@ -529,10 +533,10 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
             sq * SW_ROWS + lane > 0 ? (double)(xr[lane] - xr[lane + 1]) : 0.0;
     };
 
-    const int mycand = task.cand0 + (cwarp ? warp : 0);
+    const int mycand = task.cand0 + (cwarp ? wc : 0);
     const double ybx_c = part ? 0.0 : ybx[mycand];
     const double *mysc = scal + (size_t)mycand * ngrid * 3;
-    double *snap = snapbase + (size_t)(cwarp ? warp : 0) * SW_SNAP * ldF;
+    double *snap = snapbase + (size_t)(cwarp ? wc : 0) * SW_SNAP * ldF;
     double f[CPL], g[CPL];
 #pragma unroll
     for (int q = 0; q < CPL; ++q) {
@@ -545,7 +549,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
     int next_grid = head + 1;
 
     auto flush = [&]() {
-        if (cwarp) {
+        if (cwarp && sub == 0) {
             double sse = -1.0;
             int row = 0x7fffffff;
             if (lane < nsnap) {
@@ -622,8 +626,8 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
         }
         if (cwarp) {
             const double *cv = scvt + (size_t)h * NV * SW_ROWS;
-            const double *bw = cv + warp * SW_ROWS;
-            const double *xw = cv + (W + warp) * SW_ROWS;
+            const double *bw = cv + wc * SW_ROWS;
+            const double *xw = cv + (W + wc) * SW_ROWS;
             const double *dv = cv + 2 * W * SW_ROWS;
             const double *rowb = sbo + (size_t)sg * SW_ROWS * MP;
             int slot = nsnap;
@@ -633,7 +637,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
                 const double di = dv[r];  // 0 for the first row
 #pragma unroll
                 for (int q = 0; q < CPL; ++q) {
-                    const int c = lane + 32 * q;
+                    const int c = lane + 32 * (sub + split * q);
                     const double bv = rowp[min(c, m - 1)];  // unconditional load, then select
                     const double xv = c < m ? bv : (c == m ? bxk : 0.0);
                     f[q] = fma(di, g[q], f[q]);
@@ -643,7 +647,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
                     double *fs = snap + (size_t)slot * ldF;
 #pragma unroll
                     for (int q = 0; q < CPL; ++q) {
-                        const int c = lane + 32 * q;
+                        const int c = lane + 32 * (sub + split * q);
                         if (c <= m) {
                             fs[c] = f[q];
                         }
@@ -683,7 +687,7 @@ __global__ void __launch_bounds__(32 * (SW_MAXW + 1), 1)
     if (nsnap > 0) {
         flush();
     }
-    if (cwarp && lane == 0 && !part) {
+    if (cwarp && sub == 0 && lane == 0 && !part) {
         hsse[mycand] = best;
         hrow[mycand] = besti >= 0 ? pk[besti] : -1;
     }
@@ -1376,18 +1380,28 @@ void scale_columns(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const 
 // is 4 stages deep when it fits in 200 KB with the snapshots, else 2.
 static size_t sweep_smem(int m, int w, int stages) { return SweepSmem(m, w, stages).total; }
 
+int sweep_split(int m, int candidates)
+{
+    // More than 32 components put 2 FMAs per component slot and row on a
+    // warp; with few candidates (the sweep is then a latency-bound walk, not
+    // FP64-pipe bound) two warps share each candidate instead.
+    return m + 1 > 32 && candidates <= 2 * 152 ? 2 : 1;
+}
+
 int sweep_warps(int m, int candidates)
 {
     // Each candidate warp issues two dependent FP64 FMAs per row and an SM
     // sub-partition's FP64 pipe takes one warp instruction per ~64 cycles, so
-    // a candidate warp wants a sub-partition of its own: 4 candidates per
+    // a candidate warp wants a sub-partition of its own: 4 candidate warps per
     // block (warps map to sub-partitions by index mod 4; the light loader
     // shares one), one block per SM up to 4 x 152 candidates, then 5.
+    // Returns candidates per block: warps / sweep_split.
+    const int split = sweep_split(m, candidates);
     int w = candidates <= 4 * 152 ? 4 : SW_MAXW;
-    while (w > 1 && sweep_smem(m, w, 2) > 200 * 1024) {
+    while (w > split && sweep_smem(m, w, 2) > 200 * 1024) {
         --w;
     }
-    return w;
+    return std::max(1, w / split);
 }
 
 int sweep_grid_rows(int head, int tail, int min_span)
@@ -1441,12 +1455,13 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
                 const float *xsort, const float *bs, const float *bxs, const double *Bo,
                 size_t ldbo, const double *ybo, const double *ybx, const double *scal, int n,
                 int m, int head, int tail, int min_span, double tol, double *hsse, int *hrow,
-                int warps_per_block, long long *launches, double *part)
+                int warps_per_block, long long *launches, double *part, int split)
 {
     if (ntasks <= 0) {
         return;
     }
-    const int warps = warps_per_block;
+    verify(split >= 1 && split <= 4, "sweep split out of range", 2);
+    const int warps = warps_per_block * split;
     verify(warps >= 1 && warps <= SW_MAXW, "sweep block size out of range", 2);
     const int stages = sweep_smem(m, warps, 4) <= 200 * 1024 ? 4 : 2;
     const size_t smem = sweep_smem(m, warps, stages);
@@ -1459,13 +1474,13 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
                            " basis functions");
     }
     const int ngrid = sweep_grid_rows(head, tail, min_span);
-    const int comps = m + 1;
+    const int comps = (m + split) / split;  // components per warp: ceil((m + 1) / split)
 #define LAUNCH_SWEEP(CPL, S)                                                                   \
     do {                                                                                       \
         allow_smem(k_sweep<CPL, S>, smem);                                                     \
         k_sweep<CPL, S><<<ntasks, 32 * (warps + 1), smem, st>>>(                               \
             tasks, perm, xsort, bs, bxs, Bo, ldbo, ybo, ybx, scal, ngrid, n, m, head, tail,    \
-            min_span, tol, hsse, hrow, part);                                                  \
+            min_span, tol, hsse, hrow, part, split);                                           \
     } while (0)
 #define LAUNCH_CPL(CPL)            \
     do {                           \

@@ -95,8 +95,8 @@ void normalize_ybx(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const 
 void scale_columns(cudaStream_t st, float *Bx, size_t ldBx, int n, int P, const double *s,
                    double tol, long long *launches);
 
-// Candidates per hinge-sweep block (one warp each) for m live basis columns
-// and `candidates` candidates in the launch.
+// Candidates per hinge-sweep block for m live basis columns and `candidates`
+// candidates in the launch (sweep_split warps each).
 int sweep_warps(int m, int candidates);
 
 // Number of grid rows (cut candidates) of the sweep: rows head+1, head+1+min_span, ... < tail.
@@ -131,7 +131,12 @@ void sweep_fp64(cudaStream_t st, const SweepTask *tasks, int ntasks, const int *
                 const float *xsort, const float *bs, const float *bxs, const double *Bo,
                 size_t ldbo, const double *ybo, const double *ybx, const double *scal, int n,
                 int m, int head, int tail, int min_span, double tol, double *hsse, int *hrow,
-                int warps_per_block, long long *launches, double *part = nullptr);
+                int warps_per_block, long long *launches, double *part = nullptr,
+                int split = 1);
+
+// Warps per candidate of the FP64 sweep (1 or 2) for m basis columns and
+// `candidates` candidates in the launch; sweep_warps already accounts for it.
+int sweep_split(int m, int candidates);
 
 // The scores of the deferred sweep (the reference's: fy = fy_partial + f_m ybx
 // as the chain's last fused step, uw = fy - w, sse = den > tol ? uw^2 / (den +

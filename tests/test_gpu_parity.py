@@ -233,3 +233,38 @@ def test_fit_with_weights_and_nan_target(gpu, port_lib):
                  None if np.isnan(r["hinge"]) else float(r["hinge"])) for r in model]
 
     assert path(m_g) == path(m_c)
+
+
+@pytest.mark.parametrize("defer", ["deferred", "direct"])
+def test_wide_basis_matches_oracle(gpu, port, defer, monkeypatch):
+    """More than 31 basis columns: the FP64 sweep then gives a candidate two
+    component slots per lane, or, with few candidates, two warps. Bit-exact
+    against the oracle either way, scored deferred or directly."""
+    import oracle
+
+    if defer == "direct":
+        monkeypatch.setenv("MARS_GPU_DEFER_BYTES", "0")
+    rng = np.random.default_rng(40)
+    n, p = 3000, 6
+    X, y, w = _rand_problem(n, p, 40)
+    a_g = gpu.MarsAlgo(X, y, w, 48)
+    a_c = oracle.OracleAlgo(X, y, w, 48, kind="port")
+    for _ in range(400):
+        if a_c.nbasis() >= 40:
+            break
+        j = int(rng.integers(p))
+        b = int(rng.integers(a_c.nbasis()))
+        t = float(X[int(rng.integers(n)), j])
+        ap = ("+" if rng.random() < 0.5 else "-", j, b, t)
+        assert a_g.append(*ap) == a_c.append(*ap)
+    assert a_g.nbasis() == a_c.nbasis() >= 33
+    m = a_c.nbasis()
+    for cands in (3, 60):  # a few candidates (two warps each), then many (one warp)
+        mask = np.zeros((p, m), bool)
+        picks = rng.choice(p * m, size=cands, replace=False)
+        mask.flat[picks] = True
+        rg = a_g.eval(mask, 3, 2, False, 1)
+        rc = a_c.eval(mask, 3, 2, False, 1)
+        assert rg[0] == rc[0]
+        for k in (1, 2, 3):
+            np.testing.assert_array_equal(rg[k], rc[k])
