@@ -266,7 +266,7 @@ def roofline(st, workload_name, precision):
                 "limiter": ("FP64 pipe (ncu: 57% active) and FP64 dependency latency; DRAM < 1% "
                             "of peak" if precision == "fp64" else
                             "latency of each warp's sequential walk over the sorted rows "
-                            "(ncu: issue 32% active, no FP64, DRAM 6% of peak)")}
+                            "(ncu: issue 38% active, no FP64, DRAM 6% of peak)")}
     ms = max(st["ms_project"], 1e-9)
     ach = st["project_flops"] / (ms * 1e-3) / 1e12
     return {"kernel": "projection", "bound": "tensor", "achieved": ach, "peak": bf16,

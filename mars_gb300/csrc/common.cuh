@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <map>
 #include <mutex>
+#include <utility>
 #include <stdexcept>
 #include <string>
 
@@ -35,9 +36,11 @@ template <class K>
 void allow_smem(K kernel, size_t bytes)
 {
     static std::mutex mu;
-    static std::map<const void *, size_t> set;
+    static std::map<std::pair<int, const void *>, size_t> set;  // (device, kernel) -> bytes
+    int dev = 0;
+    CUDA_CHECK(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> lock(mu);
-    size_t &cur = set[reinterpret_cast<const void *>(kernel)];
+    size_t &cur = set[{dev, reinterpret_cast<const void *>(kernel)}];
     if (bytes > cur) {
         CUDA_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)bytes));

@@ -886,14 +886,14 @@ static int fast_sweep_bps(int m, int w, int stages)
 // Registers per thread of the sweep kernel (the instances differ little).
 static int fast_sweep_regs()
 {
-    static int regs = 0;
-    if (regs == 0) {
+    static const int regs = [] {
         cudaFuncAttributes fa;
-        regs = cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4>) == cudaSuccess
-                   ? std::max(fa.numRegs, 32)
-                   : 168;
+        const int r = cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4>) == cudaSuccess
+                          ? std::max(fa.numRegs, 32)
+                          : 168;
         cudaGetLastError();
-    }
+        return r;
+    }();
     return regs;
 }
 
