@@ -4,6 +4,7 @@
 // candidate); long reductions over rows are split deterministically
 // (fixed per-thread order, fixed block tree, fixed order across blocks).
 #include "fp64.cuh"
+#include "xchain.cuh"
 
 #include <type_traits>
 
@@ -11,6 +12,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 namespace mgpu {
@@ -269,6 +271,87 @@ __global__ void __launch_bounds__(CC_THREADS) k_colchain(Op op, int n, int P, do
     }
     if (warp == 0 && lane < ncols) {
         out[j0 + lane] = acc;
+    }
+}
+
+// The same column chains, exact and parallel over the rows (xchain.cuh): one
+// block per chain, one chunk of L consecutive rows per thread. Each thread sums
+// its chunk in float-float; a block scan of those sums guesses every chunk's
+// entry value; each thread runs its chunk XC_RUNS times from its guess (thread
+// 0 runs chunk 0 once, from the true start 0); thread 0 then walks the chunks in
+// order, translating a run's end or re-running the chunk. The value equals the
+// chain k_colchain runs, bit for bit.
+constexpr int XC_MAXK = 512;
+
+template <class Op>
+__global__ void __launch_bounds__(XC_MAXK) k_xchain(Op op, int n, int L, double *__restrict__ out)
+{
+    __shared__ XcChunk ch[XC_MAXK];
+    __shared__ double wsum[XC_MAXK / 32];
+    const int j = blockIdx.x, t = threadIdx.x, K = blockDim.x;
+    const int lane = t & 31, warp = t >> 5, nw = K >> 5;
+    const float *col = op.column(j);
+    const float *yc = op.ycolumn();
+    const float prm = op.param(j);
+    const auto term = [&](int i, float &a, float &b) {
+        const float v = op.value(__ldg(col + i), prm);
+        a = v;
+        if constexpr (Op::kUsesY) {
+            b = __ldg(yc + i);
+        } else {
+            b = v;
+        }
+    };
+    const int i0 = (int)min((long long)n, (long long)t * L), i1 = min(n, i0 + L);
+
+    XcGuess g;
+    for (int i = i0; i < i1; ++i) {
+        float a, b;
+        term(i, a, b);
+        g.add_product(a, b);
+    }
+    const double v = g.value();
+    double inc = v;  // inclusive prefix within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) {
+            inc += u;
+        }
+    }
+    if (lane == 31) {
+        wsum[warp] = inc;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        double w = lane < nw ? wsum[lane] : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) {
+                w += u;
+            }
+        }
+        if (lane < nw) {
+            wsum[lane] = w;
+        }
+    }
+    __syncthreads();
+    const double guess = (inc - v) + (warp > 0 ? wsum[warp - 1] : 0.0);
+    double acc = 0.0;
+    if (t == 0) {
+        acc = xc_run(term, i0, i1, 0.0);
+    } else {
+        xc_speculate(term, i0, i1, guess, ch[t]);
+    }
+    __syncthreads();
+    if (t == 0) {
+        for (int c = 1; c < K; ++c) {
+            const int c0 = (int)min((long long)n, (long long)c * L), c1 = min(n, c0 + L);
+            bool redone = false;
+            acc = xc_resolve(term, c0, c1, ch[c], acc, &redone);
+        }
+        out[j] = acc;
     }
 }
 
@@ -1286,13 +1369,44 @@ TG_INST(StoredSrc, float)
 TG_INST(StoredSrc, double)
 #undef TG_INST
 
+// Chunks per chain for k_xchain, or 0 where k_colchain is the faster form.
+// Costs in SM cycles over the GPU: a chain as written takes ~70 cycles a row;
+// FP64 throughput is ~2 FMAs per cycle per SM; k_xchain issues XC_RUNS + 1 FMAs
+// per element and its walk takes ~450 cycles a chunk. MARS_GPU_XCHAIN = 0 or 1
+// forces either kernel.
+int xchain_chunks(int n, int P)
+{
+    const char *fv = std::getenv("MARS_GPU_XCHAIN");
+    const int force = fv && *fv ? std::atoi(fv) : -1;
+    if (n <= 0 || force == 0) {
+        return 0;
+    }
+    const int K = (int)std::min<size_t>(XC_MAXK, std::max<size_t>(32, round_up(ceil_div(n, 2048), 32)));
+    if (force == 1) {
+        return K;
+    }
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) {
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const double fp64 = 2.0 * std::max(1, sms);
+    const double plain = std::max(70.0 * n, (double)P * n / fp64);
+    const double chunked = (XC_RUNS + 1.0) * P * n / fp64 + 450.0 * K;
+    return chunked < 0.7 * plain ? K : 0;
+}
+
 template <class Op>
 void colchain(cudaStream_t st, const Op &op, int n, int P, double *out, long long *launches)
 {
     if (P <= 0) {
         return;
     }
-    k_colchain<Op><<<(unsigned)ceil_div(P, CC_COLS), CC_THREADS, 0, st>>>(op, n, P, out);
+    const int K = xchain_chunks(n, P);
+    if (K > 0) {
+        k_xchain<Op><<<(unsigned)P, (unsigned)K, 0, st>>>(op, n, (int)ceil_div(n, K), out);
+    } else {
+        k_colchain<Op><<<(unsigned)ceil_div(P, CC_COLS), CC_THREADS, 0, st>>>(op, n, P, out);
+    }
     LAUNCH_CHECK();
     *launches += 1;
 }

@@ -268,3 +268,60 @@ def test_wide_basis_matches_oracle(gpu, port, defer, monkeypatch):
         assert rg[0] == rc[0]
         for k in (1, 2, 3):
             np.testing.assert_array_equal(rg[k], rc[k])
+
+
+# The column chains (norms of the projected columns, ybx, the norms of X) run
+# either as written, one thread per chain (MARS_GPU_XCHAIN=0), or chunked over
+# the rows with speculative runs and an exact walk (MARS_GPU_XCHAIN=1). Both
+# must give the reference's values bit for bit.
+XCHAIN = {"sequential": "0", "chunked": "1"}
+
+
+@pytest.mark.parametrize("kernel", sorted(XCHAIN))
+@pytest.mark.parametrize("name", cases.EVAL_CASES)
+def test_column_chain_kernels_match_oracle(name, kernel, gpu, port, monkeypatch):
+    import oracle
+
+    monkeypatch.setenv("MARS_GPU_XCHAIN", XCHAIN[kernel])
+    X, y, w, appends, evals = cases.eval_case(name)
+    a_gpu = gpu.MarsAlgo(X, y, w, cases.EVAL_MAX_TERMS)
+    a_cpu = oracle.OracleAlgo(X, y, w, cases.EVAL_MAX_TERMS, kind="port")
+    assert a_gpu.yvar() == a_cpu.yvar()
+    for ap in appends:
+        assert a_gpu.append(*ap) == a_cpu.append(*ap)
+    for i, (ms, es, lo) in enumerate(evals):
+        mask = cases.eval_mask(X.shape[1], a_cpu.nbasis(), i)
+        rg = a_gpu.eval(mask, ms, es, lo, 1)
+        rc = a_cpu.eval(mask, ms, es, lo, 1)
+        assert rg[0] == rc[0]
+        for k in (1, 2, 3):
+            np.testing.assert_array_equal(rg[k], rc[k])
+
+
+@pytest.mark.parametrize("kernel", sorted(XCHAIN))
+def test_column_chains_on_quantised_data(kernel, be_gpu, be_port, monkeypatch):
+    """Quantised inputs make the chains' terms short dyadic numbers: long runs of
+    exact sums and rounding ties, over n = 300,000 rows (160 chunks of 1,875)."""
+    monkeypatch.setenv("MARS_GPU_XCHAIN", XCHAIN[kernel])
+    rng = np.random.default_rng(41)
+    n, m = 300_000, 6
+    Bo = scenarios.make_orthonormal_basis(n, m, rng)
+    B = (rng.integers(-32, 33, (n, m)) / 16).astype(np.float32)
+    B[:, 0] = 1.0
+    x = (rng.integers(-1024, 1025, n) / 64).astype(np.float32)
+    mask = np.arange(m, dtype=np.int32)
+    r_g = be_gpu.orthonormalize(np.asfortranarray(B), x, mask, Bo, m, 1e-14)
+    r_c = be_port.orthonormalize(np.asfortranarray(B), x, mask, Bo, m, 1e-14)
+    np.testing.assert_array_equal(r_g[0], r_c[0])
+    np.testing.assert_array_equal(r_g[1], r_c[1])
+    assert r_g[2] == r_c[2]
+
+
+@pytest.mark.parametrize("kernel", sorted(XCHAIN))
+def test_golden_term_path_chain_kernels(kernel, gpu, monkeypatch):
+    monkeypatch.setenv("MARS_GPU_PRECISION", "fp64")
+    monkeypatch.setenv("MARS_GPU_XCHAIN", XCHAIN[kernel])
+    g = load_fit("hinge_search")
+    X, y, w, kw = cases.fit_case("hinge_search")
+    model = mars.fit(X, y, w, **kw)
+    assert_same_path(model, g)

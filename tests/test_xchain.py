@@ -1,0 +1,158 @@
+"""The chunked exact accumulation (mars_gb300/csrc/xchain.cuh) on the host.
+
+The kernels that replace the reference's sequential FP64 column chains
+(kernels.cc:215-237, kernels.cc:361-366, marsalgo.cc:359-369) cut the rows into
+chunks, run each chunk speculatively from a guessed entry value, and walk the
+chunks once. tests/xchain_host.cpp builds the same header on the host; these
+tests check its result against the recurrence as written, bit for bit, on data
+chosen to break each of the checks: ties, binade crossings, sign changes, exact
+zeros, subnormals, NaN and infinities, and guesses that are wrong on purpose.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def xlib(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("xchain") / "xchain_host.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off",
+                    "-o", out, os.path.join(HERE, "xchain_host.cpp")], check=True)
+    lib = ctypes.CDLL(out)
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.xc_host_sequential.restype = ctypes.c_double
+    lib.xc_host_sequential.argtypes = [fp, fp, ctypes.c_int]
+    lib.xc_host_chunked.restype = ctypes.c_double
+    lib.xc_host_chunked.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
+    return lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def run(lib, a, b, K, mode=0, scale=0.0):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    n = a.size
+    re = ctypes.c_int(0)
+    want = lib.xc_host_sequential(_ptr(a), _ptr(b), n)
+    got = lib.xc_host_chunked(_ptr(a), _ptr(b), n, K, mode, scale, ctypes.byref(re))
+    return want, got, re.value
+
+
+def same(x, y):
+    return np.array(x, np.float64).view(np.uint64) == np.array(y, np.float64).view(np.uint64)
+
+
+def cases(seed=0):
+    r = np.random.default_rng(seed)
+    n = 20000
+    z = r.standard_normal(n).astype(np.float32)
+    yield "signed", z, r.standard_normal(n).astype(np.float32)
+    yield "squares", z, z
+    yield "positive", np.abs(z), np.abs(r.standard_normal(n)).astype(np.float32)
+    # a head of 1.5 * 2^54 (ulp 4) then small integers: every step rounds and a
+    # quarter of them are exact ties
+    big = r.integers(1, 1 << 12, n).astype(np.float32)
+    big[0] = 1.5 * 2.0 ** 24
+    one = np.ones(n, np.float32)
+    one[0] = 2.0 ** 30
+    yield "ties", big, one
+    # quantised data: products are short dyadics
+    q = (r.integers(-64, 64, n) / 16).astype(np.float32)
+    yield "quantised", q, (r.integers(-8, 8, n) / 4).astype(np.float32)
+    # exponents spread over +-40 binades
+    w = (r.standard_normal(n) * 2.0 ** r.integers(-40, 40, n)).astype(np.float32)
+    yield "wide", w, r.standard_normal(n).astype(np.float32)
+    # exact cancellation back to zero
+    c = np.repeat(r.standard_normal(n // 2).astype(np.float32), 2)
+    s = np.tile(np.array([1, -1], np.float32), n // 2)
+    yield "cancel", c, s
+    # drifting across many binades, both signs
+    d = (np.linspace(-3, 3, n) ** 3).astype(np.float32)
+    yield "drift", d, np.ones(n, np.float32)
+    # subnormal products
+    t = (r.standard_normal(n) * 1e-20).astype(np.float32)
+    yield "tiny", t, (r.standard_normal(n) * 1e-20).astype(np.float32)
+
+
+@pytest.mark.parametrize("K", [1, 2, 7, 32, 160, 1024])
+def test_chunked_equals_sequential(xlib, K):
+    for name, a, b in cases():
+        want, got, _ = run(xlib, a, b, K)
+        assert same(want, got), (name, K, want, got)
+
+
+@pytest.mark.parametrize("mode,scale", [(1, 1e-9), (1, 1e-3), (1, -0.5), (2, 1.0),
+                                        (2, -3.0), (2, 2.0), (2, 1e6), (3, 0.0),
+                                        (3, 1.0), (3, -7.5), (3, float("inf")),
+                                        (3, float("nan"))])
+def test_wrong_guesses_are_caught(xlib, mode, scale):
+    for name, a, b in cases(1):
+        want, got, _ = run(xlib, a, b, 64, mode, scale)
+        assert same(want, got), (name, mode, scale, want, got)
+
+
+def test_special_values(xlib):
+    r = np.random.default_rng(2)
+    n = 5000
+    for bad in (np.nan, np.inf, -np.inf):
+        a = r.standard_normal(n).astype(np.float32)
+        a[n // 3] = bad
+        want, got, _ = run(xlib, a, np.ones(n, np.float32), 50)
+        assert same(want, got) or (np.isnan(want) and np.isnan(got)), (bad, want, got)
+    for n in (0, 1, 2, 3, 31, 33):
+        a = r.standard_normal(n).astype(np.float32)
+        for K in (1, 2, 5, 64):
+            want, got, _ = run(xlib, a, a, K)
+            assert same(want, got), (n, K)
+
+
+def test_few_chunks_are_redone(xlib):
+    """With the kernel's guesses a sum of squares re-runs (almost) no chunk; a signed
+    random walk re-runs the chunks where it changes sign or climbs two binades."""
+    r = np.random.default_rng(3)
+    n = 200000
+    z = r.standard_normal(n).astype(np.float32)
+    want, got, redone = run(xlib, z, z, 1024)
+    assert same(want, got)
+    assert redone <= 4, redone
+    want, got, redone = run(xlib, z, r.standard_normal(n).astype(np.float32), 1024)
+    assert same(want, got)
+    assert redone <= 160, redone
+
+
+def test_translation_is_used(xlib):
+    """The checks must not reject everything: with guesses a few ulps off, chunks of
+    squares, of positive terms and of rounding ties are resolved by translation."""
+    for name, a, b in cases(5):
+        if name not in ("squares", "positive", "ties"):
+            continue
+        for k in (0.0, 1.0, 2.0, 3.0, -5.0):
+            want, got, redone = run(xlib, a, b, 64, 2, k)
+            assert same(want, got), (name, k)
+            assert redone <= 2, (name, k, redone)
+
+
+def test_random_sweep(xlib):
+    r = np.random.default_rng(4)
+    for it in range(200):
+        n = int(r.integers(0, 3000))
+        scale_a = 2.0 ** int(r.integers(-20, 20))
+        a = (r.standard_normal(n) * scale_a).astype(np.float32)
+        if it % 3 == 0:
+            b = a
+        elif it % 3 == 1:
+            b = np.abs(r.standard_normal(n)).astype(np.float32)
+        else:
+            b = (r.integers(-3, 4, n) / 2).astype(np.float32)
+        K = int(r.integers(1, 300))
+        want, got, _ = run(xlib, a, b, K)
+        assert same(want, got), (it, n, K)
