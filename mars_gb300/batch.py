@@ -15,27 +15,34 @@ from . import marslib
 from .mars import forward_pass
 
 
-def fit_many(problems, threads=16, precision=None):
+def fit_many(problems, threads=16, precision=None, stats=None):
     """Fit every (X, y, w, kwargs) of ``problems`` (w may be None); returns
     (models, seconds per fit) in the input order. ``precision``: 'fp64'
-    (default) or 'mixed' for every handle."""
-
-    class Lib:
-        __version__ = getattr(marslib, "__version__", "0.12")
-
-        @staticmethod
-        def MarsAlgo(*a):
-            o = marslib.MarsAlgo(*a)
-            if precision is not None:
-                o.set_precision(precision)
-            return o
+    (default) or 'mixed' for every handle. When ``stats`` is a list, each fit's
+    handle counters (marslib.MarsAlgo.stats()) are appended to it, in order."""
 
     def one(prob):
         X, y, w, kw = prob
+        handles = []
+
+        class Lib:
+            __version__ = getattr(marslib, "__version__", "0.12")
+
+            @staticmethod
+            def MarsAlgo(*a):
+                o = marslib.MarsAlgo(*a)
+                if precision is not None:
+                    o.set_precision(precision)
+                handles.append(o)
+                return o
+
         t0 = time.perf_counter()
         model = forward_pass(Lib, X, y, w, **kw)
-        return model, time.perf_counter() - t0
+        dt = time.perf_counter() - t0
+        return model, dt, handles[-1].stats() if stats is not None and handles else None
 
     with ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
         out = list(ex.map(one, problems))
-    return [m for m, _ in out], [t for _, t in out]
+    if stats is not None:
+        stats.extend(st for _, _, st in out)
+    return [m for m, _, _ in out], [t for _, t, _ in out]

@@ -468,7 +468,7 @@ void eval_block_fp64(mars_gpu_algo *a, Fp64Ctx &c, int Pc, const int *cx_d, cons
                        c.bsort->as<float>(), &c.stats->kernel_launches);
         CUDA_CHECK(cudaEventRecord(c.ev_fork, c.st));
         CUDA_CHECK(cudaStreamWaitEvent(c.st2, c.ev_fork, 0));
-        hinge_scalars(c.st2, c.stasks->as<SweepTask>(), (int)stasks.size(), a->xsort.as<float>(),
+        hinge_scalars(c.st2, c.stasks->as<SweepTask>(), (int)stasks.size(), Pc, a->xsort.as<float>(),
                       a->ysort.as<float>(), c.bsort->as<float>(), n, head, tail, min_span,
                       c.scal->as<double>(), &c.stats->kernel_launches);
         CUDA_CHECK(cudaEventRecord(c.ev_join, c.st2));

@@ -5,6 +5,7 @@
 // (fixed per-thread order, fixed block tree, fixed order across blocks).
 #include "fp64.cuh"
 #include "xchain.cuh"
+#include "xhinge.cuh"
 
 #include <type_traits>
 
@@ -1045,6 +1046,187 @@ __global__ void __launch_bounds__(SC_THREADS)
     }
 }
 
+// The same scalars, exact and parallel over the rows (xhinge.cuh): one block
+// per candidate (blockIdx.x the task, blockIdx.y its candidate), one chunk of L
+// consecutive rows per thread. Per level: float-float guesses of every chunk's
+// entry values from a block scan, XC_RUNS speculative runs per chain (thread 0
+// runs chunk 0 from the true start), then one thread per chain walks the chunks
+// (different warps, so the walks overlap). Last, every thread re-runs its chunk
+// from the exact entry values and writes k0, k1, w at its grid rows. The values
+// equal those of k_hinge_scalars bit for bit.
+constexpr int XH_MAXK = 256;
+
+size_t xh_smem_bytes(int K)
+{
+    return sizeof(XcChunk) * 3 * (size_t)K + sizeof(double) * (XS_N * (size_t)K + XH_MAXK / 32);
+}
+
+// Exclusive prefix over the block's threads of v (a guess: rounding is harmless).
+__device__ double xh_block_prefix(double v, double *wsum)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) {
+            inc += u;
+        }
+    }
+    __syncthreads();  // wsum of the previous call has been read
+    if (lane == 31) {
+        wsum[warp] = inc;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        double w = lane < nw ? wsum[lane] : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) {
+                w += u;
+            }
+        }
+        if (lane < nw) {
+            wsum[lane] = w;
+        }
+    }
+    __syncthreads();
+    return (inc - v) + (warp > 0 ? wsum[warp - 1] : 0.0);
+}
+
+// Chain j's walk over chunks 1 .. K-2: st[j][c + 1] from st[j][c] and the
+// chunk's record; M is the set of chains a re-run of the chunk needs.
+template <int M>
+__device__ void xh_walk(const XhRows &R, int j, const XcChunk *rec, double *st, int K, int L,
+                        int tail)
+{
+    for (int c = 1; c + 1 < K; ++c) {
+        const int c0 = min(tail, c * L), c1 = min(tail, c0 + L);
+        bool redone = false;
+        st[j * K + c + 1] = xc_resolve_with(rec[c], st[j * K + c], [&](double v) {
+            XhState s;
+#pragma unroll
+            for (int q = 0; q < XS_N; ++q) {
+                s.v[q] = st[q * K + c];
+            }
+            s.v[j] = v;
+            xh_run<M>(R, c0, c1, s);
+            return s.v[j];
+        }, &redone);
+    }
+}
+
+__global__ void __launch_bounds__(XH_MAXK)
+    k_hinge_xscalars(const SweepTask *__restrict__ tasks, const float *__restrict__ xsort,
+                     const float *__restrict__ ysort, const float *__restrict__ bs, int n,
+                     int head, int tail, int min_span, int ngrid, double *__restrict__ scal)
+{
+    const SweepTask task = tasks[blockIdx.x];
+    const int q = blockIdx.y;
+    if (q >= task.count) {
+        return;  // the whole block
+    }
+    extern __shared__ __align__(16) unsigned char xsm[];
+    const int K = blockDim.x, t = threadIdx.x;
+    XcChunk *ch = reinterpret_cast<XcChunk *>(xsm);                                  // [3][K]
+    double *st = reinterpret_cast<double *>(xsm + sizeof(XcChunk) * 3 * (size_t)K);  // [XS_N][K]
+    double *wsum = st + XS_N * K;
+    const int cand = task.cand0 + q;
+    const XhRows R{bs + (size_t)cand * n, ysort + (size_t)task.xcol * n,
+                   xsort + (size_t)task.xcol * n};
+    const int L = (tail + K - 1) / K;
+    const int i0 = (int)min((long long)tail, (long long)t * L), i1 = min(tail, i0 + L);
+    const int w1 = 32 < K ? 32 : 0, w2 = 64 < K ? 64 : 0;  // walkers of chains 1 and 2
+#pragma unroll
+    for (int j = 0; j < XS_N; ++j) {
+        st[j * K + t] = 0.0;
+    }
+    double g[3], gp[3];
+
+    // level 1: b2, vb
+    xh_guess1(R, i0, i1, g);
+    gp[0] = xh_block_prefix(g[0], wsum);
+    gp[1] = xh_block_prefix(g[1], wsum);
+    if (t == 0) {
+        XhState s{};
+        xh_run<XH_B2 | XH_VB>(R, i0, i1, s);
+        if (K > 1) {
+            st[XS_B2 * K + 1] = s.v[XS_B2];
+            st[XS_VB * K + 1] = s.v[XS_VB];
+        }
+    } else {
+        xh_spec1(R, i0, i1, gp, ch + t, K);
+    }
+    __syncthreads();
+    if (t == 0) {
+        xh_walk<XH_B2>(R, XS_B2, ch, st, K, L, tail);
+    }
+    if (t == w1) {
+        xh_walk<XH_VB>(R, XS_VB, ch + K, st, K, L, tail);
+    }
+    __syncthreads();
+
+    // level 2: bd, w, k0
+    xh_guess2(R, i0, i1, st[XS_B2 * K + t], st[XS_VB * K + t], g);
+    gp[0] = xh_block_prefix(g[0], wsum);
+    gp[1] = xh_block_prefix(g[1], wsum);
+    gp[2] = xh_block_prefix(g[2], wsum);
+    if (t == 0) {
+        XhState s{};
+        xh_run<XH_B2 | XH_VB | XH_BD | XH_W | XH_K0>(R, i0, i1, s);
+        if (K > 1) {
+            st[XS_BD * K + 1] = s.v[XS_BD];
+            st[XS_W * K + 1] = s.v[XS_W];
+            st[XS_K0 * K + 1] = s.v[XS_K0];
+        }
+    } else {
+        xh_spec2(R, i0, i1, st[XS_B2 * K + t], st[XS_VB * K + t], gp, ch + t, K);
+    }
+    __syncthreads();
+    if (t == 0) {
+        xh_walk<XH_B2 | XH_BD>(R, XS_BD, ch, st, K, L, tail);
+    }
+    if (t == w1) {
+        xh_walk<XH_VB | XH_W>(R, XS_W, ch + K, st, K, L, tail);
+    }
+    if (t == w2) {
+        xh_walk<XH_B2 | XH_K0>(R, XS_K0, ch + 2 * K, st, K, L, tail);
+    }
+    __syncthreads();
+
+    // level 3: k1
+    xh_guess3(R, i0, i1, st[XS_B2 * K + t], st[XS_BD * K + t], g);
+    gp[0] = xh_block_prefix(g[0], wsum);
+    if (t == 0) {
+        XhState s{};
+        xh_run<XH_B2 | XH_BD | XH_K1>(R, i0, i1, s);
+        if (K > 1) {
+            st[XS_K1 * K + 1] = s.v[XS_K1];
+        }
+    } else {
+        xh_spec3(R, i0, i1, st[XS_B2 * K + t], st[XS_BD * K + t], gp, ch + t);
+    }
+    __syncthreads();
+    if (t == 0) {
+        xh_walk<XH_B2 | XH_BD | XH_K1>(R, XS_K1, ch, st, K, L, tail);
+    }
+    __syncthreads();
+
+    // the grid rows of this thread's chunk
+    XhState s;
+#pragma unroll
+    for (int j = 0; j < XS_N; ++j) {
+        s.v[j] = st[j * K + t];
+    }
+    double *out = scal + (size_t)cand * ngrid * 3;
+    xh_output(R, i0, i1, s, head, min_span, [&](int gq, double k0, double k1, double w) {
+        out[(size_t)gq * 3] = k0;
+        out[(size_t)gq * 3 + 1] = k1;
+        out[(size_t)gq * 3 + 2] = w;
+    });
+}
+
 __global__ void k_sort_keys(const float *__restrict__ X, size_t ldX, int n, int col,
                             float *__restrict__ keys, int *__restrict__ vals)
 {
@@ -1372,7 +1554,8 @@ TG_INST(StoredSrc, double)
 // Chunks per chain for k_xchain, or 0 where k_colchain is the faster form.
 // Costs in SM cycles over the GPU: a chain as written takes ~70 cycles a row;
 // FP64 throughput is ~2 FMAs per cycle per SM; k_xchain issues XC_RUNS + 1 FMAs
-// per element and its walk takes ~450 cycles a chunk. MARS_GPU_XCHAIN = 0 or 1
+// per element (the runs from the guess and from zero) and its walk takes ~450
+// cycles a chunk. MARS_GPU_XCHAIN = 0 or 1
 // forces either kernel.
 int xchain_chunks(int n, int P)
 {
@@ -1550,11 +1733,54 @@ void gather_candidates(cudaStream_t st, const int *perm, const float *Bx, size_t
     *launches += 1;
 }
 
-void hinge_scalars(cudaStream_t st, const SweepTask *tasks, int ntasks, const float *xsort,
-                   const float *ysort, const float *bs, int n, int head, int tail, int min_span,
-                   double *scal, long long *launches)
+// Threads (chunks) per candidate for k_hinge_xscalars, or 0 where k_hinge_scalars
+// is the better form. k_hinge_scalars advances a row per ~370 cycles and issues
+// 6 FP64 FMAs per row and candidate; k_hinge_xscalars issues ~40 (the XC_RUNS
+// runs and the run from zero of each chain, and the lower chains re-run beside
+// them) on one SM per candidate, and walks its chunks three times at ~450 cycles
+// a chunk. Both run beside the projection, whose FP64 chains they would slow
+// down once the candidates outnumber the SMs: the chunked form is taken only
+// for at most one candidate per SM, and where it is the faster of the two.
+// MARS_GPU_XCHAIN = 0 or 1 forces either kernel.
+int xh_chunks(int tail, int ncand)
+{
+    const char *fv = std::getenv("MARS_GPU_XCHAIN");
+    const int force = fv && *fv ? std::atoi(fv) : -1;
+    if (tail <= 0 || ncand <= 0 || force == 0) {
+        return 0;
+    }
+    const int K = (int)std::min<size_t>(XH_MAXK, std::max<size_t>(32, round_up(ceil_div(tail, 1024), 32)));
+    if (force == 1) {
+        return K;
+    }
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) {
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    if (ncand > sms) {
+        return 0;
+    }
+    const double plain = 370.0 * tail;
+    const double chunked = 40.0 * tail / 2.0 + 3 * 450.0 * K;
+    return chunked < 0.7 * plain ? K : 0;
+}
+
+void hinge_scalars(cudaStream_t st, const SweepTask *tasks, int ntasks, int ncand,
+                   const float *xsort, const float *ysort, const float *bs, int n, int head,
+                   int tail, int min_span, double *scal, long long *launches)
 {
     if (ntasks <= 0) {
+        return;
+    }
+    const int K = xh_chunks(tail, ncand);
+    if (K > 0) {
+        const size_t smem = xh_smem_bytes(K);
+        allow_smem(k_hinge_xscalars, smem);
+        k_hinge_xscalars<<<dim3((unsigned)ntasks, 32), (unsigned)K, smem, st>>>(
+            tasks, xsort, ysort, bs, n, head, tail, min_span,
+            sweep_grid_rows(head, tail, min_span), scal);
+        LAUNCH_CHECK();
+        *launches += 1;
         return;
     }
     allow_smem(k_hinge_scalars, ScSmem::total);

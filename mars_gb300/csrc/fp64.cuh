@@ -115,10 +115,10 @@ void gather_candidates(cudaStream_t st, const int *perm, const float *Bx, size_t
 // Scalar recurrences of the hinge sweep (k0, k1, w at every grid row) for the
 // candidates of `tasks` (at most 32 per task, one input column each), from the
 // sorted parents bs and the sorted y; scal holds (candidates,
-// sweep_grid_rows, 3) doubles.
-void hinge_scalars(cudaStream_t st, const SweepTask *tasks, int ntasks, const float *xsort,
-                   const float *ysort, const float *bs, int n, int head, int tail, int min_span,
-                   double *scal, long long *launches);
+// sweep_grid_rows, 3) doubles. ncand: the candidates of all tasks together.
+void hinge_scalars(cudaStream_t st, const SweepTask *tasks, int ntasks, int ncand,
+                   const float *xsort, const float *ysort, const float *bs, int n, int head,
+                   int tail, int min_span, double *scal, long long *launches);
 
 // Hinge sweep in FP64 (marsalgo.cc:508-657), one warp per candidate; tasks
 // hold at most sweep_warps(m) candidates; scal from hinge_scalars.

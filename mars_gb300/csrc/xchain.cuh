@@ -29,8 +29,10 @@
 //  3. the chunks are walked in order with the true value t (xc_resolve): where t
 //     is in the binade of the chunk's start, the run with t's residue applies if
 //     |t - its start| is inside that run's margin, and the chunk's end is the
-//     run's end plus (t - its start), an exact FP64 add; anywhere else the chunk
-//     is re-run from t in order.
+//     run's end plus (t - its start), an exact FP64 add; where t is +0 (a chain
+//     whose terms have all been zero so far, as a hinge parent's are on one side
+//     of its knot), a fifth run from +0 gives the end directly; anywhere else the
+//     chunk is re-run from t in order.
 // The result equals the sequential recurrence bit for bit whatever the data (NaN,
 // infinities, zeros, subnormals, sign changes included): every chunk the checks
 // cannot vouch for is recomputed in order.
@@ -89,6 +91,7 @@ struct XcChunk {
     double start;            // the guess with its two last mantissa bits cleared
     double end[XC_RUNS];     // end of the run from start + r ulps
     double margin[XC_RUNS];  // largest |t - (start + r ulps)| run r vouches for, or -1
+    double zero_end;         // end of the run from +0 (a chain still at its start value)
 };
 
 // Margin of one run. h0 is the high word of its start; [hmin, hmax] the range of
@@ -116,40 +119,64 @@ XC_HD double xc_margin(uint32_t h0, uint32_t hmin, uint32_t hmax, bool edge, boo
     return xc_words((Elo - 20u) << 20, 0u) - xc_words((Ehi - 51u) << 20, 0u);
 }
 
-// The XC_RUNS speculative runs of rows [i0, i1) from `guess`. term(i, a, b)
-// yields the f32 factors of row i.
-template <class Term>
-XC_HD void xc_speculate(const Term &term, int i0, int i1, double guess, XcChunk &c)
-{
-    const uint32_t h0 = xc_hi(guess), l0 = xc_lo(guess) & ~(uint32_t)(XC_RUNS - 1);
-    double a[XC_RUNS];
+// The XC_RUNS speculative runs of one chain through one chunk: begin() from the
+// guess, step() once per row with the row's two FP64 factors (exact products of
+// f32 values, or a lower-level chain's value times an exact factor), finish()
+// into the chunk's record.
+struct XcSpec {
+    double a[XC_RUNS], z;
     uint32_t mn[XC_RUNS], mx[XC_RUNS], ed[XC_RUNS];
-#pragma unroll
-    for (int r = 0; r < XC_RUNS; ++r) {
-        a[r] = xc_words(h0, l0 | (uint32_t)r);
-        mn[r] = 0xffffffffu;
-        mx[r] = 0u;
-        ed[r] = 0u;
-    }
-    for (int i = i0; i < i1; ++i) {
-        float x, y;
-        term(i, x, y);
-        const double xd = (double)x, yd = (double)y;
+    uint32_t h0, l0;
+    XC_HD void begin(double guess)
+    {
+        z = 0.0;
+        h0 = xc_hi(guess);
+        l0 = xc_lo(guess) & ~(uint32_t)(XC_RUNS - 1);
 #pragma unroll
         for (int r = 0; r < XC_RUNS; ++r) {
-            a[r] = fma(xd, yd, a[r]);
+            a[r] = xc_words(h0, l0 | (uint32_t)r);
+            mn[r] = 0xffffffffu;
+            mx[r] = 0u;
+            ed[r] = 0u;
+        }
+    }
+    XC_HD void step(double x, double y)
+    {
+        z = fma(x, y, z);
+#pragma unroll
+        for (int r = 0; r < XC_RUNS; ++r) {
+            a[r] = fma(x, y, a[r]);
             const uint32_t h = xc_hi(a[r]);
             mn[r] = xc_umin(mn[r], h);
             mx[r] = xc_umax(mx[r], h);
             ed[r] |= (uint32_t)(((h + 1u) & 0xfffffu) < 2u);
         }
     }
-    c.start = xc_words(h0, l0);
+    XC_HD void finish(XcChunk &c, bool empty) const
+    {
+        c.zero_end = z;
+        c.start = xc_words(h0, l0);
 #pragma unroll
-    for (int r = 0; r < XC_RUNS; ++r) {
-        c.end[r] = a[r];
-        c.margin[r] = xc_margin(h0, mn[r], mx[r], ed[r] != 0u, i1 <= i0);
+        for (int r = 0; r < XC_RUNS; ++r) {
+            c.end[r] = a[r];
+            c.margin[r] = xc_margin(h0, mn[r], mx[r], ed[r] != 0u, empty);
+        }
     }
+};
+
+// The speculative runs of rows [i0, i1) from `guess`. term(i, a, b) yields the
+// f32 factors of row i.
+template <class Term>
+XC_HD void xc_speculate(const Term &term, int i0, int i1, double guess, XcChunk &c)
+{
+    XcSpec sp;
+    sp.begin(guess);
+    for (int i = i0; i < i1; ++i) {
+        float x, y;
+        term(i, x, y);
+        sp.step((double)x, (double)y);
+    }
+    sp.finish(c, i1 <= i0);
 }
 
 // The rows [i0, i1) in order from t: the reference's recurrence as written.
@@ -164,12 +191,15 @@ XC_HD double xc_run(const Term &term, int i0, int i1, double t)
     return t;
 }
 
-// The value after rows [i0, i1) given the true value t before them. *redone is
-// set when the chunk had to be re-run.
-template <class Term>
-XC_HD double xc_resolve(const Term &term, int i0, int i1, const XcChunk &c, double t,
-                        bool *redone)
+// The value after a chunk given the true value t before it, from the chunk's
+// record; rerun(t) runs the chunk in order where the record cannot vouch for
+// the translation, and *redone is then set.
+template <class Rerun>
+XC_HD double xc_resolve_with(const XcChunk &c, double t, const Rerun &rerun, bool *redone)
 {
+    if (xc_hi(t) == 0u && xc_lo(t) == 0u) {
+        return c.zero_end;  // t is +0: the run from +0 is the chain itself
+    }
     const uint32_t hs = xc_hi(c.start);
     if ((xc_hi(t) >> 20) == (hs >> 20)) {
         const uint32_t r = xc_lo(t) & (uint32_t)(XC_RUNS - 1);
@@ -179,7 +209,14 @@ XC_HD double xc_resolve(const Term &term, int i0, int i1, const XcChunk &c, doub
         }
     }
     *redone = true;
-    return xc_run(term, i0, i1, t);
+    return rerun(t);
+}
+
+template <class Term>
+XC_HD double xc_resolve(const Term &term, int i0, int i1, const XcChunk &c, double t,
+                        bool *redone)
+{
+    return xc_resolve_with(c, t, [&](double v) { return xc_run(term, i0, i1, v); }, redone);
 }
 
 // Float-float accumulation of exact f32 products, for the guesses.
@@ -199,6 +236,27 @@ struct XcGuess {
         const float t = e + (lo + pl);
         hi = s + t;
         lo = t - (hi - s);
+    }
+    // the sum += d * v, d f32, v a float-float value
+    XC_HD void add_scaled(float d, float vh, float vl)
+    {
+#ifdef __CUDA_ARCH__
+        const float ph = __fmul_rn(d, vh);
+#else
+        const float ph = d * vh;
+#endif
+        const float pl = fmaf(d, vh, -ph) + d * vl;
+        const float s = hi + ph;
+        const float bb = s - hi;
+        const float e = (hi - (s - bb)) + (ph - bb);
+        const float t = e + (lo + pl);
+        hi = s + t;
+        lo = t - (hi - s);
+    }
+    XC_HD void set(double v)
+    {
+        hi = (float)v;
+        lo = (float)(v - (double)hi);
     }
     XC_HD double value() const { return (double)hi + (double)lo; }
 };

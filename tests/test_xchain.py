@@ -156,3 +156,100 @@ def test_random_sweep(xlib):
         K = int(r.integers(1, 300))
         want, got, _ = run(xlib, a, b, K)
         assert same(want, got), (it, n, K)
+
+
+def _hinge_lib(xlib):
+    fp = ctypes.POINTER(ctypes.c_float)
+    dp = ctypes.POINTER(ctypes.c_double)
+    xlib.xh_host_sequential.restype = None
+    xlib.xh_host_sequential.argtypes = [fp, fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+    xlib.xh_host_chunked.restype = None
+    xlib.xh_host_chunked.argtypes = [fp, fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int)]
+    return xlib
+
+
+def run_hinge(lib, b, y, x, head, min_span, K):
+    b, y, x = (np.ascontiguousarray(v, np.float32) for v in (b, y, x))
+    tail = b.size
+    ng = (tail - 1 - (head + 1)) // min_span + 1 if tail - 1 >= head + 1 else 0
+    want = np.full(3 * max(ng, 1), -7.0)
+    got = np.full(3 * max(ng, 1), -7.0)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.xh_host_sequential(_ptr(b), _ptr(y), _ptr(x), tail, head, min_span,
+                           want.ctypes.data_as(dp))
+    re = ctypes.c_int(0)
+    lib.xh_host_chunked(_ptr(b), _ptr(y), _ptr(x), tail, head, min_span, K,
+                        got.ctypes.data_as(dp), ctypes.byref(re))
+    return want, got, re.value
+
+
+def hinge_cases(seed):
+    r = np.random.default_rng(seed)
+    n = 30000
+    x = np.sort(r.standard_normal(n).astype(np.float32))[::-1].copy()
+    y = r.standard_normal(n).astype(np.float32)
+    b = np.maximum(r.standard_normal(n), 0).astype(np.float32)
+    yield "hinge parent", b, y, x
+    yield "intercept, skewed y", np.ones(n, np.float32), (y + 0.3).astype(np.float32), x
+    xq = np.sort((r.integers(0, 50, n) / 8).astype(np.float32))[::-1].copy()  # ties: d = 0
+    yield "quantised x", np.abs(y), (r.integers(-4, 5, n) / 4).astype(np.float32), xq
+    b2 = b.copy()
+    b2[n // 3: n // 2] = 0  # a run of zero parent values
+    yield "zero run", b2, y, x
+    yield "wide", (np.abs(y) * 2.0 ** r.integers(-30, 30, n)).astype(np.float32), y, x
+
+
+@pytest.mark.parametrize("K", [1, 2, 32, 96, 256])
+def test_hinge_scalars_chunked_equal_sequential(xlib, K):
+    lib = _hinge_lib(xlib)
+    for name, b, y, x in hinge_cases(6):
+        for head, span in ((0, 1), (3, 7), (100, 33)):
+            want, got, _ = run_hinge(lib, b, y, x, head, span, K)
+            assert (want.view(np.uint64) == got.view(np.uint64)).all(), (name, K, head, span)
+
+
+def test_hinge_scalars_few_chunks_redone(xlib):
+    lib = _hinge_lib(xlib)
+    r = np.random.default_rng(7)
+    n = 200000
+    x = np.sort(r.standard_normal(n).astype(np.float32))[::-1].copy()
+    b = np.maximum(r.standard_normal(n), 0).astype(np.float32)
+    y = (r.standard_normal(n) + 0.1).astype(np.float32)
+    want, got, redone = run_hinge(lib, b, y, x, 0, 6, 256)
+    assert (want.view(np.uint64) == got.view(np.uint64)).all()
+    # six chains walked over 255 chunks each
+    assert redone <= 0.1 * 6 * 255, redone
+
+
+def test_hinge_scalars_short_and_empty_chunks(xlib):
+    lib = _hinge_lib(xlib)
+    r = np.random.default_rng(8)
+    for tail in (1, 2, 3, 5, 31, 33, 40):
+        x = np.sort(r.standard_normal(tail).astype(np.float32))[::-1].copy()
+        y = r.standard_normal(tail).astype(np.float32)
+        b = np.abs(r.standard_normal(tail)).astype(np.float32)
+        for K in (32, 64):
+            for head, span in ((0, 1), (1, 2)):
+                want, got, _ = run_hinge(lib, b, y, x, head, span, K)
+                assert (want.view(np.uint64) == got.view(np.uint64)).all(), (tail, K, head)
+
+
+def test_zero_prefix_needs_no_rerun(xlib):
+    """A hinge parent is zero on one side of its knot: every chain then stays at
+    +0 for a stretch of chunks, which the run from +0 resolves."""
+    lib = _hinge_lib(xlib)
+    r = np.random.default_rng(9)
+    n = 100000
+    x = np.sort(r.standard_normal(n).astype(np.float32))[::-1].copy()
+    y = r.standard_normal(n).astype(np.float32)
+    b = np.maximum(r.standard_normal(n), 0).astype(np.float32)
+    b[: n // 2] = 0
+    want, got, redone = run_hinge(lib, b, y, x, 0, 5, 256)
+    assert (want.view(np.uint64) == got.view(np.uint64)).all()
+    assert redone <= 60, redone
+    z = r.standard_normal(n).astype(np.float32)
+    z[: n // 3] = 0
+    want, got, redone = run(xlib, z, z, 512)
+    assert same(want, got)
+    assert redone <= 4, redone

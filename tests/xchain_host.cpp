@@ -1,8 +1,9 @@
-// Host build of the chunked exact accumulation (mars_gb300/csrc/xchain.cuh) for
-// the CPU tests: the same xc_speculate / xc_resolve the kernel runs, with the
-// chunk layout of the kernel, against the plain sequential recurrence.
-#include "../mars_gb300/csrc/xchain.cuh"
+// Host build of the chunked exact accumulations (mars_gb300/csrc/xchain.cuh,
+// xhinge.cuh) for the CPU tests: the routines the kernels run, in the kernels
+// chunk layout and phase order, against the recurrences run in order.
+#include "../mars_gb300/csrc/xhinge.cuh"
 
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -77,5 +78,133 @@ double xc_host_chunked(const float *a, const float *b, int n, int K, int guess_m
         *redone = nre;
     }
     return t;
+}
+
+// The hinge scalars in order: out[3 q + {0, 1, 2}] = k0, k1, w at grid row q.
+void xh_host_sequential(const float *b, const float *y, const float *x, int tail, int head,
+                        int min_span, double *out)
+{
+    const XhRows R{b, y, x};
+    XhState s{};
+    xh_output(R, 0, tail, s, head, min_span, [&](int q, double k0, double k1, double w) {
+        out[3 * q] = k0;
+        out[3 * q + 1] = k1;
+        out[3 * q + 2] = w;
+    });
+}
+
+// The phases of k_hinge_xscalars with K chunks; *redone counts re-run chunks.
+void xh_host_chunked(const float *b, const float *y, const float *x, int tail, int head,
+                     int min_span, int K, double *out, int *redone)
+{
+    const XhRows R{b, y, x};
+    const int L = tail > 0 ? (tail + K - 1) / K : 0;
+    auto lo = [&](int c) { return c * L < tail ? c * L : tail; };
+    auto hi = [&](int c) { return lo(c) + L < tail ? lo(c) + L : tail; };
+    std::vector<double> st((size_t)XS_N * K, 0.0), g(3 * (size_t)K, 0.0), gs(3 * (size_t)K);
+    std::vector<XcChunk> ch(3 * (size_t)K);
+    auto S = [&](int j, int c) -> double & { return st[(size_t)j * K + c]; };
+    int nre = 0;
+    auto prefix = [&](int nv) {
+        for (int v = 0; v < nv; ++v) {
+            double acc = 0.0;
+            for (int c = 0; c < K; ++c) {
+                gs[(size_t)v * K + c] = acc;
+                acc += g[(size_t)c * 3 + v];
+            }
+        }
+    };
+    auto guess = [&](int v, int c) { return gs[(size_t)v * K + c]; };
+    auto walk = [&](int j, int slot, auto rerun_mask) {
+        for (int c = 1; c + 1 < K; ++c) {
+            bool re = false;
+            const double t = S(j, c);
+            S(j, c + 1) = xc_resolve_with(ch[(size_t)slot * K + c], t, [&](double v) {
+                XhState s{};
+                for (int q = 0; q < XS_N; ++q) {
+                    s.v[q] = S(q, c);
+                }
+                s.v[j] = v;
+                xh_run<decltype(rerun_mask)::value>(R, lo(c), hi(c), s);
+                return s.v[j];
+            }, &re);
+            nre += re ? 1 : 0;
+        }
+    };
+    // level 1
+    for (int c = 0; c < K; ++c) {
+        xh_guess1(R, lo(c), hi(c), &g[(size_t)c * 3]);
+    }
+    prefix(2);
+    for (int c = 0; c < K; ++c) {
+        if (c == 0) {
+            XhState s{};
+            xh_run<XH_B2 | XH_VB>(R, lo(0), hi(0), s);
+            if (K > 1) {
+                S(XS_B2, 1) = s.v[XS_B2];
+                S(XS_VB, 1) = s.v[XS_VB];
+            }
+        } else {
+            const double gg[2] = {guess(0, c), guess(1, c)};
+            xh_spec1(R, lo(c), hi(c), gg, &ch[c], K);
+        }
+    }
+    walk(XS_B2, 0, std::integral_constant<int, XH_B2>());
+    walk(XS_VB, 1, std::integral_constant<int, XH_VB>());
+    // level 2
+    for (int c = 0; c < K; ++c) {
+        xh_guess2(R, lo(c), hi(c), S(XS_B2, c), S(XS_VB, c), &g[(size_t)c * 3]);
+    }
+    prefix(3);
+    for (int c = 0; c < K; ++c) {
+        if (c == 0) {
+            XhState s{};
+            xh_run<XH_B2 | XH_VB | XH_BD | XH_W | XH_K0>(R, lo(0), hi(0), s);
+            if (K > 1) {
+                S(XS_BD, 1) = s.v[XS_BD];
+                S(XS_W, 1) = s.v[XS_W];
+                S(XS_K0, 1) = s.v[XS_K0];
+            }
+        } else {
+            const double gg[3] = {guess(0, c), guess(1, c), guess(2, c)};
+            xh_spec2(R, lo(c), hi(c), S(XS_B2, c), S(XS_VB, c), gg, &ch[c], K);
+        }
+    }
+    walk(XS_BD, 0, std::integral_constant<int, XH_B2 | XH_BD>());
+    walk(XS_W, 1, std::integral_constant<int, XH_VB | XH_W>());
+    walk(XS_K0, 2, std::integral_constant<int, XH_B2 | XH_K0>());
+    // level 3
+    for (int c = 0; c < K; ++c) {
+        xh_guess3(R, lo(c), hi(c), S(XS_B2, c), S(XS_BD, c), &g[(size_t)c * 3]);
+    }
+    prefix(1);
+    for (int c = 0; c < K; ++c) {
+        if (c == 0) {
+            XhState s{};
+            xh_run<XH_B2 | XH_BD | XH_K1>(R, lo(0), hi(0), s);
+            if (K > 1) {
+                S(XS_K1, 1) = s.v[XS_K1];
+            }
+        } else {
+            const double gg[1] = {guess(0, c)};
+            xh_spec3(R, lo(c), hi(c), S(XS_B2, c), S(XS_BD, c), gg, &ch[c]);
+        }
+    }
+    walk(XS_K1, 0, std::integral_constant<int, XH_B2 | XH_BD | XH_K1>());
+    // output
+    for (int c = 0; c < K; ++c) {
+        XhState s{};
+        for (int q = 0; q < XS_N; ++q) {
+            s.v[q] = S(q, c);
+        }
+        xh_output(R, lo(c), hi(c), s, head, min_span, [&](int q, double k0, double k1, double w) {
+            out[3 * q] = k0;
+            out[3 * q + 1] = k1;
+            out[3 * q + 2] = w;
+        });
+    }
+    if (redone) {
+        *redone = nre;
+    }
 }
 }
