@@ -1054,7 +1054,7 @@ __global__ void __launch_bounds__(SC_THREADS)
 // (different warps, so the walks overlap). Last, every thread re-runs its chunk
 // from the exact entry values and writes k0, k1, w at its grid rows. The values
 // equal those of k_hinge_scalars bit for bit.
-constexpr int XH_MAXK = 256;
+constexpr int XH_MAXK = 512;
 
 size_t xh_smem_bytes(int K)
 {

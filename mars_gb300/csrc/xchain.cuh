@@ -171,6 +171,7 @@ XC_HD void xc_speculate(const Term &term, int i0, int i1, double guess, XcChunk 
 {
     XcSpec sp;
     sp.begin(guess);
+#pragma unroll 4
     for (int i = i0; i < i1; ++i) {
         float x, y;
         term(i, x, y);
@@ -183,6 +184,7 @@ XC_HD void xc_speculate(const Term &term, int i0, int i1, double guess, XcChunk 
 template <class Term>
 XC_HD double xc_run(const Term &term, int i0, int i1, double t)
 {
+#pragma unroll 4
     for (int i = i0; i < i1; ++i) {
         float x, y;
         term(i, x, y);

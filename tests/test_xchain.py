@@ -200,7 +200,7 @@ def hinge_cases(seed):
     yield "wide", (np.abs(y) * 2.0 ** r.integers(-30, 30, n)).astype(np.float32), y, x
 
 
-@pytest.mark.parametrize("K", [1, 2, 32, 96, 256])
+@pytest.mark.parametrize("K", [1, 2, 32, 96, 256, 512])
 def test_hinge_scalars_chunked_equal_sequential(xlib, K):
     lib = _hinge_lib(xlib)
     for name, b, y, x in hinge_cases(6):
