@@ -1,0 +1,68 @@
+"""bench.py's multi-rank host logic on CPU (gloo, world size 2).
+
+The forward pass of one fit does not shard: `bench.py --gpus N` runs N replicas,
+one per rank, and reports the max over ranks of the timed span and the sum of
+their work. These tests run that reduction over two gloo ranks, and the
+reference arm under torchrun with two ranks (rank 0 alone times it and prints).
+"""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+pytest.importorskip("torch")
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+REDUCE = r"""
+import bench
+t = bench.dist()
+rank = int(__import__("os").environ["RANK"])
+print(bench.allmax(t, 1.5 + rank), bench.allsum(t, 10 * (rank + 1)))
+t.destroy_process_group()
+"""
+
+
+def test_replica_reductions_over_gloo():
+    port = _free_port()
+    procs = []
+    for rank in range(2):
+        env = dict(os.environ, RANK=str(rank), LOCAL_RANK=str(rank), WORLD_SIZE="2",
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, "-c", REDUCE], cwd=ROOT, env=env,
+                                      stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                                      text=True))
+    outs = [p.communicate(timeout=300) for p in procs]
+    for p, (out, err) in zip(procs, outs):
+        assert p.returncode == 0, err
+        mx, total = out.split()
+        assert float(mx) == 2.5  # the slowest rank's span
+        assert float(total) == 30.0  # the work of both replicas
+
+
+def test_reference_arm_under_torchrun_two_ranks():
+    port = _free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py",
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3",
+           "--workload", "plain_fit"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1  # rank 0 only
+    line = lines[0]
+    assert line["impl"] == "reference"
+    # config 1 is a linear-only fit: no knots are scored, the time is what is measured
+    assert line["ms_per_step"] > 0 and line["e2e"]["value"] == line["value"]
+    assert line["cpu_baseline"]["kind"] == "port"
+    assert line["steps"] == 1 and line["warmup"] == 3
