@@ -6,6 +6,7 @@
 #include "host_exact.h"
 
 #include "error.h"
+#include "xchain.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -13,13 +14,238 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <condition_variable>
+#include <cstdlib>
+#include <functional>
+#include <mutex>
 #include <thread>
+
+#include <unistd.h>
 
 namespace mgpu {
 
 namespace {
 constexpr double kDgksRatioSq = 9.0;  // kernels.h:17
+
+// ---------------------------------------------------------------------------
+// An append of a long column on several host cores. Its elementwise loops (the
+// new column, the Gram-Schmidt updates v -= c q, the scalings and the row-major
+// copy) split over a process-wide thread pool: memory-bound, and each element's
+// value does not depend on the split. Taken for appends of at least
+// MARS_GPU_HOST_PAR_ROWS rows (default 262,144) when the pool is free; shorter
+// columns, and appends while another append holds the pool, run in order on
+// the calling thread.
+//
+// The serial FP64 chains (the dot products and norms) stay in order unless
+// MARS_GPU_HOST_XCHAIN=1, which runs them chunked with the exact speculation of
+// xchain.cuh (guesses from plain FP64 partial sums, XC_RUNS + 1 speculative runs
+// per chunk of ~2,048 rows, an in-order walk). On the host the speculative runs'
+// bookkeeping costs ~3x a plain chain step per row, so the chunked form gains
+// little over eight x86 cores. Either way the results are the same bit for bit.
+// ---------------------------------------------------------------------------
+
+// A process-wide pool of host threads. The caller takes part as worker 0; idle
+// workers spin briefly on the job counter, then sleep.
+class HostPool {
+  public:
+    explicit HostPool(int nt) : nt_(nt)
+    {
+        for (int w = 1; w < nt_; ++w) {
+            th_.emplace_back([this, w] { loop(w); });
+        }
+    }
+    int size() const { return nt_; }
+    // fn(w) for w = 0 .. size() - 1; returns when every worker has finished.
+    void run(const std::function<void(int)> &fn)
+    {
+        job_ = &fn;
+        pending_.store(nt_ - 1, std::memory_order_relaxed);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            epoch_.fetch_add(1, std::memory_order_release);
+        }
+        cv_.notify_all();
+        fn(0);
+        while (pending_.load(std::memory_order_acquire) != 0) {
+        }
+    }
+
+  private:
+    void loop(int w)
+    {
+        unsigned seen = 0;
+        for (;;) {
+            unsigned e = epoch_.load(std::memory_order_acquire);
+            for (int spin = 0; e == seen && spin < (1 << 16); ++spin) {
+                e = epoch_.load(std::memory_order_acquire);
+            }
+            if (e == seen) {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return epoch_.load(std::memory_order_acquire) != seen; });
+                e = epoch_.load(std::memory_order_acquire);
+            }
+            seen = e;
+            (*job_)(w);
+            pending_.fetch_sub(1, std::memory_order_acq_rel);
+        }
+    }
+    int nt_;
+    std::vector<std::thread> th_;
+    std::atomic<unsigned> epoch_{0};
+    std::atomic<int> pending_{0};
+    const std::function<void(int)> *job_ = nullptr;
+    std::mutex mu_;
+    std::condition_variable cv_;
+};
+
+std::mutex g_pool_use;  // one append at a time uses the pool
+
+// The pool of this process (none in a child forked after it was made: the
+// child has no worker threads).
+HostPool *host_pool()
+{
+    static const pid_t owner = getpid();
+    static HostPool *pool = [] {
+        const unsigned hc = std::thread::hardware_concurrency();
+        const int nt = (int)std::min(16u, std::max(1u, hc));
+        return nt > 1 ? new HostPool(nt) : nullptr;  // lives until the process exits
+    }();
+    return getpid() == owner ? pool : nullptr;
 }
+
+size_t host_par_rows()
+{
+    const char *v = std::getenv("MARS_GPU_HOST_PAR_ROWS");
+    return v && *v ? (size_t)std::strtoull(v, nullptr, 10) : (size_t)262144;
+}
+
+bool host_xchain()
+{
+    const char *v = std::getenv("MARS_GPU_HOST_XCHAIN");
+    return v && *v == '1';
+}
+
+// Runs the append's loops in order (pool == nullptr) or over the pool.
+struct Par {
+    HostPool *pool = nullptr;
+    bool chunked_chains = false;
+
+    // fn(i0, i1) over [0, n) in pieces; elementwise work only.
+    template <class F>
+    void rows(size_t n, const F &fn) const
+    {
+        if (!pool) {
+            fn((size_t)0, n);
+            return;
+        }
+        const size_t T = (size_t)pool->size(), L = (n + T - 1) / T;
+        pool->run([&](int w) {
+            const size_t i0 = std::min(n, (size_t)w * L), i1 = std::min(n, i0 + L);
+            if (i0 < i1) {
+                fn(i0, i1);
+            }
+        });
+    }
+
+    // acc = fma(x_i, y_i, acc) over i = 0 .. n-1 in order, from 0; term(i, x, y)
+    // gives row i's FP64 factors. Chunks of ~2,048 rows (a signed chain then
+    // rarely leaves its binade inside one), a contiguous range of them per thread.
+    template <class Term>
+    double chain(size_t n, const Term &term) const
+    {
+        auto run_in_order = [&](size_t i0, size_t i1, double t) {
+            for (size_t i = i0; i < i1; ++i) {
+                double x, y;
+                term(i, x, y);
+                t = std::fma(x, y, t);
+            }
+            return t;
+        };
+        if (!pool || !chunked_chains) {
+            return run_in_order(0, n, 0.0);
+        }
+        constexpr size_t kRows = 2048;
+        const int T = pool->size();
+        const size_t C = std::max<size_t>((size_t)T, (n + kRows - 1) / kRows);
+        const size_t L = (n + C - 1) / C, per = (C + T - 1) / T;
+        static std::vector<XcChunk> rec;  // used under the pool lock only
+        static std::vector<double> guess;
+        rec.resize(C);
+        guess.resize(C);
+        double end0 = 0.0;
+        auto lo = [&](size_t c) { return std::min(n, c * L); };
+        auto hi = [&](size_t c) { return std::min(n, lo(c) + L); };
+        pool->run([&](int w) {  // chunk sums, eight partial sums each
+            for (size_t c = (size_t)w * per; c < std::min(C, (size_t)(w + 1) * per); ++c) {
+                double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                size_t i = lo(c);
+                for (; i + 8 <= hi(c); i += 8) {
+                    for (int k = 0; k < 8; ++k) {
+                        double x, y;
+                        term(i + k, x, y);
+                        s[k] += x * y;
+                    }
+                }
+                for (; i < hi(c); ++i) {
+                    double x, y;
+                    term(i, x, y);
+                    s[0] += x * y;
+                }
+                guess[c] = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+            }
+        });
+        double pre = 0.0;
+        for (size_t c = 0; c < C; ++c) {
+            const double v = guess[c];
+            guess[c] = pre;
+            pre += v;
+        }
+        pool->run([&](int w) {
+            for (size_t c = (size_t)w * per; c < std::min(C, (size_t)(w + 1) * per); ++c) {
+                if (c == 0) {
+                    end0 = run_in_order(lo(0), hi(0), 0.0);
+                    continue;
+                }
+                XcSpec sp;
+                sp.begin(guess[c]);
+                for (size_t i = lo(c); i < hi(c); ++i) {
+                    double x, y;
+                    term(i, x, y);
+                    sp.step(x, y);
+                }
+                sp.finish(rec[c], hi(c) <= lo(c));
+            }
+        });
+        double t = end0;
+        for (size_t c = 1; c < C; ++c) {
+            bool redone = false;
+            t = xc_resolve_with(rec[c], t, [&](double v) { return run_in_order(lo(c), hi(c), v); },
+                                &redone);
+        }
+        return t;
+    }
+};
+
+// Holds the pool for one append when its columns are long enough.
+struct ParScope {
+    Par par;
+    bool held = false;
+    explicit ParScope(size_t n)
+    {
+        if (n >= host_par_rows() && host_pool() && g_pool_use.try_lock()) {
+            held = true;
+            par.pool = host_pool();
+            par.chunked_chains = host_xchain();
+        }
+    }
+    ~ParScope()
+    {
+        if (held) {
+            g_pool_use.unlock();
+        }
+    }
+};
+}  // namespace
 
 void HostBasis::init(const float *X_, const float *y_, const float *w, size_t n_, size_t p_,
                      size_t ldx_, size_t max_terms_)
@@ -121,90 +347,94 @@ double HostBasis::dsse() const
 namespace {
 
 // kernels.cc:194-211 against column-major Bo (column stride n).
-double mgs_project(size_t n, size_t m, double *v, const float *BoC)
+double mgs_project(const Par &par, size_t n, size_t m, double *v, const float *BoC)
 {
     double proj = 0.0;
     for (size_t j = 0; j < m; ++j) {
         const float *q = BoC + j * n;
-        double c = 0.0;
-        for (size_t i = 0; i < n; ++i) {
-            c = std::fma((double)q[i], v[i], c);
-        }
-        for (size_t i = 0; i < n; ++i) {
-            v[i] = std::fma(-c, (double)q[i], v[i]);
-        }
+        const double c = par.chain(n, [&](size_t i, double &x, double &y) {
+            x = (double)q[i];
+            y = v[i];
+        });
+        par.rows(n, [&](size_t i0, size_t i1) {
+            for (size_t i = i0; i < i1; ++i) {
+                v[i] = std::fma(-c, (double)q[i], v[i]);
+            }
+        });
         proj = std::fma(c, c, proj);
     }
     return proj;
 }
 
-double sum_sq(const double *v, size_t n)
+double sum_sq(const Par &par, const double *v, size_t n)
 {
-    double acc = 0.0;
-    for (size_t i = 0; i < n; ++i) {
-        acc = std::fma(v[i], v[i], acc);
-    }
-    return acc;
+    return par.chain(n, [&](size_t i, double &x, double &y) { x = y = v[i]; });
 }
 
 }  // namespace
 
 double HostBasis::append(char type, int xcol, int bcol, float h, long *dgks)
 {
+    const ParScope scope(n);
+    const Par &par = scope.par;
     const float sx = s[xcol];
     const float *bp = B.data() + (size_t)bcol * n;
     const float *xp = X + (size_t)xcol * ldx;
     float *Bm = B.data() + m * n;
-    for (size_t i = 0; i < n; ++i) {
-        float val;
-        if (type == 'l') {
-            val = sx * bp[i] * xp[i];
-        } else {
-            const float t = (type == '+') ? xp[i] - h : h - xp[i];
-            val = sx * bp[i] * ((t < 0.0f) ? 0.0f : t);
-        }
-        Bm[i] = val;
-    }
     std::vector<double> v(n);
-    for (size_t i = 0; i < n; ++i) {
-        v[i] = (double)Bm[i];
-    }
-    const float raw = (float)std::sqrt(sum_sq(v.data(), n));
-    for (size_t i = 0; i < n; ++i) {
-        Bm[i] /= raw;
-    }
+    par.rows(n, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; ++i) {
+            float val;
+            if (type == 'l') {
+                val = sx * bp[i] * xp[i];
+            } else {
+                const float t = (type == '+') ? xp[i] - h : h - xp[i];
+                val = sx * bp[i] * ((t < 0.0f) ? 0.0f : t);
+            }
+            Bm[i] = val;
+            v[i] = (double)val;
+        }
+    });
+    const float raw = (float)std::sqrt(sum_sq(par, v.data(), n));
+    par.rows(n, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; ++i) {
+            Bm[i] /= raw;
+        }
+    });
     // kernels.cc:239-281
-    const double proj = mgs_project(n, m, v.data(), BoC.data());
-    double vn = sum_sq(v.data(), n);
+    const double proj = mgs_project(par, n, m, v.data(), BoC.data());
+    double vn = sum_sq(par, v.data(), n);
     if (vn > tol && vn * kDgksRatioSq < proj) {
         if (dgks) {
             ++*dgks;
         }
-        mgs_project(n, m, v.data(), BoC.data());
-        vn = sum_sq(v.data(), n);
+        mgs_project(par, n, m, v.data(), BoC.data());
+        vn = sum_sq(par, v.data(), n);
     }
     const double wn = std::sqrt(vn);
     if (wn * wn > tol) {
-        for (size_t i = 0; i < n; ++i) {
-            v[i] /= wn;
-        }
         float *q = BoC.data() + m * n;
-        for (size_t i = 0; i < n; ++i) {
-            q[i] = (float)v[i];
-        }
-        double ybo_m = 0.0;
-        for (size_t i = 0; i < n; ++i) {
-            ybo_m = std::fma((double)q[i], (double)y[i], ybo_m);
-        }
+        par.rows(n, [&](size_t i0, size_t i1) {
+            for (size_t i = i0; i < i1; ++i) {
+                v[i] /= wn;
+                q[i] = (float)v[i];
+            }
+        });
+        double ybo_m = par.chain(n, [&](size_t i, double &x, double &y) {
+            x = (double)q[i];
+            y = (double)this->y[i];
+        });
         double ybo_sq = ybo_m * ybo_m;
         for (double e : ybo) {
             ybo_sq = std::fma(e, e, ybo_sq);
         }
         const double mse = (1. - ybo_sq) / (double)n;
         if (mse >= -tol) {
-            for (size_t i = 0; i < n; ++i) {
-                BoR[i * max_terms + m] = q[i];
-            }
+            par.rows(n, [&](size_t i0, size_t i1) {
+                for (size_t i = i0; i < i1; ++i) {
+                    BoR[i * max_terms + m] = q[i];
+                }
+            });
             ybo.push_back(ybo_m);
             m += 1;
             return mse < 0.0 ? 0.0 : mse;

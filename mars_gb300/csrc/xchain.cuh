@@ -41,10 +41,14 @@
 
 #ifdef __CUDACC__
 #define XC_HD __host__ __device__ __forceinline__
+#define XC_UNROLL _Pragma("unroll")
+#define XC_UNROLL4 _Pragma("unroll 4")
 #else
 #include <cmath>
 #include <cstring>
 #define XC_HD inline
+#define XC_UNROLL
+#define XC_UNROLL4
 #endif
 
 XC_HD uint32_t xc_hi(double v)
@@ -132,7 +136,7 @@ struct XcSpec {
         z = 0.0;
         h0 = xc_hi(guess);
         l0 = xc_lo(guess) & ~(uint32_t)(XC_RUNS - 1);
-#pragma unroll
+XC_UNROLL
         for (int r = 0; r < XC_RUNS; ++r) {
             a[r] = xc_words(h0, l0 | (uint32_t)r);
             mn[r] = 0xffffffffu;
@@ -143,7 +147,7 @@ struct XcSpec {
     XC_HD void step(double x, double y)
     {
         z = fma(x, y, z);
-#pragma unroll
+XC_UNROLL
         for (int r = 0; r < XC_RUNS; ++r) {
             a[r] = fma(x, y, a[r]);
             const uint32_t h = xc_hi(a[r]);
@@ -156,7 +160,7 @@ struct XcSpec {
     {
         c.zero_end = z;
         c.start = xc_words(h0, l0);
-#pragma unroll
+XC_UNROLL
         for (int r = 0; r < XC_RUNS; ++r) {
             c.end[r] = a[r];
             c.margin[r] = xc_margin(h0, mn[r], mx[r], ed[r] != 0u, empty);
@@ -171,7 +175,7 @@ XC_HD void xc_speculate(const Term &term, int i0, int i1, double guess, XcChunk 
 {
     XcSpec sp;
     sp.begin(guess);
-#pragma unroll 4
+XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         float x, y;
         term(i, x, y);
@@ -184,7 +188,7 @@ XC_HD void xc_speculate(const Term &term, int i0, int i1, double guess, XcChunk 
 template <class Term>
 XC_HD double xc_run(const Term &term, int i0, int i1, double t)
 {
-#pragma unroll 4
+XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         float x, y;
         term(i, x, y);

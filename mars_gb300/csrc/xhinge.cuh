@@ -46,7 +46,7 @@ struct XhState {
 template <int M>
 XC_HD void xh_run(const XhRows &R, int i0, int i1, XhState &s)
 {
-#pragma unroll 4
+XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         const double bk = (double)R.bk(i);
         if (i > 0) {
@@ -78,7 +78,7 @@ XC_HD void xh_run(const XhRows &R, int i0, int i1, XhState &s)
 XC_HD void xh_guess1(const XhRows &R, int i0, int i1, double *g)
 {
     XcGuess b2, vb;
-#pragma unroll 4
+XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         const float bk = R.bk(i);
         b2.add_product(bk, bk);
@@ -93,7 +93,7 @@ XC_HD void xh_spec1(const XhRows &R, int i0, int i1, const double *g, XcChunk *c
     XcSpec sb, sv;
     sb.begin(g[0]);
     sv.begin(g[1]);
-#pragma unroll 4
+XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         const double bk = (double)R.bk(i);
         sb.step(bk, bk);
@@ -110,7 +110,7 @@ XC_HD void xh_guess2(const XhRows &R, int i0, int i1, double b2, double vb, doub
     XcGuess fb2, fvb, bd, w, k0;
     fb2.set(b2);
     fvb.set(vb);
-#pragma unroll 4
+XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         const float bk = R.bk(i);
         if (i > 0) {
@@ -136,7 +136,7 @@ XC_HD void xh_spec2(const XhRows &R, int i0, int i1, double b2, double vb, const
     sbd.begin(g[0]);
     sw.begin(g[1]);
     sk0.begin(g[2]);
-#pragma unroll 4
+XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         const double bk = (double)R.bk(i);
         if (i > 0) {
@@ -160,7 +160,7 @@ XC_HD void xh_guess3(const XhRows &R, int i0, int i1, double b2, double bd, doub
     XcGuess fb2, fbd, k1;
     fb2.set(b2);
     fbd.set(bd);
-#pragma unroll 4
+XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         const float bk = R.bk(i);
         if (i > 0) {
@@ -178,7 +178,7 @@ XC_HD void xh_spec3(const XhRows &R, int i0, int i1, double b2, double bd, const
 {
     XcSpec sk;
     sk.begin(g[0]);
-#pragma unroll 4
+XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         const double bk = (double)R.bk(i);
         if (i > 0) {
@@ -205,7 +205,7 @@ XC_HD void xh_output(const XhRows &R, int i0, int i1, XhState s, int head, int m
                      const Emit &emit)
 {
     int g = xh_first_grid(i0, head, min_span);
-#pragma unroll 4
+XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         xh_run<XH_ALL>(R, i, i + 1, s);
         if (i == g) {
