@@ -177,33 +177,6 @@ MARS_GPU_API int mars_gpu_orthonormalize_col(size_t n, size_t m, double *v, cons
                                 double tol, double *w, long *dgks);
 
 /*
- *  mars_gpu_orthonormalize_noalloc: mars_gpu_orthonormalize on DEVICE arrays,
- *  queued on the caller's stream, allocating no device memory. It has no
- *  counterpart in the reference (its mars::cuda::orthonormalize allocates).
- *
- *  For callers that cannot let a library allocate: a process whose own pool
- *  (for example PyTorch's caching allocator) holds the device memory, so a
- *  cudaMalloc inside the library could fail; and a caller with work running on
- *  other streams, which a cudaFree would stall because it waits for the whole
- *  device.
- *
- *  B, x, Bo, Bx and s are device pointers with the meanings and layouts of
- *  mars_gpu_orthonormalize; mask (p ints) is a host array. s may be NULL.
- *  stream is a cudaStream_t (NULL: the default stream). The working memory is
- *  one fixed array of module-scope device memory (about 2.2 MB per device), so
- *  p <= MARS_GPU_NOALLOC_MAX_CANDIDATES and m * p <= MARS_GPU_NOALLOC_MAX_COEFS;
- *  larger problems are rejected with MARS_GPU_EINVAL. The caller clears
- *  nothing: every scratch value read is written earlier in the same call.
- *
- *  The first call on each device does the setup (loads the module and looks up
- *  the scratch address with that device current); make it before any stream
- *  capture. The call synchronises `stream` once (to read how many columns
- *  DGKS retried) and returns with the final scaling queued. All calls on one
- *  device share the one scratch array: calls that overlap -- from two host
- *  threads, or on two streams whose work can run at the same time -- race and
- *  give wrong results.
- */
-/*
  *  Differentiable expansion of a fitted model: the basis of mars.expand
  *  (mars.py:423-450) with the prediction pred = B beta, and its backward pass.
  *  No counterpart in the reference (its expand is numpy, without gradients).
@@ -234,12 +207,52 @@ MARS_GPU_API int mars_gpu_expand_backward(const int *kind, const int *parent, co
                              size_t ldx, size_t N, const float *g, float *dX, size_t lddx,
                              double *dbeta, double *dknot, void *workspace, void *stream);
 
+/*
+ *  mars_gpu_orthonormalize_noalloc: mars_gpu_orthonormalize on DEVICE arrays,
+ *  queued on the caller's stream, allocating no device memory. It has no
+ *  counterpart in the reference (its mars::cuda::orthonormalize allocates).
+ *
+ *  For callers that cannot let a library allocate: a process whose own pool
+ *  (for example PyTorch's caching allocator) holds the device memory, so a
+ *  cudaMalloc inside the library could fail; and a caller with work running on
+ *  other streams, which a cudaFree would stall because it waits for the whole
+ *  device.
+ *
+ *  B, x, Bo, Bx and s are device pointers with the meanings and layouts of
+ *  mars_gpu_orthonormalize; B has ncolB columns and every mask[j] must be below
+ *  ncolB (checked); mask (p ints) is a host array. s may be NULL. stream is a
+ *  cudaStream_t (NULL: the default stream). The working memory is one fixed
+ *  array of module-scope device memory (about 2.2 MB per device, held by every
+ *  device that loads the library until the process exits), so
+ *  p <= MARS_GPU_NOALLOC_MAX_CANDIDATES and m * p <= MARS_GPU_NOALLOC_MAX_COEFS;
+ *  larger problems are rejected with MARS_GPU_EINVAL before any work is queued.
+ *  The caller clears nothing: every scratch value read is written earlier in
+ *  the same call.
+ *
+ *  Each call looks up the scratch address with the calling thread's current
+ *  device (the first call on a device also loads the module there). The call
+ *  copies the mask from pageable host memory and synchronises `stream` once
+ *  (to read how many columns DGKS retried), so it cannot be issued while that
+ *  stream is being captured into a CUDA graph. It returns with the final
+ *  scaling queued. All calls on one device share the one scratch array: calls
+ *  that overlap -- from two host threads, or on two streams whose work can run
+ *  at the same time -- race and give wrong results.
+ */
 #define MARS_GPU_NOALLOC_MAX_CANDIDATES 4096
 #define MARS_GPU_NOALLOC_MAX_COEFS 262144
 MARS_GPU_API int mars_gpu_orthonormalize_noalloc(size_t n, size_t m, size_t p, const float *B,
-                                    size_t ldB, const float *x, const int *mask,
+                                    size_t ldB, size_t ncolB, const float *x, const int *mask,
                                     const float *Bo, size_t ldBo, float *Bx, size_t ldBx,
                                     double *s, double tol, void *stream, long *dgks);
+
+/*
+ *  Bytes currently handed out by the library's stream-ordered memory pool on
+ *  the calling thread's current device (cudaMemPoolAttrUsedMemCurrent): what
+ *  live handles hold. A diagnostic for tests (a call that allocates nothing
+ *  leaves it unchanged); never fails when a device is visible.
+ */
+MARS_GPU_API int mars_gpu_pool_used_bytes(size_t *out);
+
 
 #ifdef __cplusplus
 }

@@ -947,7 +947,7 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         }
     }
     std::vector<ExactResult> lo;
-    const int threads = std::max(1u, std::thread::hardware_concurrency());
+    const int threads = usable_cores();
     const int host_max = (int)env_double("MARS_GPU_MIXED_HOST_MAX", threads);
     if ((int)lo_q.size() <= host_max) {
         // few leftovers: the host cores, whose serial f64 chains are ~50x
@@ -1375,6 +1375,17 @@ int mars_gpu_get_stats(const mars_gpu_algo *a, mars_gpu_stats *out)
         }
     }
     return MARS_GPU_OK;
+}
+
+int mars_gpu_pool_used_bytes(size_t *out)
+{
+    return guarded([&] {
+        verify(out != nullptr, "null argument");
+        verify(mars_gpu_device_count() > 0, "no CUDA device is visible", MARS_GPU_ECUDA);
+        unsigned long long used = 0;  // the attribute is a 64-bit count
+        CUDA_CHECK(cudaMemPoolGetAttribute(device_pool(), cudaMemPoolAttrUsedMemCurrent, &used));
+        *out = (size_t)used;
+    });
 }
 
 int mars_gpu_orth_error(mars_gpu_algo *a, double *max_abs, double *rss)

@@ -20,6 +20,7 @@
 #include <mutex>
 #include <thread>
 
+#include <sched.h>
 #include <unistd.h>
 
 namespace mgpu {
@@ -66,7 +67,12 @@ class HostPool {
         }
         cv_.notify_all();
         fn(0);
-        while (pending_.load(std::memory_order_acquire) != 0) {
+        // the workers usually finish within microseconds of the caller; past
+        // a short spin, give the core away so a descheduled worker can run
+        for (int spin = 0; pending_.load(std::memory_order_acquire) != 0; ++spin) {
+            if (spin >= 1024) {
+                std::this_thread::yield();
+            }
         }
     }
 
@@ -77,6 +83,9 @@ class HostPool {
         for (;;) {
             unsigned e = epoch_.load(std::memory_order_acquire);
             for (int spin = 0; e == seen && spin < (1 << 16); ++spin) {
+                if (spin >= 1024) {
+                    std::this_thread::yield();
+                }
                 e = epoch_.load(std::memory_order_acquire);
             }
             if (e == seen) {
@@ -100,14 +109,32 @@ class HostPool {
 
 std::mutex g_pool_use;  // one append at a time uses the pool
 
+}  // namespace
+
+// Cores this process may run on: its CPU affinity mask (which a cgroup or
+// taskset narrows), else the hardware thread count.
+int usable_cores()
+{
+    cpu_set_t set;
+    CPU_ZERO(&set);
+    if (sched_getaffinity(0, sizeof(set), &set) == 0) {
+        const int c = CPU_COUNT(&set);
+        if (c > 0) {
+            return c;
+        }
+    }
+    return (int)std::max(1u, std::thread::hardware_concurrency());
+}
+
+namespace {
+
 // The pool of this process (none in a child forked after it was made: the
 // child has no worker threads).
 HostPool *host_pool()
 {
     static const pid_t owner = getpid();
     static HostPool *pool = [] {
-        const unsigned hc = std::thread::hardware_concurrency();
-        const int nt = (int)std::min(16u, std::max(1u, hc));
+        const int nt = std::min(16, usable_cores());
         return nt > 1 ? new HostPool(nt) : nullptr;  // lives until the process exits
     }();
     return getpid() == owner ? pool : nullptr;
@@ -309,7 +336,7 @@ void HostBasis::init(const float *X_, const float *y_, const float *w, size_t n_
     s.assign(p, 1.0f);
     std::vector<double> sq(p, 0.0);
     {
-        const int nt = (int)std::max<size_t>(1, std::min<size_t>(p, std::thread::hardware_concurrency()));
+        const int nt = (int)std::max<size_t>(1, std::min<size_t>(p, (size_t)usable_cores()));
         std::atomic<size_t> next{0};
         std::vector<std::thread> pool;
         for (int t = 0; t < nt; ++t) {

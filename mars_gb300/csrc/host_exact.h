@@ -51,6 +51,9 @@ struct ExactResult {
 ExactResult exact_candidate(const HostBasis &hb, int xcol, int bcol, const int32_t *perm,
                             int min_span, int head, int tail);
 
+// Cores this process may run on (its CPU affinity mask; at least 1).
+int usable_cores();
+
 // Evaluate a list of candidates on up to `threads` host threads.
 void exact_candidates(const HostBasis &hb, const std::vector<int> &xcol,
                       const std::vector<int> &bcol, const std::vector<const int32_t *> &perm,

@@ -10,8 +10,6 @@
 #include "common.cuh"
 #include "fp64.cuh"
 
-#include <mutex>
-
 using namespace mgpu;
 
 namespace {
@@ -35,24 +33,15 @@ constexpr size_t NA_BYTES = OFF_ONE + 256;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
-constexpr int NA_MAX_DEVICES = 64;
-std::mutex g_addr_mu;
-void *g_addr[NA_MAX_DEVICES] = {};
-
-// Address of the scratch on the current device, looked up once per device.
+// Address of the scratch on the current device. Looked up on every call (a
+// cheap runtime query), so a new primary context -- after cudaDeviceReset,
+// say -- never leaves a stale address behind.
 unsigned char *scratch_address()
 {
-    int dev = -1;
-    CUDA_CHECK(cudaGetDevice(&dev));
-    verify(dev >= 0 && dev < NA_MAX_DEVICES, "device ordinal out of range", MARS_GPU_ECUDA);
-    std::lock_guard<std::mutex> lock(g_addr_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        verify(p != nullptr, "scratch symbol has no device address", MARS_GPU_ECUDA);
-        g_addr[dev] = p;
-    }
-    return static_cast<unsigned char *>(g_addr[dev]);
+    void *p = nullptr;
+    CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    verify(p != nullptr, "scratch symbol has no device address", MARS_GPU_ECUDA);
+    return static_cast<unsigned char *>(p);
 }
 
 const float kOne = 1.0f;
@@ -62,7 +51,7 @@ const float kOne = 1.0f;
 extern "C" {
 
 int mars_gpu_orthonormalize_noalloc(size_t n, size_t m, size_t p, const float *B, size_t ldB,
-                                    const float *x, const int *mask, const float *Bo,
+                                    size_t ncolB, const float *x, const int *mask, const float *Bo,
                                     size_t ldBo, float *Bx, size_t ldBx, double *s, double tol,
                                     void *stream, long *dgks)
 {
@@ -79,7 +68,8 @@ int mars_gpu_orthonormalize_noalloc(size_t n, size_t m, size_t p, const float *B
         verify(m * p <= NA_MAX_T,
                "m * p exceeds the fixed scratch (at most MARS_GPU_NOALLOC_MAX_COEFS)");
         for (size_t j = 0; j < p; ++j) {
-            verify(mask[j] >= 0, "negative basis index in mask");
+            verify(mask[j] >= 0 && (size_t)mask[j] < ncolB,
+                   "basis index in mask outside the columns of B");
         }
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         unsigned char *base = scratch_address();

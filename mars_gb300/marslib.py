@@ -86,8 +86,9 @@ def load():
         "mars_gpu_orth_error": (i, [vp, dp, dp]),
         "mars_gpu_orthonormalize": (i, [sz, sz, sz, fp, sz, fp, ip, fp, sz, fp, sz, dp, d, lp]),
         "mars_gpu_orthonormalize_col": (i, [sz, sz, dp, fp, sz, d, dp, lp]),
-        "mars_gpu_orthonormalize_noalloc": (i, [sz, sz, sz, vp, sz, vp, ip, vp, sz, vp, sz, vp,
-                                                d, vp, lp]),
+        "mars_gpu_orthonormalize_noalloc": (i, [sz, sz, sz, vp, sz, sz, vp, ip, vp, sz, vp, sz,
+                                                vp, d, vp, lp]),
+        "mars_gpu_pool_used_bytes": (i, [ctypes.POINTER(sz)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -260,21 +261,30 @@ def orthonormalize_col(v, Bo, m, tol):
     return w.value, v, c.value
 
 
+def pool_used_bytes():
+    """Bytes the library's device memory pool has handed out (current device)."""
+    L = load()
+    v = ctypes.c_size_t(0)
+    check(L.mars_gpu_pool_used_bytes(ctypes.byref(v)))
+    return v.value
+
+
 # Limits of the fixed scratch of mars_gpu_orthonormalize_noalloc (mars_gpu.h).
 NOALLOC_MAX_CANDIDATES = 4096
 NOALLOC_MAX_COEFS = 262144
 
 
-def orthonormalize_noalloc(n, m, mask, B_ptr, ldB, x_ptr, Bo_ptr, ldBo, Bx_ptr, ldBx, s_ptr, tol,
-                           stream_ptr=0):
+def orthonormalize_noalloc(n, m, mask, B_ptr, ldB, ncolB, x_ptr, Bo_ptr, ldBo, Bx_ptr, ldBx,
+                           s_ptr, tol, stream_ptr=0):
     """mars_gpu_orthonormalize on caller-owned device arrays (integer device
     addresses), queued on `stream_ptr` (a cudaStream_t; 0 = default stream),
-    with no device allocation. mask is a host int array of parent columns.
-    Returns the number of columns DGKS retried."""
+    with no device allocation. mask is a host int array of parent columns,
+    each below ncolB (the columns of B). Returns the number of columns DGKS
+    retried."""
     L = load()
     mask = np.ascontiguousarray(mask, dtype=np.int32)
     c = ctypes.c_long(0)
-    check(L.mars_gpu_orthonormalize_noalloc(n, m, len(mask), B_ptr, ldB, x_ptr,
+    check(L.mars_gpu_orthonormalize_noalloc(n, m, len(mask), B_ptr, ldB, ncolB, x_ptr,
                                             _p(mask, ctypes.c_int), Bo_ptr, ldBo, Bx_ptr, ldBx,
                                             s_ptr or None, tol, stream_ptr or None,
                                             ctypes.byref(c)))

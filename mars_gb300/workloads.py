@@ -108,6 +108,14 @@ def batched_fits(count=256, seed=0, n_lo=1_000, n_hi=200_000, p_lo=5, p_hi=50,
     return fits
 
 
+def batched_fits_top(k=4, count=256, seed=0):
+    """The k fits of ``batched_fits(count, seed)`` with the largest n * p, in
+    their order within the batch (the top of the n and p ranges)."""
+    fits = batched_fits(count=count, seed=seed)
+    order = sorted(range(len(fits)), key=lambda i: -fits[i][0].shape[0] * fits[i][0].shape[1])
+    return [fits[i] for i in sorted(order[:k])]
+
+
 def digest(*arrays):
     """sha256 over the raw bytes of the arrays (to pin generated inputs)."""
     h = hashlib.sha256()

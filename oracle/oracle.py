@@ -13,7 +13,9 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = os.environ.get("MARS_REFERENCE_DIR", "/root/reference")
+# The reference checkout, when one is present: named by MARS_REFERENCE_DIR
+# (no default; without it only the port is built).
+REF_DIR = os.environ.get("MARS_REFERENCE_DIR")
 
 _PATHS = {
     "port": os.path.join(HERE, "_build", "libmars_oracle.so"),
@@ -34,11 +36,16 @@ _c_i32_p = ctypes.POINTER(ctypes.c_int32)
 def build(with_reference=None, quiet=True):
     """Compile the port (always) and the reference build (when its sources exist)."""
     targets = ["port"]
+    ref_dir = os.environ.get("MARS_REFERENCE_DIR") or REF_DIR
     if with_reference is None:
-        with_reference = os.path.isfile(os.path.join(REF_DIR, "marsalgo.cc"))
+        with_reference = bool(ref_dir) and os.path.isfile(os.path.join(ref_dir, "marsalgo.cc"))
     if with_reference:
+        if not ref_dir:
+            raise RuntimeError("MARS_REFERENCE_DIR must name the reference checkout")
         targets.append("ref")
-    cmd = ["make", "-C", HERE, "REF=" + REF_DIR, "PYTHON=" + (os.environ.get("PYTHON") or "python3")]
+    cmd = ["make", "-C", HERE, "PYTHON=" + (os.environ.get("PYTHON") or "python3")]
+    if ref_dir:
+        cmd.append("REF=" + ref_dir)
     out = subprocess.run(cmd + targets, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)

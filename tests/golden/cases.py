@@ -19,7 +19,16 @@ FIT_CASES = [
     "batched_small_1",
     "batched_small_2",
     "default_tail",
+    "precision_stress",
+    "batched_top_0",
+    "batched_top_1",
+    "batched_top_2",
+    "batched_top_3",
 ]
+# Fixtures that take minutes to hours of reference CPU time; the tests that
+# need them skip when they are absent.
+LARGE_CASES = ["precision_stress", "batched_top_0", "batched_top_1", "batched_top_2",
+               "batched_top_3"]
 EVAL_CASES = ["eval_planted_knot", "eval_ties"]
 EVAL_MAX_TERMS = 16
 
@@ -53,6 +62,13 @@ def fit_case(name):
         k = int(name.rsplit("_", 1)[1])
         fits = workloads.batched_fits(count=3, seed=4, n_hi=20_000, p_hi=12)
         X, y, kw = fits[k]
+    elif name == "precision_stress":
+        # the full precision-stress workload at the reference's default tail span
+        X, y, kw = workloads.precision_stress()
+        kw["tail_span"] = 0.02
+    elif name.startswith("batched_top_"):
+        k = int(name.rsplit("_", 1)[1])
+        X, y, kw = workloads.batched_fits_top(4)[k]
     elif name == "default_tail":
         X, y, _ = workloads.hinge_search(n=12_000, p=6, seed=9)
         kw = dict(max_terms=13)

@@ -3,8 +3,7 @@
 
 Runs the reference's own ``mars.py`` over its own ``marslib`` binding, built
 from the reference sources by ``make -C oracle ref`` into ``oracle/_ref/``.
-This needs the reference checkout (default /root/reference, override with
-MARS_REFERENCE_DIR); the fixtures it writes are small JSON/npz files that the
+This needs the reference checkout, named by MARS_REFERENCE_DIR; the fixtures it writes are small JSON/npz files that the
 tests read anywhere, with no access to the reference.
 
 Each term-path fixture stores, per fitted basis row: type, parent basis,
@@ -24,7 +23,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("MARS_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("MARS_REFERENCE_DIR")
 sys.path.insert(0, ROOT)
 
 from mars_gb300 import workloads  # noqa: E402
@@ -32,6 +31,8 @@ from tests.golden import cases  # noqa: E402
 
 
 def _import_reference():
+    if not REF or not os.path.isfile(os.path.join(REF, "mars.py")):
+        raise SystemExit("set MARS_REFERENCE_DIR to the reference checkout")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + REF],
                    check=True, capture_output=True)
     sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))

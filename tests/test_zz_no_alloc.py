@@ -46,7 +46,7 @@ def _noalloc(torch, lib, B, x, mask, Bo, m, tol, stream):
     torch.cuda.synchronize()
     outs = []
     for _ in range(2):
-        dgks = lib.orthonormalize_noalloc(n, m, mask, dB.data_ptr(), n, dx.data_ptr(),
+        dgks = lib.orthonormalize_noalloc(n, m, mask, dB.data_ptr(), n, B.shape[1], dx.data_ptr(),
                                           dBo.data_ptr(), Bo.shape[1], dBx.data_ptr(), n,
                                           ds.data_ptr(), tol, stream.cuda_stream)
         stream.synchronize()
@@ -84,13 +84,19 @@ def test_noalloc_default_stream_and_null_s(gpu):
     dBo = torch.from_numpy(Bo).to(dev)
     dBx = torch.zeros((p, n), dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
-    marslib.orthonormalize_noalloc(n, m, mask, dB.data_ptr(), n, dx.data_ptr(), dBo.data_ptr(),
-                                   Bo.shape[1], dBx.data_ptr(), n, 0, tol, 0)
-    free_before = torch.cuda.mem_get_info(0)[0]
-    marslib.orthonormalize_noalloc(n, m, mask, dB.data_ptr(), n, dx.data_ptr(), dBo.data_ptr(),
-                                   Bo.shape[1], dBx.data_ptr(), n, 0, tol, 0)
+    marslib.orthonormalize_noalloc(n, m, mask, dB.data_ptr(), n, B.shape[1], dx.data_ptr(),
+                                   dBo.data_ptr(), Bo.shape[1], dBx.data_ptr(), n, 0, tol, 0)
     torch.cuda.synchronize()
-    assert torch.cuda.mem_get_info(0)[0] == free_before  # no device allocation in the call
+    free_before = torch.cuda.mem_get_info(0)[0]
+    pool_before = marslib.pool_used_bytes()
+    marslib.orthonormalize_noalloc(n, m, mask, dB.data_ptr(), n, B.shape[1], dx.data_ptr(),
+                                   dBo.data_ptr(), Bo.shape[1], dBx.data_ptr(), n, 0, tol, 0)
+    torch.cuda.synchronize()
+    # no device allocation in the call: neither from the driver nor from the
+    # library's own pool (which keeps freed memory cached, so a pool
+    # allocation would not show in the free device memory)
+    assert torch.cuda.mem_get_info(0)[0] == free_before
+    assert marslib.pool_used_bytes() == pool_before
     np.testing.assert_array_equal(dBx.cpu().numpy().T, Bx_ref)
 
 
@@ -105,8 +111,12 @@ def test_noalloc_rejects_oversize(gpu):
     ptr = buf.data_ptr()
     too_many = np.zeros(marslib.NOALLOC_MAX_CANDIDATES + 1, np.int32)
     with pytest.raises(RuntimeError, match="too many candidate columns"):
-        marslib.orthonormalize_noalloc(n, 1, too_many, ptr, n, ptr, ptr, 1, ptr, n, 0, 1e-14)
+        marslib.orthonormalize_noalloc(n, 1, too_many, ptr, n, 1, ptr, ptr, 1, ptr, n, 0, 1e-14)
     m = marslib.NOALLOC_MAX_COEFS // 64 + 1
     with pytest.raises(RuntimeError, match="exceeds the fixed scratch"):
-        marslib.orthonormalize_noalloc(n, m, np.zeros(64, np.int32), ptr, n, ptr, ptr, m, ptr,
+        marslib.orthonormalize_noalloc(n, m, np.zeros(64, np.int32), ptr, n, 1, ptr, ptr, m, ptr,
                                        n, 0, 1e-14)
+    # a parent index past the columns of B is refused before any device access
+    with pytest.raises(RuntimeError, match="outside the columns of B"):
+        marslib.orthonormalize_noalloc(n, 1, np.array([0, 8], np.int32), ptr, n, 8, ptr, ptr, 1,
+                                       ptr, n, 0, 1e-14)
