@@ -1,27 +1,41 @@
 #!/usr/bin/env python3
 """Forward-pass benchmark on one GB300 (or N independent replicas).
 
-One step = one complete MARS forward pass (mars.fit) of the full hinge-search
-workload: X n=100,000 x p=20 iid N(0,1) float32, y = 6 random hinges + 3 hinge
-products + N(0, 0.5^2), max_terms=31, max_degree=2, tail_span=0 (synthetic,
-seeded; mars_gb300/workloads.py). Metric: knot evaluations per second (grid
-cuts scored by the hinge sweep, summed over every epoch and candidate), and
-the fit time.
+Default workload (the metric's own config): precision stress, X n=1,000,000 x
+p=100 float32 with AR(1) column correlation rho=0.9 and 5 near-duplicate
+columns, y = 2 x_a + 3 x_b + x_a x_b over 5 column pairs + N(0,1),
+max_terms=63, max_degree=3, tail_span=0.02 (the reference's default; synthetic,
+seeded: mars_gb300/workloads.py), in mixed precision.
 
-value        knot-evals/s over the device span of the fits (CUDA events on the
-             library's stream from the first eval to the last append; X, y
-             already resident in HBM), whole job (all ranks) / max rank time.
-e2e          the same metric through mars.fit with host arrays: host->device
-             upload of X, y, w and every eval's result download inside the
-             timed region (wall clock with the device synchronised).
+Step. The fit has one epoch per selected term pair (~31 for 63 terms), each an
+eval of every (input, parent) candidate plus the append of the chosen pair;
+one step is one epoch. The first W epochs of the fit are the warm-up, the next
+K are timed, and the fit then runs to its end untimed (so the term path can
+be checked against the reference's); with W + K past the fit's epochs the
+timed region continues into a second fit. Inputs are far larger than the
+129 MB L2 (X 400 MB, the projected candidates ~24 GB per epoch), so L2 is not
+flushed between steps. --workload hinge_search (config 2) keeps one full fit
+per step.
+
+value        knot-evals/s over the device span of the timed epochs (CUDA
+             events on the library's stream; X, y resident in HBM), whole job
+             (all ranks) / max rank time.
+e2e          the same knot-evals over the host wall time of those epochs
+             through mars.fit (host mask in, host results out every epoch)
+             plus the fit's upload of X, y, w charged in full.
+fp64         the plain FP64 GPU forward pass of the same workload: fit time,
+             the same timed epochs, speed-up, identical term path.
 roofline     the dominant kernel of the timed region against the measured
              peaks in MEASURED_PEAKS.json (HBM GB/s or tensor TFLOP/s).
 cpu_baseline the CPU oracle (the C restatement of the reference CPU path) on
-             the host cores, one fit of the same workload.
+             the host cores, on a sample of the same epochs' candidates.
 
---impl reference times that CPU implementation alone on the same workload.
-Under torchrun (N > 1) every rank runs its own replica on its own GPU (the
-fit does not exchange data between GPUs); timing is max over ranks.
+--impl reference times that CPU implementation alone: step k is one eval of
+a sample of the candidates of epoch W + k (16 input columns, 3 parents each,
+on the basis the reference's own fit had built by then, replayed from the
+committed reference fixture). Under torchrun (N > 1) every rank runs its own
+replica on its own GPU (the fit does not exchange data between GPUs); timing
+is max over ranks.
 """
 import argparse
 import json
@@ -51,6 +65,8 @@ WORKLOADS = {
     "precision_stress": "precision_stress n=1000000 p=100 AR(1) rho=0.9 + 5 near-duplicates, "
                         "max_terms=63 max_degree=3 tail_span=0.02 (config 3; the reference's "
                         "default tail span)",
+    "precision_stress_small": "precision_stress n=30000 p=20 AR(1) rho=0.9 + 3 near-duplicates, "
+                              "max_terms=21 tail_span=0 (a small case of config 3's shape)",
     "plain_fit": "plain_fit n=10000 p=2 linear_only max_terms=17 (config 1)",
     "batched": "256 independent fits, n log-uniform 1e3..2e5, p uniform 5..50, 4 random hinges "
                "+ N(0,1) noise, max_terms=21, tail_span=0 (config 4)",
@@ -65,9 +81,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default=os.environ.get("MARS_BENCH_PRECISION", "fp64"),
+    ap.add_argument("--precision", default=os.environ.get("MARS_BENCH_PRECISION", "mixed"),
                     choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="hinge_search", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="precision_stress", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the FP64 comparator fits when timing the mixed path")
@@ -83,7 +99,13 @@ def workload(name):
         X, y, kw = workloads.precision_stress()
         kw["tail_span"] = 0.02
         return X, y, kw
+    if name == "precision_stress_small":
+        return workloads.precision_stress(n=30_000, p=20, n_dup=3, seed=5, max_terms=21)
     return workloads.plain_fit()
+
+
+# workloads timed one epoch per step (the others: one fit per step)
+EPOCH_WORKLOADS = ("precision_stress", "precision_stress_small")
 
 
 class Counting:
@@ -246,11 +268,28 @@ def traffic_ratio(precision, workload_name, kernel):
     return None
 
 
+def limiter(precision, workload_name, kernel):
+    """What the committed ncu summary of `kernel` on this workload says bounds
+    it (profiles/limiters.txt), with the summary's file name; None when no
+    capture of this workload exists."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "limiters.txt")) as f:
+            for line in f:
+                if line.startswith("#") or "|" not in line:
+                    continue
+                key, text, src = [x.strip() for x in line.split("|")]
+                if key.split() == [precision, workload_name, kernel]:
+                    return {"limiter": text, "capture": "profiles/" + src}
+    except OSError:
+        pass
+    return {"limiter": None, "capture": "none of this workload"}
+
+
 def roofline(st, workload_name, precision):
     """The dominant kernel against its roofline. The hinge sweep is charged
-    with its algorithmic bytes against HBM bandwidth. The FP64 sweep is bound
-    by the FP64 pipe and the fast sweep by the latency of its sequential row
-    walk (the captures in profiles/), so the fraction is small by construction."""
+    with its algorithmic bytes against HBM bandwidth; the projection with its
+    algorithmic FLOPs against the bf16 tensor peak. What bounds the kernel
+    comes from the committed capture of this workload, when there is one."""
     hbm, bf16, src = peaks()
     phases = {"sweep": st["ms_sweep"], "project": st["ms_project"]}
     dom = max(phases, key=phases.get)
@@ -263,14 +302,13 @@ def roofline(st, workload_name, precision):
                 "unit": "GB/s", "frac": ach / hbm, "peak_source": src,
                 "algorithmic_bytes_per_launch": per_launch,
                 "traffic": None if ratio is None else ratio * per_launch,
-                "limiter": ("FP64 pipe (ncu: 57% active) and FP64 dependency latency; DRAM < 1% "
-                            "of peak" if precision == "fp64" else
-                            "latency of each warp's sequential walk over the sorted rows "
-                            "(ncu: issue 38% active, no FP64, DRAM 6% of peak)")}
+                **limiter(precision, workload_name, kern)}
     ms = max(st["ms_project"], 1e-9)
     ach = st["project_flops"] / (ms * 1e-3) / 1e12
-    return {"kernel": "projection", "bound": "tensor", "achieved": ach, "peak": bf16,
-            "unit": "TFLOP/s", "frac": ach / bf16, "peak_source": src, "traffic": None}
+    kern = "projection"
+    return {"kernel": kern, "bound": "tensor", "achieved": ach, "peak": bf16,
+            "unit": "TFLOP/s", "frac": ach / bf16, "peak_source": src, "traffic": None,
+            **limiter(precision, workload_name, kern)}
 
 
 def cpu_threads():
@@ -449,8 +487,331 @@ def run_expand(args):
     return 0
 
 
+STAT_KEYS = ("ms_project", "ms_sweep", "ms_dgks", "ms_normalize", "ms_append", "ms_sort",
+             "ms_redecide", "ms_gather", "ms_redecide_gpu", "project_flops", "sweep_bytes",
+             "evals", "candidates", "redecided", "redecided_flagged", "kernel_launches",
+             "h2d_bytes", "d2h_bytes", "knot_evals", "dgks_fired")
+
+
+class EpochSteps:
+    """Step boundaries at the epochs of one or more fits.
+
+    Fed by the fit's callback after every epoch (eval + append). The timed
+    region opens after `warmup` epochs and closes after `warmup + steps`;
+    across it the handle's device span (CUDA events on its stream), the host
+    wall time and the counters are accumulated, handle by handle when the
+    region spans two fits."""
+
+    def __init__(self, warmup, steps, on_open=None, on_close=None):
+        self.W, self.K = warmup, steps
+        self.on_open, self.on_close = on_open, on_close
+        self.done = 0
+        self.timing = False
+        self.closed = False
+        self.algo = None
+        self.t_create = []      # (seconds, h2d bytes) of each fit's construction
+        self.span_ms = 0.0
+        self.wall = 0.0
+        self.acc = {k: 0.0 for k in STAT_KEYS}
+        self.epoch_ms = []      # device ms of every epoch of the first fit
+        self._prev_span = 0.0
+
+    def _sync(self):
+        import torch
+
+        torch.cuda.synchronize()
+
+    def created(self, algo, seconds):
+        if self.timing:
+            self._fold(self.algo)  # the old handle's share so far
+        self.algo = algo
+        st = algo.stats()
+        self.t_create.append((seconds, st["h2d_bytes"]))
+        self._prev_span = 0.0
+        if self.timing:
+            self._base = st  # the new fit's upload ran inside the open region
+
+    def _fold(self, algo):
+        st = algo.stats()
+        self.span_ms += st["ms_span"] - self._base["ms_span"]
+        for k in STAT_KEYS:
+            self.acc[k] += st[k] - self._base[k]
+
+    def epoch(self):
+        st = self.algo.stats()
+        self.epoch_ms.append(st["ms_span"] - self._prev_span)
+        self._prev_span = st["ms_span"]
+        self.done += 1
+        if not self.timing and not self.closed and self.done == self.W:
+            self._sync()
+            if self.on_open:
+                self.on_open()
+            self.timing = True
+            self._base = self.algo.stats()
+            self._t0 = time.perf_counter()
+        elif self.timing and self.done == self.W + self.K:
+            self._sync()
+            self.wall += time.perf_counter() - self._t0
+            self._fold(self.algo)
+            self.timing = False
+            self.closed = True
+            if self.on_close:
+                self.on_close()
+
+
+def epoch_fit(X, y, kw, precision, steps):
+    """One fit through the public fit loop with the epoch boundaries of
+    `steps`; returns (model, wall seconds, final stats, knot-evals)."""
+    from mars_gb300 import marslib
+    from mars_gb300.mars import forward_pass
+
+    def factory(X_, y_, w_, mt):
+        t0 = time.perf_counter()
+        a = marslib.MarsAlgo(X_, y_, w_, mt)
+        a.set_precision(precision)
+        steps.created(a, time.perf_counter() - t0)
+        return a
+
+    lib = Counting(factory)
+    t0 = time.perf_counter()
+    model = forward_pass(lib, X, y, None, callback=lambda *a: steps.epoch(), **kw)
+    wall = time.perf_counter() - t0
+    st = lib.algo.stats()
+    st["orth_max"], st["rss"] = lib.algo.orth_error()
+    return model, wall, st, lib.knot_evals
+
+
+def epoch_grid(X, kw):
+    from mars_gb300 import workloads
+
+    n, p = X.shape
+    endspan = max(int(n * kw.get("tail_span", 0.02)), 1)
+    alpha = 1 / p
+    min_span = max(int(-np.log2(-np.log(1 - alpha) / (n * alpha)) / 2.5), 1)
+    return endspan, min_span, workloads.knot_evals(n, endspan, min_span)
+
+
+def parents_of_model(path):
+    """Input columns along each basis' parent chain, from a term path."""
+    parents = [[]]
+    for kind, b, x, _h in path[1:]:
+        parents.append(parents[b] + [x])
+    return parents
+
+
+def cpu_epoch_sample(X, y, kw, path, epoch, algo_state, threads, ncols=16, nparents=3):
+    """Time the oracle port on a sample of the candidates of `epoch`: the
+    basis the fit had built by then (replayed from `path`, the fit's term
+    sequence, onto algo_state["algo"] as needed), `ncols` input columns and
+    `nparents` allowed parents of each (seeded), one eval call with `threads`
+    host threads. Returns (seconds, knot-evals)."""
+    import oracle
+
+    if not oracle.available("port"):
+        oracle.build(with_reference=False)
+    n, p = X.shape
+    if algo_state.get("algo") is None:
+        w = np.ones(n, dtype=np.float32)
+        algo_state["algo"] = oracle.OracleAlgo(X, y, w, kw["max_terms"], kind="port")
+        algo_state["epochs"] = 0
+        algo_state["row"] = 1
+    algo = algo_state["algo"]
+    # epochs append one term ('l') or a pair ('+', '-')
+    while algo_state["epochs"] < epoch and algo_state["row"] < len(path):
+        r = algo_state["row"]
+        kind, b, x, h = path[r]
+        algo.append(kind, x, b, np.nan if h is None else h)
+        r += 1
+        if kind == "+" and r < len(path) and path[r][0] == "-":
+            kind, b, x, h = path[r]
+            algo.append(kind, x, b, h)
+            r += 1
+        algo_state["row"] = r
+        algo_state["epochs"] += 1
+    m = algo.nbasis()
+    parents = parents_of_model(path[:m])
+    max_degree = kw.get("max_degree", 3)
+    rng = np.random.default_rng(1000 + epoch)
+    mask = np.zeros((p, m), dtype=bool)
+    for q in range(ncols):
+        i = (epoch * ncols + q) % p
+        ok = [j for j in range(m) if len(parents[j]) < max_degree and i not in parents[j]]
+        for j in rng.permutation(ok)[:nparents]:
+            mask[i, j] = True
+    endspan, min_span, grid = epoch_grid(X, kw)
+    t0 = time.perf_counter()
+    algo.eval(mask, min_span, endspan, False, threads)
+    return time.perf_counter() - t0, int(mask.sum()) * grid
+
+
+def path_epochs(path):
+    """Epochs of a fit with this term path: one per linear term or hinge pair."""
+    e, r = 0, 1
+    while r < len(path):
+        r += 2 if path[r][0] == "+" and r + 1 < len(path) and path[r + 1][0] == "-" else 1
+        e += 1
+    return max(e, 1)
+
+
+def reference_path(workload_name):
+    path = os.path.join(ROOT, "tests", "golden", workload_name + ".json")
+    if not os.path.isfile(path):
+        return None
+    with open(path) as f:
+        g = json.load(f)
+    return [(r["type"], r["basis"], r["input"], r["hinge"]) for r in g["model"]]
+
+
+def run_reference_epochs(args):
+    """--impl reference on the epoch workload: the oracle port, step k = one
+    eval of a sample of epoch W + k's candidates (cpu_epoch_sample)."""
+    if RANK != 0:
+        return 0
+    X, y, kw = workload(args.workload)
+    path = reference_path(args.workload)
+    base = {"impl": "reference", "metric": METRIC, "config": {"workload": WORKLOADS[args.workload]}}
+    if path is None:
+        base["unavailable"] = "no reference term path committed for this workload"
+        print(json.dumps(base))
+        return 0
+    threads = cpu_threads()
+    state = {}
+    epochs = path_epochs(path)
+    for e in range(args.warmup):
+        cpu_epoch_sample(X, y, kw, path, e % epochs, state, threads)
+    total_t, total_k = 0.0, 0
+    for k in range(args.steps):
+        e = (args.warmup + k) % epochs
+        if e < state.get("epochs", 0):
+            state.clear()  # past the fit's last epoch: start the basis again
+        dt, kn = cpu_epoch_sample(X, y, kw, path, e, state, threads)
+        total_t += dt
+        total_k += kn
+    value = total_k / total_t
+    line = dict(base)
+    line.update({
+        "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "per step: 16 input columns x 3 parents of epoch W+k's "
+                                   "candidates on the reference fit's basis at that epoch"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    })
+    print(json.dumps(line))
+    return 0
+
+
+def run_epoch_steps(args):
+    """Default: the config-3 fit, one step per epoch (module docstring)."""
+    tdist = dist()
+    from mars_gb300 import marslib
+
+    marslib.load()
+    X, y, kw = workload(args.workload)
+    clocks = Clocks() if RANK == 0 else None
+
+    def opened():
+        if tdist is not None:
+            tdist.barrier()
+        if clocks:
+            clocks.start()
+
+    def closed():
+        if tdist is not None:
+            tdist.barrier()
+
+    steps = EpochSteps(args.warmup, args.steps, opened, closed)
+    fits = []
+    while not steps.closed:
+        fits.append(epoch_fit(X, y, kw, args.precision, steps))
+        if len(fits) > 1 + (args.warmup + args.steps) // 2:
+            raise RuntimeError("the fit stops before its epochs reach the timed region")
+    clk = clocks.stop() if clocks else None
+    model, fit_wall, st, _ = fits[0]
+    acc = steps.acc
+    t_dev = allmax(tdist, steps.span_ms * 1e-3)
+    create_s, create_h2d = steps.t_create[0]
+    t_e2e = allmax(tdist, steps.wall + create_s)
+    k_all = allsum(tdist, acc["knot_evals"])
+    epochs_fit = len(steps.epoch_ms) if len(fits) == 1 else None
+    line = {
+        "metric": METRIC,
+        "value": k_all / t_dev,
+        "unit": UNIT,
+        "n_gpus": WORLD,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_dev / args.steps,
+        "fit_time_s": st["ms_span"] * 1e-3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32 with f64 carries; f64 re-decision",
+        "precision": args.precision,
+        "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload],
+                   "step": "one epoch of the fit (eval of every candidate + append); epochs "
+                           "%d..%d of the fit timed" % (args.warmup, args.warmup + args.steps - 1),
+                   "l2": "not flushed: inputs larger than L2 (X 400 MB)",
+                   "parallelism": "replicas" if WORLD > 1 else "single GPU"},
+        "e2e": {"value": k_all / t_e2e, "unit": UNIT,
+                "h2d_bytes_per_step": int((acc["h2d_bytes"] + create_h2d) / args.steps),
+                "d2h_bytes_per_step": int(acc["d2h_bytes"] / args.steps),
+                "note": "host wall time of the timed epochs through the fit loop plus the "
+                        "fit's X, y, w upload"},
+        "gpu_launches": int(acc["kernel_launches"]),
+        "knot_evals_per_step": int(acc["knot_evals"] / args.steps),
+        "epochs_in_fit": epochs_fit,
+        "terms": len(model),
+        "fit_wall_s": fit_wall,
+        "roofline": roofline(acc, args.workload, args.precision),
+        "phase_ms_per_step": {k[3:]: acc[k] / args.steps for k in STAT_KEYS if
+                              k.startswith("ms_")},
+        "clocks": clk,
+        "orthogonality": {"max_abs_QtQ_minus_I": st["orth_max"], "rss": st["rss"]},
+    }
+    if args.precision == "mixed":
+        line["redecided_fraction"] = acc["redecided"] / max(1, acc["candidates"])
+    ref = reference_path(args.workload)
+    if ref is not None:
+        line["term_path_identical_to_reference"] = path_of(model) == ref
+    if args.precision == "mixed" and not args.no_compare:
+        fsteps = EpochSteps(args.warmup, args.steps)
+        fmodel, _, fst, _ = epoch_fit(X, y, kw, "fp64", fsteps)
+        fp_timed = sum(fsteps.epoch_ms[args.warmup:args.warmup + args.steps]) * 1e-3
+        my_timed = (sum(steps.epoch_ms[args.warmup:args.warmup + args.steps]) * 1e-3
+                    if len(fits) == 1 else None)
+        line["fp64"] = {"fit_time_s": fst["ms_span"] * 1e-3,
+                        "value": (acc["knot_evals"] / fp_timed) if fp_timed else None,
+                        "speedup": fst["ms_span"] / max(st["ms_span"], 1e-9),
+                        "speedup_timed_epochs": (fp_timed / my_timed) if my_timed else None}
+        line["term_path_identical_to_fp64"] = path_of(model) == path_of(fmodel)
+        line["orthogonality"]["fp64_max_abs_QtQ_minus_I"] = fst["orth_max"]
+        line["orthogonality"]["rss_rel_err_vs_fp64"] = (
+            abs(st["rss"] - fst["rss"]) / max(abs(fst["rss"]), 1e-300))
+    if RANK == 0 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        e = args.warmup + args.steps // 2
+        dt, kn = cpu_epoch_sample(X, y, kw, path_of(model), e, {}, threads)
+        line["cpu_baseline"] = {"value": kn / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "16 input columns x 3 parents of epoch %d's "
+                                          "candidates, one eval" % e,
+                                "seconds": dt}
+    if RANK == 0:
+        print(json.dumps(line))
+    if tdist is not None:
+        tdist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload in EPOCH_WORKLOADS:
+        if args.impl == "reference":
+            return run_reference_epochs(args)
+        return run_epoch_steps(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":

@@ -66,3 +66,37 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert line["ms_per_step"] > 0 and line["e2e"]["value"] == line["value"]
     assert line["cpu_baseline"]["kind"] == "port"
     assert line["steps"] == 1 and line["warmup"] == 3
+
+
+def test_reference_arm_epoch_steps():
+    """The epoch-step reference arm (the default workload's): each step one
+    eval of a sample of an epoch's candidates on the reference fit's basis
+    replayed from its fixture; here on the small case of the same shape."""
+    cmd = [sys.executable, "bench.py", "--impl", "reference", "--steps", "2", "--warmup", "3",
+           "--workload", "precision_stress_small"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    line = lines[0]
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["steps"] == 2 and line["warmup"] == 3
+    assert line["cpu_baseline"]["kind"] == "port"
+
+
+def test_epoch_sample_replays_the_reference_basis():
+    """The sampled state is the reference fit's basis at that epoch: its
+    column count follows the term path, and each sampled candidate obeys the
+    degree and self-interaction rules."""
+    import bench
+    from tests.golden import cases
+
+    X, y, w, kw = cases.fit_case("precision_stress_small")
+    path = bench.reference_path("precision_stress_small")
+    state = {}
+    dt, kn = bench.cpu_epoch_sample(X, y, kw, path, 3, state, 2, ncols=4, nparents=2)
+    assert dt > 0 and kn > 0
+    assert state["epochs"] == 3
+    m = state["algo"].nbasis()
+    assert 1 + 3 <= m <= 1 + 6
+    assert bench.path_epochs(path) >= 3
