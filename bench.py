@@ -711,6 +711,7 @@ def run_epoch_steps(args):
     marslib.load()
     X, y, kw = workload(args.workload)
     clocks = Clocks() if RANK == 0 else None
+    clk = {}
 
     def opened():
         if tdist is not None:
@@ -719,6 +720,8 @@ def run_epoch_steps(args):
             clocks.start()
 
     def closed():
+        if clocks:
+            clk["v"] = clocks.stop()
         if tdist is not None:
             tdist.barrier()
 
@@ -728,7 +731,7 @@ def run_epoch_steps(args):
         fits.append(epoch_fit(X, y, kw, args.precision, steps))
         if len(fits) > 1 + (args.warmup + args.steps) // 2:
             raise RuntimeError("the fit stops before its epochs reach the timed region")
-    clk = clocks.stop() if clocks else None
+    clk = clk.get("v")
     model, fit_wall, st, _ = fits[0]
     acc = steps.acc
     t_dev = allmax(tdist, steps.span_ms * 1e-3)

@@ -820,6 +820,17 @@ int fast_sweep_mid(int head, int tail, int n)
     return std::max(0, std::min((head + tail) / 2, n - 1));
 }
 
+void fast_norms_moments(cudaStream_t st, const float *Bx, int n, const float *y, double tol,
+                        const FillSrc &src, int P, double *s, double *ybx, double *mom,
+                        long long *launches)
+{
+    k_fast_norms<<<(unsigned)P, 256, 0, st>>>(Bx, n, y, tol, s, ybx);
+    LAUNCH_CHECK();
+    k_parent_moments<<<(unsigned)P, 256, 0, st>>>(src, n, mom);
+    LAUNCH_CHECK();
+    *launches += 2;
+}
+
 void fast_project(cudaStream_t st, const FillSrc &src, const float *BoC, int n, int m, int P,
                   const float *y, double tol, const FastScratch &ws, long long *launches)
 {
@@ -862,11 +873,7 @@ void fast_project(cudaStream_t st, const FillSrc &src, const float *BoC, int n, 
         LAUNCH_CHECK();
         *launches += 3;
     }
-    k_fast_norms<<<(unsigned)P, 256, 0, st>>>(ws.Bx, n, y, tol, ws.s, ws.ybx);
-    LAUNCH_CHECK();
-    k_parent_moments<<<(unsigned)P, 256, 0, st>>>(src, n, ws.mom);
-    LAUNCH_CHECK();
-    *launches += 2;
+    fast_norms_moments(st, ws.Bx, n, y, tol, src, P, ws.s, ws.ybx, ws.mom, launches);
 }
 
 static size_t fast_sweep_smem(int m, int w, int stages) { return FastSweepSmem(m, w, stages).total; }

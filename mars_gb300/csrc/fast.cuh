@@ -28,6 +28,12 @@ int fast_ksplit(int n);
 void fast_project(cudaStream_t st, const FillSrc &src, const float *BoC, int n, int m, int P,
                   const float *y, double tol, const FastScratch &ws, long long *launches);
 
+// s = ||Bx||^2, ybx = scale(s) (Bx . y) and the parent moments mom (the last
+// steps of fast_project).
+void fast_norms_moments(cudaStream_t st, const float *Bx, int n, const float *y, double tol,
+                        const FillSrc &src, int P, double *s, double *ybx, double *mom,
+                        long long *launches);
+
 // Chunked FP32 / FP64-carry hinge sweep of every candidate, in two halves:
 // tasks with dir 0 sweep from the top and score the cuts up to
 // fast_sweep_mid(), tasks with dir 1 sweep the mirror hinge from the bottom

@@ -1,0 +1,838 @@
+// Tensor-core projection of the mixed-precision fast pass (tc.cuh).
+//
+// Two kernels, both issuing tcgen05.mma (kind::tf32, one elected thread per
+// CTA, accumulators in tensor memory) with the FP32 operands split into two
+// TF32 terms (3 products per K step, FP32 accumulation):
+//
+//   k_tc_tgemm    T^T (P x m) = src^T Bo: tile = 128 candidates x N = m
+//                 padded to 16, K = the rows of one split of the n rows, 32 at
+//                 a time. Bo (hi, lo) arrives by TMA from the column-major
+//                 split copies; the candidate operand (hi, lo) is formed by
+//                 eight producer warps from its source columns and written in
+//                 the same 128-byte-swizzled K-major layout. Partials per
+//                 split are summed in FP64 in a fixed order (k_tc_treduce).
+//   k_tc_project  Bx (n x P) = src - Bo T: persistent, tile = 128 rows x 64
+//                 candidates, K = m padded to 32; Bo rows (hi, lo) and T
+//                 (hi, lo) both by TMA, two accumulator buffers in tensor
+//                 memory so the epilogue of one tile overlaps the MMAs of the
+//                 next; the epilogue subtracts from the source column and
+//                 stores Bx column-major (coalesced across a warp's rows).
+//
+// Every wait on an mbarrier is bounded (about four seconds of global time):
+// on expiry the waiting thread records MARS_GPU_ETIMEOUT in the error word,
+// raises the block's abort flag, and every thread winds down to the common
+// exit, where in-flight TMA copies and MMAs are waited for (again bounded)
+// and the tensor memory is freed.
+#include "tc.cuh"
+
+#include "../../include/mars_gpu.h"
+#include "fast.cuh"
+
+#include <cuda.h>
+
+#include <algorithm>
+#include <mutex>
+
+namespace mgpu {
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// PTX helpers (sm_100 family: mbarrier, TMA, tcgen05)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+
+constexpr unsigned long long TC_WAIT_NS = 4000000000ull;  // 4 s
+
+// Waits for the phase of `bar` with parity `parity`. Returns false when the
+// block is aborting (flag raised elsewhere) or when this wait ran out, in
+// which case it raises the flag and records the error. With `drain` set the
+// abort flag is ignored (used at exit to let in-flight work land).
+__device__ __noinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
+                                       int *err, bool drain = false)
+{
+    const unsigned long long t0 = global_ns();
+    for (uint32_t it = 0;; ++it) {
+        if (mbar_try(bar, parity)) {
+            return true;
+        }
+        if (!drain && *abort_flag) {
+            return false;
+        }
+        if ((it & 63) == 63) {
+            if (global_ns() - t0 > TC_WAIT_NS) {
+                *abort_flag = 1;
+                atomicExch(err, MARS_GPU_ETIMEOUT);
+                return false;
+            }
+            __nanosleep(128);
+        }
+    }
+}
+
+// mbar_wait by lane 0 of the warp, its result given to every lane.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t *bar, uint32_t parity,
+                                               volatile int *abort_flag, int *err)
+{
+    bool ok = true;
+    if ((threadIdx.x & 31) == 0) {
+        ok = mbar_wait(bar, parity, abort_flag, err);
+    }
+    return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+}
+
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap *map)
+{
+    asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+// Whole warp: allocate `ncols` tensor-memory columns, address into *dst.
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(dst)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr),
+                 "r"(ncols)
+                 : "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem], kind::tf32, cta_group::1.
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Arrive on `bar` once every MMA this thread issued so far has completed.
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+            smem_u32(bar))
+        : "memory");
+}
+
+// 16 consecutive 32-bit columns of this warp's 32 tensor-memory lanes
+// (thread = lane), then wait for the load.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+        "%11, %12, %13, %14, %15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        v[i] = __uint_as_float(r[i]);
+    }
+}
+
+// Shared-memory matrix descriptor: K-major operand in the canonical
+// 128-byte-swizzled layout (rows of 128 bytes, 8-row atoms 1024 bytes apart).
+// `addr` is the shared address of the first K element (tile base 1024-aligned,
+// plus 32 bytes per 8 TF32 K elements).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr)
+{
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(16u >> 4) << 16;    // leading byte offset (unused with this swizzle)
+    d |= (uint64_t)(1024u >> 4) << 32;  // stride byte offset: 8 rows x 128 bytes
+    d |= (uint64_t)1 << 46;             // descriptor version (fixed 0b001)
+    d |= (uint64_t)2 << 61;             // swizzle: 128 bytes
+    return d;
+}
+
+// Instruction descriptor: D f32, A and B tf32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t tf32_idesc(int M, int N)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+// FP32 value -> (hi, lo) TF32 pair: hi keeps the top 10 mantissa bits, lo the rest (exact).
+__device__ __forceinline__ void split_tf32(float v, float &hi, float &lo)
+{
+    hi = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
+    lo = __fsub_rn(v, hi);
+}
+
+// Byte offset of element (row r, k) in a 128-byte-swizzled K-major tile of
+// f32 with 32 K elements per row.
+__device__ __forceinline__ uint32_t sw128_off(int r, int k)
+{
+    return (uint32_t)(r * 128 + ((((k >> 2) ^ (r & 7)) & 7) << 4) + ((k & 3) << 2));
+}
+
+// ---------------------------------------------------------------------------
+// Split copies of basis column c.
+// ---------------------------------------------------------------------------
+__global__ void k_tc_store_column(const float *__restrict__ col, int n, int c,
+                                  float *__restrict__ hiC, float *__restrict__ loC, size_t ldn,
+                                  float *__restrict__ hiR, float *__restrict__ loR, size_t ldk)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        float h, l;
+        split_tf32(col[i], h, l);
+        hiC[(size_t)c * ldn + i] = h;
+        loC[(size_t)c * ldn + i] = l;
+        hiR[(size_t)i * ldk + c] = h;
+        loR[(size_t)i * ldk + c] = l;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_tc_tgemm: Tp[split][j][c] = sum over the split's rows i of src(i, j) Bo[i, c]
+// ---------------------------------------------------------------------------
+constexpr int TG_PROD = 8;                     // producer warps (then epilogue)
+constexpr int TG_THREADS = 32 * (TG_PROD + 2);  // + TMA warp + MMA warp
+constexpr int TG_M = 128;                      // candidates per tile
+constexpr int TG_K = 32;                       // rows per K step
+
+struct TgLayout {
+    int S, Np;
+    uint32_t a_bytes, b_bytes, stage, bars, total;
+    __host__ __device__ TgLayout(int m, int stages)
+    {
+        S = stages;
+        Np = ((m < 16 ? 16 : m) + 15) / 16 * 16;
+        a_bytes = TG_M * 128;             // one 128 x 32 f32 operand tile
+        b_bytes = (uint32_t)Np * 128;     // one Np x 32 f32 operand tile
+        stage = 2 * a_bytes + 2 * b_bytes;  // a_hi, a_lo, b_hi, b_lo
+        bars = (uint32_t)S * stage;
+        total = bars + (uint32_t)(3 * S + 1) * 8 + 16;
+    }
+};
+
+template <class Src>
+__global__ void __launch_bounds__(TG_THREADS, 1)
+    k_tc_tgemm(Src src, const __grid_constant__ CUtensorMap map_hi,
+               const __grid_constant__ CUtensorMap map_lo, int n, int m, int P, int rps,
+               int stages, float *__restrict__ Tp, int *__restrict__ err)
+{
+    extern __shared__ unsigned char smraw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+    const TgLayout L(m, stages);
+    const int S = L.S, Np = L.Np;
+    uint64_t *prod_full = reinterpret_cast<uint64_t *>(sm + L.bars);  // [S] producer warps
+    uint64_t *tma_full = prod_full + S;                               // [S] TMA bytes
+    uint64_t *empty = tma_full + S;                                   // [S] MMA commit
+    uint64_t *done = empty + S;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j0 = blockIdx.x * TG_M, split = blockIdx.y;
+    const int r0 = split * rps, r1 = min(n, r0 + rps);
+    const int ksteps = r1 > r0 ? (r1 - r0 + TG_K - 1) / TG_K : 0;
+    const uint32_t ncols = Np <= 32 ? 32 : Np <= 64 ? 64 : Np <= 128 ? 128 : 256;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(&prod_full[s], TG_PROD);
+            mbar_init(&tma_full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == TG_PROD + 1) {
+        tmem_alloc(tmem_slot, ncols);
+    }
+    if (warp == TG_PROD && lane == 0) {
+        tma_prefetch_desc(&map_hi);
+        tma_prefetch_desc(&map_lo);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp < TG_PROD) {
+        // Producers: warp w forms candidates [16 w, 16 w + 16) of the tile,
+        // lane = row within the K step.
+        for (int k = 0; k < ksteps; ++k) {
+            const int s = k % S, fill = k / S;
+            if (fill >= 1 && !mbar_wait_warp(&empty[s], (fill - 1) & 1, abort_flag, err)) {
+                break;
+            }
+            const int i = r0 + k * TG_K + lane;
+            float v[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int j = j0 + warp * 16 + q;
+                v[q] = (i < r1 && j < P) ? src((size_t)i, j) : 0.f;
+            }
+            unsigned char *ahi = sm + (size_t)s * L.stage;
+            unsigned char *alo = ahi + L.a_bytes;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int r = warp * 16 + q;
+                float h, l;
+                split_tf32(v[q], h, l);
+                const uint32_t off = sw128_off(r, lane);
+                *reinterpret_cast<float *>(ahi + off) = h;
+                *reinterpret_cast<float *>(alo + off) = l;
+            }
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&prod_full[s]);
+            }
+        }
+    } else if (warp == TG_PROD) {
+        // TMA: the Bo rows of each K step, hi and lo.
+        if (lane == 0) {
+            int issued = 0;
+            for (int k = 0; k < ksteps; ++k) {
+                const int s = k % S, fill = k / S;
+                if (fill >= 1 && !mbar_wait(&empty[s], (fill - 1) & 1, abort_flag, err)) {
+                    break;
+                }
+                unsigned char *bhi = sm + (size_t)s * L.stage + 2 * L.a_bytes;
+                unsigned char *blo = bhi + L.b_bytes;
+                mbar_expect_tx(&tma_full[s], 2 * L.b_bytes);
+                const int x = r0 + k * TG_K;
+                tma_load_2d(bhi, &map_hi, x, 0, &tma_full[s]);
+                tma_load_2d(blo, &map_lo, x, 0, &tma_full[s]);
+                issued = k + 1;
+            }
+            // let every copy issued land before the block can exit
+            for (int k = issued > S ? issued - S : 0; k < issued; ++k) {
+                mbar_wait(&tma_full[k % S], (k / S) & 1, abort_flag, err, true);
+            }
+        }
+    } else {
+        // MMA issuer.
+        if (lane == 0) {
+            const uint32_t idesc = tf32_idesc(TG_M, Np);
+            for (int k = 0; k < ksteps; ++k) {
+                const int s = k % S, ph = (k / S) & 1;
+                if (!mbar_wait(&prod_full[s], ph, abort_flag, err) ||
+                    !mbar_wait(&tma_full[s], ph, abort_flag, err)) {
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t base = smem_u32(sm + (size_t)s * L.stage);
+                const uint32_t ahi = base, alo = base + L.a_bytes;
+                const uint32_t bhi = base + 2 * L.a_bytes, blo = bhi + L.b_bytes;
+#pragma unroll
+                for (int kk = 0; kk < TG_K / 8; ++kk) {
+                    const uint32_t o = 32u * kk;
+                    mma_tf32(tmem, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc,
+                             (k > 0 || kk > 0) ? 1u : 0u);
+                    mma_tf32(tmem, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, 1u);
+                    mma_tf32(tmem, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
+                }
+                mma_commit(&empty[s]);
+            }
+            mma_commit(done);
+            if (*abort_flag) {
+                mbar_wait(done, 0, abort_flag, err, true);  // the MMAs in flight
+            }
+        }
+    }
+    __syncwarp();
+
+    // Epilogue: warps w and w + 4 read lanes 32 (w % 4) .. (candidates), the
+    // even / odd 16-column chunks (basis components).
+    if (warp < TG_PROD && ksteps > 0) {
+        if (mbar_wait_warp(done, 0, abort_flag, err)) {
+            tc_fence_after();
+            const int q = warp & 3, half = warp >> 2;
+            const int j = j0 + 32 * q + lane;
+            for (int ch = half; ch * 16 < Np; ch += 2) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(16 * ch), v);
+                if (j < P) {
+                    float *dst = Tp + ((size_t)split * P + j) * m;
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        if (16 * ch + c < m) {
+                            dst[16 * ch + c] = v[c];
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (warp < TG_PROD && ksteps == 0) {  // an empty split contributes zeros
+        const int q = warp & 3, half = warp >> 2;
+        const int j = j0 + 32 * q + lane;
+        if (j < P) {
+            for (int c = half; c < m; c += 2) {
+                Tp[((size_t)split * P + j) * m + c] = 0.f;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == TG_PROD + 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, ncols);
+    }
+}
+
+// T[j][c] = f32(sum over splits of Tp), in a fixed order, plus the split copies
+// Thi/Tlo [P][ldk] (zero past m).
+__global__ void k_tc_treduce(const float *__restrict__ Tp, int ks, int P, int m, size_t ldk,
+                             float *__restrict__ T, float *__restrict__ Thi,
+                             float *__restrict__ Tlo)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)P * ldk) {
+        return;
+    }
+    const int j = (int)(e / ldk), c = (int)(e % ldk);
+    float t = 0.f;
+    if (c < m) {
+        const size_t cnt = (size_t)P * m, idx = (size_t)j * m + c;
+        double a = 0.0;
+        for (int q = 0; q < ks; ++q) {
+            a += (double)Tp[(size_t)q * cnt + idx];
+        }
+        t = (float)a;
+        T[idx] = t;
+    }
+    float h, l;
+    split_tf32(t, h, l);
+    Thi[e] = h;
+    Tlo[e] = l;
+}
+
+// ---------------------------------------------------------------------------
+// k_tc_project: Bx[i, j] = src(i, j) - sum_c Bo[i, c] T[j][c], persistent
+// ---------------------------------------------------------------------------
+constexpr int TP_EPI = 4;                       // epilogue warps
+constexpr int TP_THREADS = 32 * (TP_EPI + 2);   // + TMA warp + MMA warp
+constexpr int TP_M = 128;                       // rows per tile
+constexpr int TP_N = 64;                        // candidates per tile
+constexpr int TP_S = 2;                         // K-step stages
+
+struct TpLayout {
+    uint32_t a_bytes, b_bytes, stage, bars, total;
+    __host__ __device__ TpLayout()
+    {
+        a_bytes = TP_M * 128;
+        b_bytes = TP_N * 128;
+        stage = 2 * a_bytes + 2 * b_bytes;
+        bars = TP_S * stage;
+        total = bars + (2 * TP_S + 5) * 8 + 16;
+    }
+};
+
+template <class Src>
+__global__ void __launch_bounds__(TP_THREADS, 2)
+    k_tc_project(Src src, const __grid_constant__ CUtensorMap a_hi,
+                 const __grid_constant__ CUtensorMap a_lo, const __grid_constant__ CUtensorMap b_hi,
+                 const __grid_constant__ CUtensorMap b_lo, int n, int m, int P,
+                 float *__restrict__ Bx, size_t ldBx, int *__restrict__ err)
+{
+    extern __shared__ unsigned char smraw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+    const TpLayout L;
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + L.bars);  // [TP_S] TMA bytes
+    uint64_t *empty = full + TP_S;                               // [TP_S] MMA commit
+    uint64_t *acc_full = empty + TP_S;                           // [2]
+    uint64_t *acc_empty = acc_full + 2;                          // [2] epilogue warps
+    uint64_t *drain = acc_empty + 2;                             // MMAs in flight at an abort
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rt = (n + TP_M - 1) / TP_M, ct = (P + TP_N - 1) / TP_N;
+    const long tiles = (long)rt * ct;
+    const int kt = (m + 31) / 32;
+    const uint32_t ncols = 2 * TP_N;  // two accumulator buffers
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TP_S; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], TP_EPI);
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == TP_EPI + 1) {
+        tmem_alloc(tmem_slot, ncols);
+    }
+    if (warp == TP_EPI && lane == 0) {
+        tma_prefetch_desc(&a_hi);
+        tma_prefetch_desc(&a_lo);
+        tma_prefetch_desc(&b_hi);
+        tma_prefetch_desc(&b_lo);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    // tile t: candidate tile t % ct (fastest), row tile t / ct
+    if (warp == TP_EPI) {
+        if (lane == 0) {
+            long g = 0, issued = 0;
+            bool ok = true;
+            for (long t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+                const int row0 = (int)(t / ct) * TP_M, cand0 = (int)(t % ct) * TP_N;
+                for (int k = 0; k < kt; ++k, ++g) {
+                    const int s = (int)(g % TP_S);
+                    const long fill = g / TP_S;
+                    if (fill >= 1 && !mbar_wait(&empty[s], (uint32_t)((fill - 1) & 1), abort_flag,
+                                                err)) {
+                        ok = false;
+                        break;
+                    }
+                    unsigned char *st = sm + (size_t)s * L.stage;
+                    mbar_expect_tx(&full[s], L.stage);
+                    tma_load_2d(st, &a_hi, 32 * k, row0, &full[s]);
+                    tma_load_2d(st + L.a_bytes, &a_lo, 32 * k, row0, &full[s]);
+                    tma_load_2d(st + 2 * L.a_bytes, &b_hi, 32 * k, cand0, &full[s]);
+                    tma_load_2d(st + 2 * L.a_bytes + L.b_bytes, &b_lo, 32 * k, cand0, &full[s]);
+                    issued = g + 1;
+                }
+            }
+            for (long q = issued > TP_S ? issued - TP_S : 0; q < issued; ++q) {
+                mbar_wait(&full[q % TP_S], (uint32_t)((q / TP_S) & 1), abort_flag, err, true);
+            }
+        }
+    } else if (warp == TP_EPI + 1) {
+        if (lane == 0) {
+            const uint32_t idesc = tf32_idesc(TP_M, TP_N);
+            long g = 0, u = 0;
+            bool ok = true;
+            for (long t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++u) {
+                const int b = (int)(u & 1);
+                if (u >= 2 && !mbar_wait(&acc_empty[b], (uint32_t)(((u >> 1) - 1) & 1),
+                                         abort_flag, err)) {
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)(b * TP_N);
+                for (int k = 0; k < kt; ++k, ++g) {
+                    const int s = (int)(g % TP_S);
+                    if (!mbar_wait(&full[s], (uint32_t)((g / TP_S) & 1), abort_flag, err)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t base = smem_u32(sm + (size_t)s * L.stage);
+                    const uint32_t ahi = base, alo = base + L.a_bytes;
+                    const uint32_t bhi = base + 2 * L.a_bytes, blo = bhi + L.b_bytes;
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const uint32_t o = 32u * kk;
+                        mma_tf32(d, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc,
+                                 (k > 0 || kk > 0) ? 1u : 0u);
+                        mma_tf32(d, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, 1u);
+                        mma_tf32(d, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
+                    }
+                    mma_commit(&empty[s]);
+                }
+                if (ok) {
+                    mma_commit(&acc_full[b]);
+                }
+            }
+            if (*abort_flag) {
+                mma_commit(drain);  // lands once every MMA issued so far has completed
+                mbar_wait(drain, 0, abort_flag, err, true);
+            }
+        }
+    } else {
+        // Epilogue: warp w owns rows 32 w .. 32 w + 31 of each tile.
+        long u = 0;
+        for (long t = blockIdx.x; t < tiles; t += gridDim.x, ++u) {
+            const int b = (int)(u & 1);
+            if (!mbar_wait_warp(&acc_full[b], (uint32_t)((u >> 1) & 1), abort_flag, err)) {
+                break;
+            }
+            tc_fence_after();
+            const int row0 = (int)(t / ct) * TP_M, cand0 = (int)(t % ct) * TP_N;
+            float acc[TP_N];
+#pragma unroll
+            for (int ch = 0; ch < TP_N / 16; ++ch) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * TP_N + 16 * ch),
+                          v);
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    acc[16 * ch + c] = v[c];
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&acc_empty[b]);
+            }
+            const int i = row0 + 32 * warp + lane;
+            if (i < n) {
+#pragma unroll
+                for (int c = 0; c < TP_N; ++c) {
+                    const int j = cand0 + c;
+                    if (j < P) {
+                        const float v = src((size_t)i, j);
+                        Bx[(size_t)j * ldBx + i] = __fsub_rn(v, acc[c]);
+                    }
+                }
+            }
+        }
+    }
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    if (warp == TP_EPI + 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, ncols);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                 const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                 const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_tiled()
+{
+    static std::once_flag once;
+    static EncodeTiled fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess) {
+            fn = reinterpret_cast<EncodeTiled>(p);
+        }
+    });
+    verify(fn != nullptr, "cuTensorMapEncodeTiled is not available from the driver", 2);
+    return fn;
+}
+
+// 2-D f32 tensor map: `inner` contiguous elements per line, `outer` lines,
+// `pitch` elements between lines; box 32 x box_outer, 128-byte swizzle.
+CUtensorMap tmap_2d(const float *base, size_t inner, size_t outer, size_t pitch,
+                    uint32_t box_outer)
+{
+    verify(reinterpret_cast<uintptr_t>(base) % 16 == 0 && pitch % 4 == 0,
+           "tensor map base or pitch not 16-byte aligned", 2);
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+    const cuuint32_t box[2] = {32u, box_outer};
+    const cuuint32_t es[2] = {1u, 1u};
+    const CUresult r = encode_tiled()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                                      const_cast<float *>(base), dims, strides, box, es,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        throw Error(2, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    }
+    return map;
+}
+
+int sm_count()
+{
+    int dev = 0, c = 0;
+    CUDA_CHECK(cudaGetDevice(&dev));
+    CUDA_CHECK(cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev));
+    return std::max(1, c);
+}
+
+int tg_stages(int m)
+{
+    const size_t budget = 220 * 1024;
+    for (int S = 4; S >= 2; --S) {
+        if (TgLayout(m, S).total + 1024 <= budget) {
+            return S;
+        }
+    }
+    return 2;
+}
+
+void check_err(cudaStream_t st, int *err)
+{
+    int h = 0;
+    CUDA_CHECK(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_CHECK(cudaStreamSynchronize(st));
+    verify(h == 0, "a bounded wait in the tensor-core projection ran out", MARS_GPU_ETIMEOUT);
+}
+
+template <class Src>
+void t_pass(cudaStream_t st, const Src &src, const TcBasis &tb, int n, int m, int P,
+            const TcScratch &ws, long long *launches)
+{
+    const int ks = tc_ksplit(n, P);
+    const int rps = (int)round_up(ceil_div((size_t)n, (size_t)ks), TG_K);
+    const int S = tg_stages(m);
+    const TgLayout L(m, S);
+    const CUtensorMap mh = tmap_2d(tb.hiC, tb.ldn, (size_t)m, tb.ldn, (uint32_t)L.Np);
+    const CUtensorMap ml = tmap_2d(tb.loC, tb.ldn, (size_t)m, tb.ldn, (uint32_t)L.Np);
+    const size_t smem = L.total + 1024;
+    allow_smem(k_tc_tgemm<Src>, smem);
+    const dim3 grid((unsigned)ceil_div((size_t)P, TG_M), (unsigned)ks);
+    k_tc_tgemm<Src><<<grid, TG_THREADS, smem, st>>>(src, mh, ml, n, m, P, rps, S, ws.Tp, ws.err);
+    LAUNCH_CHECK();
+    const size_t cnt = (size_t)P * tb.ldk;
+    k_tc_treduce<<<(unsigned)ceil_div(cnt, 256), 256, 0, st>>>(ws.Tp, ks, P, m, tb.ldk, ws.T,
+                                                              ws.Thi, ws.Tlo);
+    LAUNCH_CHECK();
+    *launches += 2;
+}
+
+template <class Src>
+void p_pass(cudaStream_t st, const Src &src, const TcBasis &tb, int n, int m, int P,
+            const TcScratch &ws, long long *launches)
+{
+    const CUtensorMap ah = tmap_2d(tb.hiR, tb.ldk, (size_t)n, tb.ldk, TP_M);
+    const CUtensorMap al = tmap_2d(tb.loR, tb.ldk, (size_t)n, tb.ldk, TP_M);
+    const CUtensorMap bh = tmap_2d(ws.Thi, tb.ldk, (size_t)P, tb.ldk, TP_N);
+    const CUtensorMap bl = tmap_2d(ws.Tlo, tb.ldk, (size_t)P, tb.ldk, TP_N);
+    const TpLayout L;
+    const size_t smem = L.total + 1024;
+    allow_smem(k_tc_project<Src>, smem);
+    const long tiles = (long)ceil_div((size_t)n, TP_M) * (long)ceil_div((size_t)P, TP_N);
+    const long grid = std::min<long>(tiles, 2L * sm_count());
+    k_tc_project<Src><<<(unsigned)grid, TP_THREADS, smem, st>>>(src, ah, al, bh, bl, n, m, P,
+                                                                ws.Bx, (size_t)n, ws.err);
+    LAUNCH_CHECK();
+    *launches += 1;
+}
+
+}  // namespace
+
+size_t tc_ldn(size_t n) { return round_up(std::max<size_t>(n, 1), 32); }
+size_t tc_ldk(size_t max_terms) { return round_up(std::max<size_t>(max_terms, 1), 32); }
+
+void tc_store_column(cudaStream_t st, const float *col, int n, int c, const TcBasis &tb,
+                     long long *launches)
+{
+    k_tc_store_column<<<(unsigned)ceil_div((size_t)n, 256), 256, 0, st>>>(
+        col, n, c, tb.hiC, tb.loC, tb.ldn, tb.hiR, tb.loR, tb.ldk);
+    LAUNCH_CHECK();
+    *launches += 1;
+}
+
+int tc_ksplit(int n, int P)
+{
+    const int tiles = (int)ceil_div((size_t)std::max(P, 1), TG_M);
+    const int want = std::max(1, (sm_count() + tiles - 1) / tiles);
+    return std::max(1, std::min(want, std::max(1, n / (8 * TG_K))));
+}
+
+void tc_project_pass(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int n, int m,
+                     int P, const TcScratch &ws, long long *launches)
+{
+    verify(m >= 1 && m <= TC_MAX_M, "the tensor-core projection takes 1..256 basis columns");
+    CUDA_CHECK(cudaMemsetAsync(ws.err, 0, sizeof(int), st));
+    t_pass(st, src, tb, n, m, P, ws, launches);
+    p_pass(st, src, tb, n, m, P, ws, launches);
+    check_err(st, ws.err);
+}
+
+void fast_project_tc(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int n, int m,
+                     int P, const float *y, double tol, const TcScratch &ws,
+                     long long *launches)
+{
+    if (P <= 0) {
+        return;
+    }
+    verify(m >= 1 && m <= TC_MAX_M, "the tensor-core projection takes 1..256 basis columns");
+    CUDA_CHECK(cudaMemsetAsync(ws.err, 0, sizeof(int), st));
+    t_pass(st, src, tb, n, m, P, ws, launches);
+    p_pass(st, src, tb, n, m, P, ws, launches);
+    const StoredSrc stored{ws.Bx, (size_t)n, nullptr};
+    t_pass(st, stored, tb, n, m, P, ws, launches);
+    p_pass(st, stored, tb, n, m, P, ws, launches);
+    fast_norms_moments(st, ws.Bx, n, y, tol, src, P, ws.s, ws.ybx, ws.mom, launches);
+    check_err(st, ws.err);
+}
+
+}  // namespace mgpu
