@@ -246,6 +246,28 @@ MARS_GPU_API int mars_gpu_orthonormalize_noalloc(size_t n, size_t m, size_t p, c
                                     double *s, double tol, void *stream, long *dgks);
 
 /*
+ *  mars_gpu_fast_project: the projection of the mixed-precision fast pass, on
+ *  host arrays. No counterpart in the reference (whose GPU projection,
+ *  mars::cuda::project_reduce at cuda/orthonormalize.cu:704-930, runs on
+ *  cuBLAS in blocked f32 or f64): candidate j is v_j = B[:, cand_b[j]] *
+ *  (X[:, cand_x[j]] * s[cand_x[j]]) (f32); it is projected onto the
+ *  complement of the m columns of Bo ((n, m) column-major, stride ldBo):
+ *  T = Bo^T v, Bx = v - Bo T. passes = 2 applies it twice (the second pass on
+ *  the first one's residual) and fills s_out = ||Bx||^2 and
+ *  ybx_out = (Bx . y) / sqrt(s + tol) (both optional); passes = 1 stops after
+ *  one. T (P x m, row j = candidate j) receives the last pass's coefficients,
+ *  Bx (n x P column-major, ld n) the projected columns. use_tc = 1: the
+ *  tensor-core kernels (tcgen05, split-TF32; m <= 128); use_tc = 0: the FP32
+ *  SIMT kernels (passes = 2 only).
+ */
+MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float *B, size_t ldB,
+                                       size_t ncolB, const float *X, size_t ldX, size_t ncolX,
+                                       const float *s, const int *cand_x, const int *cand_b,
+                                       const float *Bo, size_t ldBo, const float *y, double tol,
+                                       int use_tc, int passes, float *T, float *Bx,
+                                       double *s_out, double *ybx_out);
+
+/*
  *  Bytes currently handed out by the library's stream-ordered memory pool on
  *  the calling thread's current device (cudaMemPoolAttrUsedMemCurrent): what
  *  live handles hold. A diagnostic for tests (a call that allocates nothing

@@ -8,6 +8,7 @@
 #include "fast.cuh"
 #include "fp64.cuh"
 #include "host_exact.h"
+#include "tc.cuh"
 
 #include <algorithm>
 #include <cfloat>
@@ -216,6 +217,11 @@ struct mars_gpu_algo {
     DevBuf Bx, T, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks, stasks, scal, part;
     DevBuf bsort, bxsort;  // per candidate: parent and normalised column in sorted order
     DevBuf fTp, fT, fmom, hflag;  // fast pass: split-K partials, T, parent moments, sweep flags
+    // Fast pass on the tensor cores: split (hi, lo) copies of the basis, the
+    // split coefficients and the kernels' error word; tc_cols basis columns
+    // copied so far.
+    DevBuf tcHiC, tcLoC, tcHiR, tcLoR, tcThi, tcTlo, tcErr;
+    size_t tc_cols = 0;
     DevBuf sort_keys, sort_vals, sort_tmp;
     // Mixed mode: the exact re-decision speculated for the previous eval's
     // contenders and for the columns appended since, beside the fast pass.
@@ -302,7 +308,9 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
                       &a->xsort, &a->ysort, &a->Bx, &a->T, &a->svec, &a->snew, &a->ybx,
                       &a->hsse, &a->hrow, &a->cand, &a->fired, &a->nfired, &a->out, &a->tasks,
                       &a->stasks, &a->scal, &a->part, &a->bsort, &a->bxsort, &a->fTp, &a->fT,
-                      &a->fmom, &a->hflag, &a->sort_keys, &a->sort_vals, &a->sort_tmp}) {
+                      &a->fmom, &a->hflag, &a->sort_keys, &a->sort_vals, &a->sort_tmp,
+                      &a->tcHiC, &a->tcLoC, &a->tcHiR, &a->tcLoR, &a->tcThi, &a->tcTlo,
+                      &a->tcErr}) {
         b->bind(a->st);
     }
     CUDA_CHECK(cudaEventCreate(&a->span_begin));
@@ -624,6 +632,43 @@ struct SpecJoin {
     }
 };
 
+// Whether the fast projection runs on the tensor cores (MARS_GPU_TC, default
+// 1; 0 selects the FP32 SIMT kernels).
+bool use_tc(size_t m)
+{
+    return m <= (size_t)TC_MAX_M && env_double("MARS_GPU_TC", 1.0) != 0.0;
+}
+
+// The split basis copies of the tensor-core projection, allocated on first
+// use (zero-filled: rows past n and columns past m are read as zeros) and
+// brought up to the live basis.
+TcBasis tc_basis(mars_gpu_algo *a)
+{
+    TcBasis tb;
+    tb.ldn = tc_ldn(a->n);
+    tb.ldk = tc_ldk(a->max_terms);
+    if (!a->tcHiC.ptr) {
+        a->tcHiC.ensure(sizeof(float) * tb.ldn * a->max_terms);
+        a->tcLoC.ensure(sizeof(float) * tb.ldn * a->max_terms);
+        a->tcHiR.ensure(sizeof(float) * a->n * tb.ldk);
+        a->tcLoR.ensure(sizeof(float) * a->n * tb.ldk);
+        a->tcErr.ensure(sizeof(int));
+        for (DevBuf *b : {&a->tcHiC, &a->tcLoC, &a->tcHiR, &a->tcLoR, &a->tcErr}) {
+            CUDA_CHECK(cudaMemsetAsync(b->ptr, 0, b->bytes, a->st));
+        }
+        a->tc_cols = 0;
+    }
+    tb.hiC = a->tcHiC.as<float>();
+    tb.loC = a->tcLoC.as<float>();
+    tb.hiR = a->tcHiR.as<float>();
+    tb.loR = a->tcLoR.as<float>();
+    for (; a->tc_cols < a->m; ++a->tc_cols) {
+        tc_store_column(a->st, a->BoC.as<float>() + a->tc_cols * a->n, (int)a->n,
+                        (int)a->tc_cols, tb, &a->stats.kernel_launches);
+    }
+    return tb;
+}
+
 // Mixed precision (MARS_GPU_PREC_MIXED). Every candidate is ranked by the
 // FP32 / FP64-carry fast pass on the GPU; the best-ranked ones -- the top
 // MARS_GPU_MIXED_TOPK (default 4) by linear and by hinge delta SSE, and any
@@ -665,7 +710,21 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
     a->ybx.ensure(sizeof(double) * maxPc);
     a->hsse.ensure(sizeof(double) * 2 * maxPc);  // two sweep directions
     a->hrow.ensure(sizeof(int) * 2 * maxPc);
-    a->fTp.ensure(sizeof(float) * (size_t)ks * maxPc * m);
+    const bool tc = use_tc(a->m);
+    TcBasis tb;
+    if (tc) {
+        tb = tc_basis(a);
+        a->tcThi.ensure(sizeof(float) * maxPc * tb.ldk);
+        a->tcTlo.ensure(sizeof(float) * maxPc * tb.ldk);
+        size_t tp = 0;  // split-K partials of the largest block (the split count varies)
+        for (auto &b : blocks) {
+            const int Pc = b.second - b.first;
+            tp = std::max(tp, (size_t)tc_ksplit(n, Pc) * (size_t)Pc);
+        }
+        a->fTp.ensure(sizeof(float) * tp * m);
+    } else {
+        a->fTp.ensure(sizeof(float) * (size_t)ks * maxPc * m);
+    }
     a->fT.ensure(sizeof(float) * maxPc * m);
     a->fmom.ensure(sizeof(double) * 3 * maxPc);
     a->hflag.ensure(sizeof(int) * 2 * maxPc);
@@ -734,10 +793,18 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         a->stats.project_flops += 4.0 * (double)n * (double)m * (double)Pc;
         cudaEvent_t t0 = a->timer.begin();
         FillSrc src{a->B.as<float>(), a->n, a->X.as<float>(), a->n, a->s.as<float>(), cx_d, cb_d};
-        FastScratch ws{a->fTp.as<float>(), a->fT.as<float>(), a->Bx.as<float>(),
-                       a->svec.as<double>(), a->ybx.as<double>(), a->fmom.as<double>()};
-        fast_project(a->st, src, a->BoC.as<float>(), n, m, Pc, a->y.as<float>(), a->tol, ws,
-                     &a->stats.kernel_launches);
+        if (tc) {
+            const TcScratch ws{a->fTp.as<float>(), a->fT.as<float>(), a->tcThi.as<float>(),
+                               a->tcTlo.as<float>(), a->Bx.as<float>(), a->svec.as<double>(),
+                               a->ybx.as<double>(), a->fmom.as<double>(), a->tcErr.as<int>()};
+            fast_project_tc(a->st, src, tb, n, m, Pc, a->y.as<float>(), a->tol, ws,
+                            &a->stats.kernel_launches);
+        } else {
+            FastScratch ws{a->fTp.as<float>(), a->fT.as<float>(), a->Bx.as<float>(),
+                           a->svec.as<double>(), a->ybx.as<double>(), a->fmom.as<double>()};
+            fast_project(a->st, src, a->BoC.as<float>(), n, m, Pc, a->y.as<float>(), a->tol, ws,
+                         &a->stats.kernel_launches);
+        }
         a->timer.end(PH_PROJECT, t0);
         if (!linear_only) {
             t0 = a->timer.begin();

@@ -9,12 +9,16 @@
 //                 a time. Bo (hi, lo) arrives by TMA from the column-major
 //                 split copies; the candidate operand (hi, lo) is formed by
 //                 eight producer warps from its source columns and written in
-//                 the same 128-byte-swizzled K-major layout. Partials per
-//                 split are summed in FP64 in a fixed order (k_tc_treduce).
+//                 the same 128-byte-swizzled K-major layout. Each 128-row
+//                 chunk is summed in tensor memory and folded into FP32
+//                 registers by drain warps; partials per split are summed in
+//                 FP64 in a fixed order (k_tc_treduce).
 //   k_tc_project  Bx (n x P) = src - Bo T: persistent, tile = 128 rows x 64
 //                 candidates, K = m padded to 32; Bo rows (hi, lo) and T
-//                 (hi, lo) both by TMA, two accumulator buffers in tensor
-//                 memory so the epilogue of one tile overlaps the MMAs of the
+//                 (hi, lo) both by TMA, two pairs of accumulators in tensor
+//                 memory (hi*hi and the small hi*lo + lo*hi apart, so the
+//                 truncating FP32 adds of the tensor cores see few large
+//                 terms) so the epilogue of one tile overlaps the MMAs of the
 //                 next; the epilogue subtracts from the source column and
 //                 stores Bx column-major (coalesced across a warp's rows).
 //
@@ -186,25 +190,6 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar)
         : "memory");
 }
 
-// 16 consecutive 32-bit columns of this warp's 32 tensor-memory lanes
-// (thread = lane), then wait for the load.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
-{
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-        "%11, %12, %13, %14, %15}, [%16];\n"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        v[i] = __uint_as_float(r[i]);
-    }
-}
-
 // Shared-memory matrix descriptor: K-major operand in the canonical
 // 128-byte-swizzled layout (rows of 128 bytes, 8-row atoms 1024 bytes apart).
 // `addr` is the shared address of the first K element (tile base 1024-aligned,
@@ -260,11 +245,21 @@ __global__ void k_tc_store_column(const float *__restrict__ col, int n, int c,
 
 // ---------------------------------------------------------------------------
 // k_tc_tgemm: Tp[split][j][c] = sum over the split's rows i of src(i, j) Bo[i, c]
+//
+// The tensor cores add into their FP32 accumulator with truncation, so a long
+// accumulation drifts low by about half an ulp per MMA. The sum therefore runs
+// in tensor memory over one chunk of TG_CHUNK K steps (128 rows) at a time, in
+// two accumulators -- hi*hi, and the small hi*lo + lo*hi -- and drain warps
+// add each chunk's sums into FP32 registers (round to nearest) while the MMAs
+// of the next chunk fill the other pair of accumulators.
 // ---------------------------------------------------------------------------
-constexpr int TG_PROD = 8;                     // producer warps (then epilogue)
-constexpr int TG_THREADS = 32 * (TG_PROD + 2);  // + TMA warp + MMA warp
-constexpr int TG_M = 128;                      // candidates per tile
-constexpr int TG_K = 32;                       // rows per K step
+constexpr int TG_PROD = 8;                                // producer warps
+constexpr int TG_DRAIN = 8;                               // drain warps
+constexpr int TG_THREADS = 32 * (TG_PROD + 2 + TG_DRAIN);  // + TMA warp + MMA warp
+constexpr int TG_M = 128;                                 // candidates per tile
+constexpr int TG_K = 32;                                  // rows per K step
+constexpr int TG_CHUNK = 4;                               // K steps per accumulation
+constexpr int TG_WTMA = TG_PROD, TG_WMMA = TG_PROD + 1, TG_WDRAIN = TG_PROD + 2;
 
 struct TgLayout {
     int S, Np;
@@ -277,9 +272,28 @@ struct TgLayout {
         b_bytes = (uint32_t)Np * 128;     // one Np x 32 f32 operand tile
         stage = 2 * a_bytes + 2 * b_bytes;  // a_hi, a_lo, b_hi, b_lo
         bars = (uint32_t)S * stage;
-        total = bars + (uint32_t)(3 * S + 1) * 8 + 16;
+        total = bars + (uint32_t)(3 * S + 5) * 8 + 16;
     }
 };
+
+// Two loads of 8 consecutive columns of this warp's lanes, one wait.
+__device__ __forceinline__ void tmem_ld8x2(uint32_t ta, uint32_t tb, float (&a)[8], float (&b)[8])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%16];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%17];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(ta), "r"(tb));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        a[i] = __uint_as_float(r[i]);
+        b[i] = __uint_as_float(r[8 + i]);
+    }
+}
 
 template <class Src>
 __global__ void __launch_bounds__(TG_THREADS, 1)
@@ -295,15 +309,19 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
     uint64_t *prod_full = reinterpret_cast<uint64_t *>(sm + L.bars);  // [S] producer warps
     uint64_t *tma_full = prod_full + S;                               // [S] TMA bytes
     uint64_t *empty = tma_full + S;                                   // [S] MMA commit
-    uint64_t *done = empty + S;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    uint64_t *acc_full = empty + S;                                   // [2] MMA commit
+    uint64_t *acc_empty = acc_full + 2;                               // [2] drain warps
+    uint64_t *drain_bar = acc_empty + 2;                              // MMAs in flight at an abort
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain_bar + 1);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int j0 = blockIdx.x * TG_M, split = blockIdx.y;
     const int r0 = split * rps, r1 = min(n, r0 + rps);
     const int ksteps = r1 > r0 ? (r1 - r0 + TG_K - 1) / TG_K : 0;
-    const uint32_t ncols = Np <= 32 ? 32 : Np <= 64 ? 64 : Np <= 128 ? 128 : 256;
+    const int nchunks = (ksteps + TG_CHUNK - 1) / TG_CHUNK;
+    // two buffers x (hi*hi, correction) x Np columns
+    const uint32_t ncols = 4 * Np <= 64 ? 64 : 4 * Np <= 128 ? 128 : 4 * Np <= 256 ? 256 : 512;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
@@ -311,14 +329,18 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
             mbar_init(&tma_full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(done, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], TG_DRAIN);
+        }
+        mbar_init(drain_bar, 1);
         *abort_flag = 0;
         fence_mbar_init();
     }
-    if (warp == TG_PROD + 1) {
+    if (warp == TG_WMMA) {
         tmem_alloc(tmem_slot, ncols);
     }
-    if (warp == TG_PROD && lane == 0) {
+    if (warp == TG_WTMA && lane == 0) {
         tma_prefetch_desc(&map_hi);
         tma_prefetch_desc(&map_lo);
     }
@@ -359,7 +381,7 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
                 mbar_arrive(&prod_full[s]);
             }
         }
-    } else if (warp == TG_PROD) {
+    } else if (warp == TG_WTMA) {
         // TMA: the Bo rows of each K step, hi and lo.
         if (lane == 0) {
             int issued = 0;
@@ -381,72 +403,101 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
                 mbar_wait(&tma_full[k % S], (k / S) & 1, abort_flag, err, true);
             }
         }
-    } else {
-        // MMA issuer.
+    } else if (warp == TG_WMMA) {
+        // MMA issuer: chunk q accumulates into buffer q & 1.
         if (lane == 0) {
             const uint32_t idesc = tf32_idesc(TG_M, Np);
-            for (int k = 0; k < ksteps; ++k) {
-                const int s = k % S, ph = (k / S) & 1;
-                if (!mbar_wait(&prod_full[s], ph, abort_flag, err) ||
-                    !mbar_wait(&tma_full[s], ph, abort_flag, err)) {
+            bool ok = true;
+            for (int q = 0; q < nchunks && ok; ++q) {
+                const int b = q & 1;
+                if (q >= 2 && !mbar_wait(&acc_empty[b], ((q >> 1) - 1) & 1, abort_flag, err)) {
                     break;
                 }
                 tc_fence_after();
-                const uint32_t base = smem_u32(sm + (size_t)s * L.stage);
-                const uint32_t ahi = base, alo = base + L.a_bytes;
-                const uint32_t bhi = base + 2 * L.a_bytes, blo = bhi + L.b_bytes;
+                const uint32_t dmain = tmem + (uint32_t)(b * 2 * Np), dcorr = dmain + Np;
+                const int k1 = min(ksteps, (q + 1) * TG_CHUNK);
+                for (int k = q * TG_CHUNK; k < k1; ++k) {
+                    const int s = k % S, ph = (k / S) & 1;
+                    if (!mbar_wait(&prod_full[s], ph, abort_flag, err) ||
+                        !mbar_wait(&tma_full[s], ph, abort_flag, err)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t base = smem_u32(sm + (size_t)s * L.stage);
+                    const uint32_t ahi = base, alo = base + L.a_bytes;
+                    const uint32_t bhi = base + 2 * L.a_bytes, blo = bhi + L.b_bytes;
 #pragma unroll
-                for (int kk = 0; kk < TG_K / 8; ++kk) {
-                    const uint32_t o = 32u * kk;
-                    mma_tf32(tmem, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc,
-                             (k > 0 || kk > 0) ? 1u : 0u);
-                    mma_tf32(tmem, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, 1u);
-                    mma_tf32(tmem, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
+                    for (int kk = 0; kk < TG_K / 8; ++kk) {
+                        const uint32_t o = 32u * kk;
+                        const uint32_t acc = (k > q * TG_CHUNK || kk > 0) ? 1u : 0u;
+                        mma_tf32(dmain, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc, acc);
+                        mma_tf32(dcorr, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, acc);
+                        mma_tf32(dcorr, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
+                    }
+                    mma_commit(&empty[s]);
                 }
-                mma_commit(&empty[s]);
+                if (ok) {
+                    mma_commit(&acc_full[b]);
+                }
             }
-            mma_commit(done);
             if (*abort_flag) {
-                mbar_wait(done, 0, abort_flag, err, true);  // the MMAs in flight
+                mma_commit(drain_bar);  // lands once every MMA issued so far has completed
+                mbar_wait(drain_bar, 0, abort_flag, err, true);
+            }
+        }
+    } else {
+        // Drain warps: lanes 32 (w % 4) .. (candidates), one half of the
+        // columns (basis components) each.
+        const int g = warp - TG_WDRAIN, lg = warp & 3, h = g >> 2;
+        const int nph = Np / 2;  // columns per drain warp, a multiple of 8, <= 64
+        float acc[64];
+#pragma unroll
+        for (int c = 0; c < 64; ++c) {
+            acc[c] = 0.f;
+        }
+        bool ok = true;
+        for (int q = 0; q < nchunks; ++q) {
+            const int b = q & 1;
+            if (!mbar_wait_warp(&acc_full[b], (q >> 1) & 1, abort_flag, err)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t tm = tmem + ((uint32_t)(32 * lg) << 16) +
+                                (uint32_t)(b * 2 * Np + h * nph);
+#pragma unroll
+            for (int c8 = 0; c8 < 8; ++c8) {
+                if (8 * c8 < nph) {
+                    float x[8], y[8];
+                    tmem_ld8x2(tm + 8 * c8, tm + Np + 8 * c8, x, y);
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) {
+                        acc[8 * c8 + t] = __fadd_rn(acc[8 * c8 + t], __fadd_rn(x[t], y[t]));
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&acc_empty[b]);
+            }
+        }
+        const int j = j0 + 32 * lg + lane;
+        if (ok && j < P) {
+            float *dst = Tp + ((size_t)split * P + j) * m + h * nph;
+#pragma unroll
+            for (int c = 0; c < 64; ++c) {
+                if (c < nph && h * nph + c < m) {
+                    dst[c] = acc[c];
+                }
             }
         }
     }
     __syncwarp();
-
-    // Epilogue: warps w and w + 4 read lanes 32 (w % 4) .. (candidates), the
-    // even / odd 16-column chunks (basis components).
-    if (warp < TG_PROD && ksteps > 0) {
-        if (mbar_wait_warp(done, 0, abort_flag, err)) {
-            tc_fence_after();
-            const int q = warp & 3, half = warp >> 2;
-            const int j = j0 + 32 * q + lane;
-            for (int ch = half; ch * 16 < Np; ch += 2) {
-                float v[16];
-                tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(16 * ch), v);
-                if (j < P) {
-                    float *dst = Tp + ((size_t)split * P + j) * m;
-#pragma unroll
-                    for (int c = 0; c < 16; ++c) {
-                        if (16 * ch + c < m) {
-                            dst[16 * ch + c] = v[c];
-                        }
-                    }
-                }
-            }
-        }
-    }
-    if (warp < TG_PROD && ksteps == 0) {  // an empty split contributes zeros
-        const int q = warp & 3, half = warp >> 2;
-        const int j = j0 + 32 * q + lane;
-        if (j < P) {
-            for (int c = half; c < m; c += 2) {
-                Tp[((size_t)split * P + j) * m + c] = 0.f;
-            }
-        }
-    }
     tc_fence_before();
     __syncthreads();
-    if (warp == TG_PROD + 1) {
+    if (warp == TG_WMMA) {
         tc_fence_after();
         tmem_dealloc(tmem, ncols);
     }
@@ -523,7 +574,7 @@ __global__ void __launch_bounds__(TP_THREADS, 2)
     const int rt = (n + TP_M - 1) / TP_M, ct = (P + TP_N - 1) / TP_N;
     const long tiles = (long)rt * ct;
     const int kt = (m + 31) / 32;
-    const uint32_t ncols = 2 * TP_N;  // two accumulator buffers
+    const uint32_t ncols = 4 * TP_N;  // two buffers x (hi*hi, correction)
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TP_S; ++s) {
@@ -592,7 +643,7 @@ __global__ void __launch_bounds__(TP_THREADS, 2)
                     break;
                 }
                 tc_fence_after();
-                const uint32_t d = tmem + (uint32_t)(b * TP_N);
+                const uint32_t dmain = tmem + (uint32_t)(b * 2 * TP_N), dcorr = dmain + TP_N;
                 for (int k = 0; k < kt; ++k, ++g) {
                     const int s = (int)(g % TP_S);
                     if (!mbar_wait(&full[s], (uint32_t)((g / TP_S) & 1), abort_flag, err)) {
@@ -606,10 +657,10 @@ __global__ void __launch_bounds__(TP_THREADS, 2)
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk) {
                         const uint32_t o = 32u * kk;
-                        mma_tf32(d, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc,
-                                 (k > 0 || kk > 0) ? 1u : 0u);
-                        mma_tf32(d, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, 1u);
-                        mma_tf32(d, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
+                        const uint32_t acc = (k > 0 || kk > 0) ? 1u : 0u;
+                        mma_tf32(dmain, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc, acc);
+                        mma_tf32(dcorr, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, acc);
+                        mma_tf32(dcorr, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
                     }
                     mma_commit(&empty[s]);
                 }
@@ -634,13 +685,14 @@ __global__ void __launch_bounds__(TP_THREADS, 2)
             const int row0 = (int)(t / ct) * TP_M, cand0 = (int)(t % ct) * TP_N;
             float acc[TP_N];
 #pragma unroll
-            for (int ch = 0; ch < TP_N / 16; ++ch) {
-                float v[16];
-                tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * TP_N + 16 * ch),
-                          v);
+            for (int ch = 0; ch < TP_N / 8; ++ch) {
+                float x[8], y[8];
+                const uint32_t tm = tmem + ((uint32_t)(32 * warp) << 16) +
+                                    (uint32_t)(b * 2 * TP_N + 8 * ch);
+                tmem_ld8x2(tm, tm + TP_N, x, y);
 #pragma unroll
-                for (int c = 0; c < 16; ++c) {
-                    acc[16 * ch + c] = v[c];
+                for (int c = 0; c < 8; ++c) {
+                    acc[8 * ch + c] = __fadd_rn(x[c], y[c]);
                 }
             }
             tc_fence_before();
@@ -810,7 +862,7 @@ int tc_ksplit(int n, int P)
 void tc_project_pass(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int n, int m,
                      int P, const TcScratch &ws, long long *launches)
 {
-    verify(m >= 1 && m <= TC_MAX_M, "the tensor-core projection takes 1..256 basis columns");
+    verify(m >= 1 && m <= TC_MAX_M, "the tensor-core projection takes 1..128 basis columns");
     CUDA_CHECK(cudaMemsetAsync(ws.err, 0, sizeof(int), st));
     t_pass(st, src, tb, n, m, P, ws, launches);
     p_pass(st, src, tb, n, m, P, ws, launches);
@@ -824,7 +876,7 @@ void fast_project_tc(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int
     if (P <= 0) {
         return;
     }
-    verify(m >= 1 && m <= TC_MAX_M, "the tensor-core projection takes 1..256 basis columns");
+    verify(m >= 1 && m <= TC_MAX_M, "the tensor-core projection takes 1..128 basis columns");
     CUDA_CHECK(cudaMemsetAsync(ws.err, 0, sizeof(int), st));
     t_pass(st, src, tb, n, m, P, ws, launches);
     p_pass(st, src, tb, n, m, P, ws, launches);
@@ -836,3 +888,132 @@ void fast_project_tc(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int
 }
 
 }  // namespace mgpu
+
+// ===========================================================================
+// Kernel-level entry point (host arrays), for tests and micro-benchmarks.
+// ===========================================================================
+extern "C" {
+
+MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float *B, size_t ldB,
+                                       size_t ncolB, const float *X, size_t ldX, size_t ncolX,
+                                       const float *s, const int *cand_x, const int *cand_b,
+                                       const float *Bo, size_t ldBo, const float *y, double tol,
+                                       int use_tc, int passes, float *T, float *Bx,
+                                       double *s_out, double *ybx_out)
+{
+    using namespace mgpu;
+    try {
+        verify(B && X && s && cand_x && cand_b && Bo && y && T && Bx, "null argument");
+        verify(n >= 1 && m >= 1 && P >= 1 && n <= 0x7fffffff && P <= 0x7fffffff,
+               "empty or oversized problem");
+        verify(ldB >= n && ldX >= n && ldBo >= n, "leading dimension smaller than the data");
+        verify(passes == 1 || passes == 2, "passes must be 1 or 2");
+        verify(use_tc || passes == 2, "the FP32 SIMT projection runs both passes");
+        for (size_t j = 0; j < P; ++j) {
+            verify(cand_x[j] >= 0 && (size_t)cand_x[j] < ncolX &&
+                       cand_b[j] >= 0 && (size_t)cand_b[j] < ncolB,
+                   "candidate index outside the columns of X or B");
+        }
+        if (use_tc) {
+            verify(m <= (size_t)TC_MAX_M, "the tensor-core projection takes 1..128 basis columns");
+        }
+        cudaStream_t st = nullptr;
+        CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        struct StreamGuard {
+            cudaStream_t s;
+            ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
+        } guard{st};
+        DevBuf dB, dX, ds, dcx, dcb, dBoC, dy, dTp, dT, dThi, dTlo, dBx, dS, dYbx, dMom, dErr,
+            hiC, loC, hiR, loR;
+        for (DevBuf *b : {&dB, &dX, &ds, &dcx, &dcb, &dBoC, &dy, &dTp, &dT, &dThi, &dTlo, &dBx,
+                          &dS, &dYbx, &dMom, &dErr, &hiC, &loC, &hiR, &loR}) {
+            b->bind(st);
+        }
+        dB.ensure(sizeof(float) * n * ncolB);
+        CUDA_CHECK(cudaMemcpy2DAsync(dB.ptr, n * 4, B, ldB * 4, n * 4, ncolB,
+                                     cudaMemcpyHostToDevice, st));
+        dX.ensure(sizeof(float) * n * ncolX);
+        CUDA_CHECK(cudaMemcpy2DAsync(dX.ptr, n * 4, X, ldX * 4, n * 4, ncolX,
+                                     cudaMemcpyHostToDevice, st));
+        ds.ensure(sizeof(float) * ncolX);
+        CUDA_CHECK(cudaMemcpyAsync(ds.ptr, s, sizeof(float) * ncolX, cudaMemcpyHostToDevice, st));
+        dcx.ensure(sizeof(int) * P);
+        dcb.ensure(sizeof(int) * P);
+        CUDA_CHECK(cudaMemcpyAsync(dcx.ptr, cand_x, sizeof(int) * P, cudaMemcpyHostToDevice, st));
+        CUDA_CHECK(cudaMemcpyAsync(dcb.ptr, cand_b, sizeof(int) * P, cudaMemcpyHostToDevice, st));
+        dBoC.ensure(sizeof(float) * n * m);
+        CUDA_CHECK(cudaMemcpy2DAsync(dBoC.ptr, n * 4, Bo, ldBo * 4, n * 4, m,
+                                     cudaMemcpyHostToDevice, st));
+        dy.ensure(sizeof(float) * n);
+        CUDA_CHECK(cudaMemcpyAsync(dy.ptr, y, sizeof(float) * n, cudaMemcpyHostToDevice, st));
+        dBx.ensure(sizeof(float) * n * P);
+        dS.ensure(sizeof(double) * P);
+        dYbx.ensure(sizeof(double) * P);
+        dMom.ensure(sizeof(double) * 3 * P);
+        dT.ensure(sizeof(float) * P * m);
+        long long launches = 0;
+        const FillSrc src{dB.as<float>(), n, dX.as<float>(), n, ds.as<float>(), dcx.as<int>(),
+                          dcb.as<int>()};
+        if (use_tc) {
+            TcBasis tb;
+            tb.ldn = tc_ldn(n);
+            tb.ldk = tc_ldk(m);
+            hiC.ensure(sizeof(float) * tb.ldn * m);
+            loC.ensure(sizeof(float) * tb.ldn * m);
+            hiR.ensure(sizeof(float) * n * tb.ldk);
+            loR.ensure(sizeof(float) * n * tb.ldk);
+            for (DevBuf *b : {&hiC, &loC, &hiR, &loR}) {
+                CUDA_CHECK(cudaMemsetAsync(b->ptr, 0, b->bytes, st));
+            }
+            tb.hiC = hiC.as<float>();
+            tb.loC = loC.as<float>();
+            tb.hiR = hiR.as<float>();
+            tb.loR = loR.as<float>();
+            for (size_t c = 0; c < m; ++c) {
+                tc_store_column(st, dBoC.as<float>() + c * n, (int)n, (int)c, tb, &launches);
+            }
+            const int ks = tc_ksplit((int)n, (int)P);
+            dTp.ensure(sizeof(float) * (size_t)ks * P * m);
+            dThi.ensure(sizeof(float) * P * tb.ldk);
+            dTlo.ensure(sizeof(float) * P * tb.ldk);
+            dErr.ensure(sizeof(int));
+            TcScratch ws{dTp.as<float>(), dT.as<float>(), dThi.as<float>(), dTlo.as<float>(),
+                         dBx.as<float>(), dS.as<double>(), dYbx.as<double>(), dMom.as<double>(),
+                         dErr.as<int>()};
+            if (passes == 1) {
+                tc_project_pass(st, src, tb, (int)n, (int)m, (int)P, ws, &launches);
+            } else {
+                fast_project_tc(st, src, tb, (int)n, (int)m, (int)P, dy.as<float>(), tol, ws,
+                                &launches);
+            }
+        } else {
+            const int ks = fast_ksplit((int)n);
+            dTp.ensure(sizeof(float) * (size_t)ks * P * m);
+            FastScratch ws{dTp.as<float>(), dT.as<float>(), dBx.as<float>(), dS.as<double>(),
+                           dYbx.as<double>(), dMom.as<double>()};
+            fast_project(st, src, dBoC.as<float>(), (int)n, (int)m, (int)P, dy.as<float>(), tol,
+                         ws, &launches);
+        }
+        CUDA_CHECK(cudaMemcpyAsync(T, dT.ptr, sizeof(float) * P * m, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaMemcpyAsync(Bx, dBx.ptr, sizeof(float) * n * P, cudaMemcpyDeviceToHost,
+                                   st));
+        if (s_out && passes == 2) {
+            CUDA_CHECK(cudaMemcpyAsync(s_out, dS.ptr, sizeof(double) * P, cudaMemcpyDeviceToHost,
+                                       st));
+        }
+        if (ybx_out && passes == 2) {
+            CUDA_CHECK(cudaMemcpyAsync(ybx_out, dYbx.ptr, sizeof(double) * P,
+                                       cudaMemcpyDeviceToHost, st));
+        }
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        return MARS_GPU_OK;
+    } catch (const Error &e) {
+        set_last_error(e.what());
+        return e.status;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return MARS_GPU_ECUDA;
+    }
+}
+
+}  // extern "C"

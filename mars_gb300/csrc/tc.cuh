@@ -41,9 +41,10 @@ struct TcScratch {
     int *err;    // one int: nonzero when a bounded wait inside a kernel gave up
 };
 
-// Largest basis the tensor-core path takes (the accumulator of one tile is
-// 128 x round_up(m, 16) FP32 in tensor memory, N <= 256).
-constexpr int TC_MAX_M = 256;
+// Largest basis the tensor-core path takes: the T contraction keeps two
+// buffers of two 128 x round_up(m, 16) FP32 accumulators in the 512 columns
+// of tensor memory.
+constexpr int TC_MAX_M = 128;
 
 // Leading dimensions of the split basis copies for n rows and max_terms columns.
 size_t tc_ldn(size_t n);
