@@ -72,6 +72,8 @@ WORKLOADS = {
                "+ N(0,1) noise, max_terms=21, tail_span=0 (config 4)",
     "expand": "differentiable prediction of a fitted hinge_search model (31 terms) on "
               "1,000,000 rows: forward + backward (config 5)",
+    "projection": "the mixed fast pass's two-pass projection alone on a slice of config 3: "
+                  "n=1,000,000 rows, m=32 basis columns, 640 candidates (20 inputs x 32 parents)",
 }
 
 
@@ -439,6 +441,50 @@ def run_batched(args):
         line["cpu_baseline"] = {"value": len(sample) / dt, "unit": "fits/s",
                                 "cores": cpu_threads(), "kind": "port",
                                 "sample": "the first 4 of the 256 fits, one after another"}
+    print(json.dumps(line))
+    return 0
+
+
+def run_projection(args):
+    """The fast projection alone (mars_gpu_fast_project), tensor cores against
+    the FP32 SIMT kernels, device time of the kernels only. Algorithmic work:
+    two passes of T = Bo^T v (2 n m P FLOP) and Bx = v - Bo T (2 n m P FLOP)."""
+    from mars_gb300 import marslib
+
+    marslib.load()
+    rng = np.random.default_rng(0)
+    n, m, p, per = 1_000_000, 32, 20, 32
+    Q, _ = np.linalg.qr(rng.standard_normal((n, m)).astype(np.float32))
+    Bo = np.asfortranarray(Q.astype(np.float32))
+    B = np.asfortranarray(np.abs(rng.standard_normal((n, m))).astype(np.float32))
+    X = np.asfortranarray(rng.standard_normal((n, p)).astype(np.float32))
+    s = np.ones(p, dtype=np.float32)
+    cx = np.repeat(np.arange(p), per).astype(np.int32)
+    cb = np.tile(np.arange(per), p).astype(np.int32)
+    y = rng.standard_normal(n).astype(np.float32)
+    P = len(cx)
+    flops = 8.0 * n * m * P
+    out = {}
+    for name, tc in (("tc", True), ("simt", False)):
+        times = []
+        for _ in range(max(args.warmup, 1)):
+            marslib.fast_project(B, X, s, cx, cb, Bo, m, y, 1e-14, use_tc=tc)
+        for _ in range(args.steps):
+            marslib.fast_project(B, X, s, cx, cb, Bo, m, y, 1e-14, use_tc=tc, timing=times)
+        out[name] = statistics.median(times)
+    _, bf16, src = peaks()
+    ach = flops / (out["tc"] * 1e-3) / 1e12
+    line = {"metric": "fast projection device time (two passes + norms)", "value": out["tc"],
+            "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": out["tc"], "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "split-TF32 (tensor cores), FP32 accumulate",
+            "data": "synthetic", "config": {"workload": WORKLOADS["projection"]},
+            "simt_fp32_ms": out["simt"], "speedup_vs_simt": out["simt"] / out["tc"],
+            "roofline": {"kernel": "k_tc_tgemm + k_tc_project", "bound": "tensor",
+                         "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+                         "frac": ach / bf16, "peak_source": src,
+                         "note": "algorithmic FLOPs (8 n m P) over the device time of the whole "
+                                 "projection; split TF32 issues 3 MMAs per product"}}
     print(json.dumps(line))
     return 0
 
@@ -821,6 +867,8 @@ def main():
         return run_batched(args)
     if args.workload == "expand":
         return run_expand(args)
+    if args.workload == "projection":
+        return run_projection(args)
     tdist = dist()
     from mars_gb300 import marslib
 

@@ -258,14 +258,16 @@ MARS_GPU_API int mars_gpu_orthonormalize_noalloc(size_t n, size_t m, size_t p, c
  *  one. T (P x m, row j = candidate j) receives the last pass's coefficients,
  *  Bx (n x P column-major, ld n) the projected columns. use_tc = 1: the
  *  tensor-core kernels (tcgen05, split-TF32; m <= 128); use_tc = 0: the FP32
- *  SIMT kernels (passes = 2 only).
+ *  SIMT kernels (passes = 2 only). ms_out (optional) receives the device time
+ *  of the projection kernels (CUDA events on the call's stream), copies
+ *  excluded.
  */
 MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float *B, size_t ldB,
                                        size_t ncolB, const float *X, size_t ldX, size_t ncolX,
                                        const float *s, const int *cand_x, const int *cand_b,
                                        const float *Bo, size_t ldBo, const float *y, double tol,
                                        int use_tc, int passes, float *T, float *Bx,
-                                       double *s_out, double *ybx_out);
+                                       double *s_out, double *ybx_out, float *ms_out);
 
 /*
  *  Bytes currently handed out by the library's stream-ordered memory pool on

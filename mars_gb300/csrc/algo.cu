@@ -220,7 +220,7 @@ struct mars_gpu_algo {
     // Fast pass on the tensor cores: split (hi, lo) copies of the basis, the
     // split coefficients and the kernels' error word; tc_cols basis columns
     // copied so far.
-    DevBuf tcHiC, tcLoC, tcHiR, tcLoR, tcThi, tcTlo, tcErr;
+    DevBuf tcHiC, tcLoC, tcHiR, tcLoR, tcThi, tcTlo, tcErr, tcTab;
     size_t tc_cols = 0;
     DevBuf sort_keys, sort_vals, sort_tmp;
     // Mixed mode: the exact re-decision speculated for the previous eval's
@@ -310,7 +310,7 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
                       &a->stasks, &a->scal, &a->part, &a->bsort, &a->bxsort, &a->fTp, &a->fT,
                       &a->fmom, &a->hflag, &a->sort_keys, &a->sort_vals, &a->sort_tmp,
                       &a->tcHiC, &a->tcLoC, &a->tcHiR, &a->tcLoR, &a->tcThi, &a->tcTlo,
-                      &a->tcErr}) {
+                      &a->tcErr, &a->tcTab}) {
         b->bind(a->st);
     }
     CUDA_CHECK(cudaEventCreate(&a->span_begin));
@@ -716,6 +716,7 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         tb = tc_basis(a);
         a->tcThi.ensure(sizeof(float) * maxPc * tb.ldk);
         a->tcTlo.ensure(sizeof(float) * maxPc * tb.ldk);
+        a->tcTab.ensure(tc_tab_bytes(maxPc));
         size_t tp = 0;  // split-K partials of the largest block (the split count varies)
         for (auto &b : blocks) {
             const int Pc = b.second - b.first;
@@ -796,7 +797,8 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         if (tc) {
             const TcScratch ws{a->fTp.as<float>(), a->fT.as<float>(), a->tcThi.as<float>(),
                                a->tcTlo.as<float>(), a->Bx.as<float>(), a->svec.as<double>(),
-                               a->ybx.as<double>(), a->fmom.as<double>(), a->tcErr.as<int>()};
+                               a->ybx.as<double>(), a->fmom.as<double>(), a->tcErr.as<int>(),
+                               a->tcTab.ptr};
             fast_project_tc(a->st, src, tb, n, m, Pc, a->y.as<float>(), a->tol, ws,
                             &a->stats.kernel_launches);
         } else {

@@ -225,6 +225,30 @@ __device__ __forceinline__ uint32_t sw128_off(int r, int k)
     return (uint32_t)(r * 128 + ((((k >> 2) ^ (r & 7)) & 7) << 4) + ((k & 3) << 2));
 }
 
+// The raw columns and scale of each candidate's source (Src::raw0/raw1/param),
+// gathered once per call so the kernels read one table entry per candidate
+// instead of following the candidate's index arrays for every element.
+struct SrcEntry {
+    const float *p0;
+    const float *p1;
+    float prm;
+};
+
+template <class Src>
+__global__ void k_tc_srctab(Src src, int P, SrcEntry *__restrict__ tab)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < P) {
+        tab[j] = SrcEntry{src.raw0(j), src.raw1(j), src.param(j)};
+    }
+}
+
+template <class Src>
+__device__ __forceinline__ float src_value(const SrcEntry &e, int i)
+{
+    return Src::kRaw == 2 ? Src::combine(e.p0[i], e.p1[i], e.prm) : e.p0[i];
+}
+
 // ---------------------------------------------------------------------------
 // Split copies of basis column c.
 // ---------------------------------------------------------------------------
@@ -272,8 +296,10 @@ struct TgLayout {
         b_bytes = (uint32_t)Np * 128;     // one Np x 32 f32 operand tile
         stage = 2 * a_bytes + 2 * b_bytes;  // a_hi, a_lo, b_hi, b_lo
         bars = (uint32_t)S * stage;
-        total = bars + (uint32_t)(3 * S + 5) * 8 + 16;
+        tab = bars + (uint32_t)(3 * S + 5) * 8 + 16;
+        total = tab + TG_M * (uint32_t)sizeof(SrcEntry);
     }
+    uint32_t tab;
 };
 
 // Two loads of 8 consecutive columns of this warp's lanes, one wait.
@@ -297,7 +323,7 @@ __device__ __forceinline__ void tmem_ld8x2(uint32_t ta, uint32_t tb, float (&a)[
 
 template <class Src>
 __global__ void __launch_bounds__(TG_THREADS, 1)
-    k_tc_tgemm(Src src, const __grid_constant__ CUtensorMap map_hi,
+    k_tc_tgemm(const SrcEntry *__restrict__ tab, const __grid_constant__ CUtensorMap map_hi,
                const __grid_constant__ CUtensorMap map_lo, int n, int m, int P, int rps,
                int stages, float *__restrict__ Tp, int *__restrict__ err)
 {
@@ -314,9 +340,14 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
     uint64_t *drain_bar = acc_empty + 2;                              // MMAs in flight at an abort
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain_bar + 1);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    SrcEntry *stab = reinterpret_cast<SrcEntry *>(sm + L.tab);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int j0 = blockIdx.x * TG_M, split = blockIdx.y;
+    if (threadIdx.x < TG_M) {
+        const int j = j0 + threadIdx.x;
+        stab[threadIdx.x] = j < P ? tab[j] : SrcEntry{nullptr, nullptr, 0.f};
+    }
     const int r0 = split * rps, r1 = min(n, r0 + rps);
     const int ksteps = r1 > r0 ? (r1 - r0 + TG_K - 1) / TG_K : 0;
     const int nchunks = (ksteps + TG_CHUNK - 1) / TG_CHUNK;
@@ -352,17 +383,32 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
     if (warp < TG_PROD) {
         // Producers: warp w forms candidates [16 w, 16 w + 16) of the tile,
         // lane = row within the K step.
+        // The loads of step k + 1 are issued before step k is stored, so two
+        // steps of source values are in flight per warp.
+        float vn[16];
+        auto load = [&](int k) {
+            const int i = r0 + k * TG_K + lane;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const SrcEntry e = stab[warp * 16 + q];
+                vn[q] = (i < r1 && e.p0 != nullptr) ? src_value<Src>(e, i) : 0.f;
+            }
+        };
+        if (ksteps > 0) {
+            load(0);
+        }
         for (int k = 0; k < ksteps; ++k) {
             const int s = k % S, fill = k / S;
-            if (fill >= 1 && !mbar_wait_warp(&empty[s], (fill - 1) & 1, abort_flag, err)) {
-                break;
-            }
-            const int i = r0 + k * TG_K + lane;
             float v[16];
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
-                const int j = j0 + warp * 16 + q;
-                v[q] = (i < r1 && j < P) ? src((size_t)i, j) : 0.f;
+                v[q] = vn[q];
+            }
+            if (k + 1 < ksteps) {
+                load(k + 1);
+            }
+            if (fill >= 1 && !mbar_wait_warp(&empty[s], (fill - 1) & 1, abort_flag, err)) {
+                break;
             }
             unsigned char *ahi = sm + (size_t)s * L.stage;
             unsigned char *alo = ahi + L.a_bytes;
@@ -533,7 +579,7 @@ __global__ void k_tc_treduce(const float *__restrict__ Tp, int ks, int P, int m,
 // ---------------------------------------------------------------------------
 // k_tc_project: Bx[i, j] = src(i, j) - sum_c Bo[i, c] T[j][c], persistent
 // ---------------------------------------------------------------------------
-constexpr int TP_EPI = 4;                       // epilogue warps
+constexpr int TP_EPI = 8;                       // epilogue warps
 constexpr int TP_THREADS = 32 * (TP_EPI + 2);   // + TMA warp + MMA warp
 constexpr int TP_M = 128;                       // rows per tile
 constexpr int TP_N = 64;                        // candidates per tile
@@ -553,7 +599,7 @@ struct TpLayout {
 
 template <class Src>
 __global__ void __launch_bounds__(TP_THREADS, 2)
-    k_tc_project(Src src, const __grid_constant__ CUtensorMap a_hi,
+    k_tc_project(const SrcEntry *__restrict__ tab, const __grid_constant__ CUtensorMap a_hi,
                  const __grid_constant__ CUtensorMap a_lo, const __grid_constant__ CUtensorMap b_hi,
                  const __grid_constant__ CUtensorMap b_lo, int n, int m, int P,
                  float *__restrict__ Bx, size_t ldBx, int *__restrict__ err)
@@ -674,42 +720,55 @@ __global__ void __launch_bounds__(TP_THREADS, 2)
             }
         }
     } else {
-        // Epilogue: warp w owns rows 32 w .. 32 w + 31 of each tile.
+        // Epilogue: warp w reads lanes 32 (w % 4) .. (the tile's rows) and
+        // handles candidates [32 h, 32 h + 32), h = w / 4, in two groups of
+        // 16: the source values are loaded before the accumulator is waited
+        // for, so their latency overlaps the MMAs.
+        const int lg = warp & 3, h = warp >> 2;
         long u = 0;
-        for (long t = blockIdx.x; t < tiles; t += gridDim.x, ++u) {
+        bool ok = true;
+        for (long t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++u) {
             const int b = (int)(u & 1);
-            if (!mbar_wait_warp(&acc_full[b], (uint32_t)((u >> 1) & 1), abort_flag, err)) {
-                break;
-            }
-            tc_fence_after();
-            const int row0 = (int)(t / ct) * TP_M, cand0 = (int)(t % ct) * TP_N;
-            float acc[TP_N];
+            const int row0 = (int)(t / ct) * TP_M, cand0 = (int)(t % ct) * TP_N + 32 * h;
+            const int i = row0 + 32 * lg + lane;
+            for (int g = 0; g < 2; ++g) {
+                float v[16];
 #pragma unroll
-            for (int ch = 0; ch < TP_N / 8; ++ch) {
-                float x[8], y[8];
-                const uint32_t tm = tmem + ((uint32_t)(32 * warp) << 16) +
-                                    (uint32_t)(b * 2 * TP_N + 8 * ch);
-                tmem_ld8x2(tm, tm + TP_N, x, y);
-#pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    acc[8 * ch + c] = __fadd_rn(x[c], y[c]);
+                for (int q = 0; q < 16; ++q) {
+                    const int j = cand0 + 16 * g + q;
+                    v[q] = (i < n && j < P) ? src_value<Src>(tab[j], i) : 0.f;
                 }
+                if (g == 0) {
+                    if (!mbar_wait_warp(&acc_full[b], (uint32_t)((u >> 1) & 1), abort_flag, err)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                }
+                const uint32_t tm = tmem + ((uint32_t)(32 * lg) << 16) +
+                                    (uint32_t)(b * 2 * TP_N + 32 * h + 16 * g);
+                float x0[8], y0[8], x1[8], y1[8];
+                tmem_ld8x2(tm, tm + TP_N, x0, y0);
+                tmem_ld8x2(tm + 8, tm + TP_N + 8, x1, y1);
+                if (i < n) {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const int j = cand0 + 16 * g + q;
+                        const float d = q < 8 ? __fadd_rn(x0[q], y0[q])
+                                              : __fadd_rn(x1[q - 8], y1[q - 8]);
+                        if (j < P) {
+                            Bx[(size_t)j * ldBx + i] = __fsub_rn(v[q], d);
+                        }
+                    }
+                }
+            }
+            if (!ok) {
+                break;
             }
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
                 mbar_arrive(&acc_empty[b]);
-            }
-            const int i = row0 + 32 * warp + lane;
-            if (i < n) {
-#pragma unroll
-                for (int c = 0; c < TP_N; ++c) {
-                    const int j = cand0 + c;
-                    if (j < P) {
-                        const float v = src((size_t)i, j);
-                        Bx[(size_t)j * ldBx + i] = __fsub_rn(v, acc[c]);
-                    }
-                }
             }
         }
     }
@@ -798,6 +857,14 @@ void check_err(cudaStream_t st, int *err)
 }
 
 template <class Src>
+void build_tab(cudaStream_t st, const Src &src, int P, SrcEntry *tab, long long *launches)
+{
+    k_tc_srctab<Src><<<(unsigned)ceil_div((size_t)P, 256), 256, 0, st>>>(src, P, tab);
+    LAUNCH_CHECK();
+    *launches += 1;
+}
+
+template <class Src>
 void t_pass(cudaStream_t st, const Src &src, const TcBasis &tb, int n, int m, int P,
             const TcScratch &ws, long long *launches)
 {
@@ -810,7 +877,8 @@ void t_pass(cudaStream_t st, const Src &src, const TcBasis &tb, int n, int m, in
     const size_t smem = L.total + 1024;
     allow_smem(k_tc_tgemm<Src>, smem);
     const dim3 grid((unsigned)ceil_div((size_t)P, TG_M), (unsigned)ks);
-    k_tc_tgemm<Src><<<grid, TG_THREADS, smem, st>>>(src, mh, ml, n, m, P, rps, S, ws.Tp, ws.err);
+    k_tc_tgemm<Src><<<grid, TG_THREADS, smem, st>>>(static_cast<const SrcEntry *>(ws.tab), mh, ml, n, m, P, rps, S, ws.Tp,
+                                                     ws.err);
     LAUNCH_CHECK();
     const size_t cnt = (size_t)P * tb.ldk;
     k_tc_treduce<<<(unsigned)ceil_div(cnt, 256), 256, 0, st>>>(ws.Tp, ks, P, m, tb.ldk, ws.T,
@@ -832,8 +900,8 @@ void p_pass(cudaStream_t st, const Src &src, const TcBasis &tb, int n, int m, in
     allow_smem(k_tc_project<Src>, smem);
     const long tiles = (long)ceil_div((size_t)n, TP_M) * (long)ceil_div((size_t)P, TP_N);
     const long grid = std::min<long>(tiles, 2L * sm_count());
-    k_tc_project<Src><<<(unsigned)grid, TP_THREADS, smem, st>>>(src, ah, al, bh, bl, n, m, P,
-                                                                ws.Bx, (size_t)n, ws.err);
+    k_tc_project<Src><<<(unsigned)grid, TP_THREADS, smem, st>>>(static_cast<const SrcEntry *>(ws.tab), ah, al, bh, bl, n, m,
+                                                                P, ws.Bx, (size_t)n, ws.err);
     LAUNCH_CHECK();
     *launches += 1;
 }
@@ -841,6 +909,7 @@ void p_pass(cudaStream_t st, const Src &src, const TcBasis &tb, int n, int m, in
 }  // namespace
 
 size_t tc_ldn(size_t n) { return round_up(std::max<size_t>(n, 1), 32); }
+size_t tc_tab_bytes(size_t P) { return sizeof(SrcEntry) * std::max<size_t>(P, 1); }
 size_t tc_ldk(size_t max_terms) { return round_up(std::max<size_t>(max_terms, 1), 32); }
 
 void tc_store_column(cudaStream_t st, const float *col, int n, int c, const TcBasis &tb,
@@ -854,8 +923,9 @@ void tc_store_column(cudaStream_t st, const float *col, int n, int c, const TcBa
 
 int tc_ksplit(int n, int P)
 {
+    // one wave of one block per SM (a second, partial wave would double the time)
     const int tiles = (int)ceil_div((size_t)std::max(P, 1), TG_M);
-    const int want = std::max(1, (sm_count() + tiles - 1) / tiles);
+    const int want = std::max(1, sm_count() / tiles);
     return std::max(1, std::min(want, std::max(1, n / (8 * TG_K))));
 }
 
@@ -864,6 +934,7 @@ void tc_project_pass(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int
 {
     verify(m >= 1 && m <= TC_MAX_M, "the tensor-core projection takes 1..128 basis columns");
     CUDA_CHECK(cudaMemsetAsync(ws.err, 0, sizeof(int), st));
+    build_tab(st, src, P, static_cast<SrcEntry *>(ws.tab), launches);
     t_pass(st, src, tb, n, m, P, ws, launches);
     p_pass(st, src, tb, n, m, P, ws, launches);
     check_err(st, ws.err);
@@ -878,9 +949,11 @@ void fast_project_tc(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int
     }
     verify(m >= 1 && m <= TC_MAX_M, "the tensor-core projection takes 1..128 basis columns");
     CUDA_CHECK(cudaMemsetAsync(ws.err, 0, sizeof(int), st));
+    build_tab(st, src, P, static_cast<SrcEntry *>(ws.tab), launches);
     t_pass(st, src, tb, n, m, P, ws, launches);
     p_pass(st, src, tb, n, m, P, ws, launches);
     const StoredSrc stored{ws.Bx, (size_t)n, nullptr};
+    build_tab(st, stored, P, static_cast<SrcEntry *>(ws.tab), launches);
     t_pass(st, stored, tb, n, m, P, ws, launches);
     p_pass(st, stored, tb, n, m, P, ws, launches);
     fast_norms_moments(st, ws.Bx, n, y, tol, src, P, ws.s, ws.ybx, ws.mom, launches);
@@ -899,7 +972,7 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
                                        const float *s, const int *cand_x, const int *cand_b,
                                        const float *Bo, size_t ldBo, const float *y, double tol,
                                        int use_tc, int passes, float *T, float *Bx,
-                                       double *s_out, double *ybx_out)
+                                       double *s_out, double *ybx_out, float *ms_out)
 {
     using namespace mgpu;
     try {
@@ -924,9 +997,9 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
             ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
         } guard{st};
         DevBuf dB, dX, ds, dcx, dcb, dBoC, dy, dTp, dT, dThi, dTlo, dBx, dS, dYbx, dMom, dErr,
-            hiC, loC, hiR, loR;
+            hiC, loC, hiR, loR, dTab;
         for (DevBuf *b : {&dB, &dX, &ds, &dcx, &dcb, &dBoC, &dy, &dTp, &dT, &dThi, &dTlo, &dBx,
-                          &dS, &dYbx, &dMom, &dErr, &hiC, &loC, &hiR, &loR}) {
+                          &dS, &dYbx, &dMom, &dErr, &hiC, &loC, &hiR, &loR, &dTab}) {
             b->bind(st);
         }
         dB.ensure(sizeof(float) * n * ncolB);
@@ -954,6 +1027,13 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
         long long launches = 0;
         const FillSrc src{dB.as<float>(), n, dX.as<float>(), n, ds.as<float>(), dcx.as<int>(),
                           dcb.as<int>()};
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        CUDA_CHECK(cudaEventCreate(&e0));
+        CUDA_CHECK(cudaEventCreate(&e1));
+        struct EventGuard {
+            cudaEvent_t a, b;
+            ~EventGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
+        } eguard{e0, e1};
         if (use_tc) {
             TcBasis tb;
             tb.ldn = tc_ldn(n);
@@ -977,9 +1057,11 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
             dThi.ensure(sizeof(float) * P * tb.ldk);
             dTlo.ensure(sizeof(float) * P * tb.ldk);
             dErr.ensure(sizeof(int));
+            dTab.ensure(tc_tab_bytes(P));
             TcScratch ws{dTp.as<float>(), dT.as<float>(), dThi.as<float>(), dTlo.as<float>(),
                          dBx.as<float>(), dS.as<double>(), dYbx.as<double>(), dMom.as<double>(),
-                         dErr.as<int>()};
+                         dErr.as<int>(), dTab.ptr};
+            CUDA_CHECK(cudaEventRecord(e0, st));
             if (passes == 1) {
                 tc_project_pass(st, src, tb, (int)n, (int)m, (int)P, ws, &launches);
             } else {
@@ -991,9 +1073,11 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
             dTp.ensure(sizeof(float) * (size_t)ks * P * m);
             FastScratch ws{dTp.as<float>(), dT.as<float>(), dBx.as<float>(), dS.as<double>(),
                            dYbx.as<double>(), dMom.as<double>()};
+            CUDA_CHECK(cudaEventRecord(e0, st));
             fast_project(st, src, dBoC.as<float>(), (int)n, (int)m, (int)P, dy.as<float>(), tol,
                          ws, &launches);
         }
+        CUDA_CHECK(cudaEventRecord(e1, st));
         CUDA_CHECK(cudaMemcpyAsync(T, dT.ptr, sizeof(float) * P * m, cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaMemcpyAsync(Bx, dBx.ptr, sizeof(float) * n * P, cudaMemcpyDeviceToHost,
                                    st));
@@ -1006,6 +1090,9 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
                                        cudaMemcpyDeviceToHost, st));
         }
         CUDA_CHECK(cudaStreamSynchronize(st));
+        if (ms_out) {
+            CUDA_CHECK(cudaEventElapsedTime(ms_out, e0, e1));
+        }
         return MARS_GPU_OK;
     } catch (const Error &e) {
         set_last_error(e.what());

@@ -39,12 +39,16 @@ struct TcScratch {
     double *ybx; // [P]
     double *mom; // [3 P] parent moments (as the SIMT fast pass)
     int *err;    // one int: nonzero when a bounded wait inside a kernel gave up
+    void *tab;   // tc_tab_bytes(P): per candidate, its source columns and scale
 };
 
 // Largest basis the tensor-core path takes: the T contraction keeps two
 // buffers of two 128 x round_up(m, 16) FP32 accumulators in the 512 columns
 // of tensor memory.
 constexpr int TC_MAX_M = 128;
+
+// Bytes of the per-candidate source table of P candidates.
+size_t tc_tab_bytes(size_t P);
 
 // Leading dimensions of the split basis copies for n rows and max_terms columns.
 size_t tc_ldn(size_t n);

@@ -90,7 +90,7 @@ def load():
                                                 vp, d, vp, lp]),
         "mars_gpu_pool_used_bytes": (i, [ctypes.POINTER(sz)]),
         "mars_gpu_fast_project": (i, [sz, sz, sz, fp, sz, sz, fp, sz, sz, fp, ip, ip, fp, sz, fp,
-                                      d, i, i, fp, fp, dp, dp]),
+                                      d, i, i, fp, fp, dp, dp, fp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -263,12 +263,13 @@ def orthonormalize_col(v, Bo, m, tol):
     return w.value, v, c.value
 
 
-def fast_project(B, X, s, cand_x, cand_b, Bo, m, y, tol, use_tc=True, passes=2):
+def fast_project(B, X, s, cand_x, cand_b, Bo, m, y, tol, use_tc=True, passes=2, timing=None):
     """The fast pass's projection (mars_gpu_fast_project) on host arrays:
     candidate j = B[:, cand_b[j]] * (X[:, cand_x[j]] * s[cand_x[j]]), projected
     off the first m columns of Bo (n, >= m) column-major f32. Returns
     (T (P, m) f32 of the last pass, Bx (n, P) f32 Fortran order, s, ybx);
-    s and ybx are None for passes=1."""
+    s and ybx are None for passes=1. `timing`, a list, receives the device
+    milliseconds of the projection kernels."""
     L = load()
     B = np.asfortranarray(B, dtype=np.float32)
     X = np.asfortranarray(X, dtype=np.float32)
@@ -282,13 +283,16 @@ def fast_project(B, X, s, cand_x, cand_b, Bo, m, y, tol, use_tc=True, passes=2):
     Bx = np.empty((n, P), dtype=np.float32, order="F")
     so = np.empty(P)
     yo = np.empty(P)
+    ms = ctypes.c_float(0.0)
     check(L.mars_gpu_fast_project(n, m, P, _p(B, ctypes.c_float), n, B.shape[1],
                                   _p(X, ctypes.c_float), n, X.shape[1], _p(s, ctypes.c_float),
                                   _p(cx, ctypes.c_int), _p(cb, ctypes.c_int),
                                   _p(Bo, ctypes.c_float), n, _p(y, ctypes.c_float), float(tol),
                                   int(bool(use_tc)), int(passes), _p(T, ctypes.c_float),
                                   _p(Bx, ctypes.c_float), _p(so, ctypes.c_double),
-                                  _p(yo, ctypes.c_double)))
+                                  _p(yo, ctypes.c_double), ctypes.byref(ms)))
+    if timing is not None:
+        timing.append(ms.value)
     if passes == 1:
         return T, Bx, None, None
     return T, Bx, so, yo

@@ -20,6 +20,7 @@ FIT_CASES = [
     "batched_small_2",
     "default_tail",
     "precision_stress",
+    "precision_stress_tail0",
     "batched_top_0",
     "batched_top_1",
     "batched_top_2",
@@ -27,8 +28,8 @@ FIT_CASES = [
 ]
 # Fixtures that take minutes to hours of reference CPU time; the tests that
 # need them skip when they are absent.
-LARGE_CASES = ["precision_stress", "batched_top_0", "batched_top_1", "batched_top_2",
-               "batched_top_3"]
+LARGE_CASES = ["precision_stress", "precision_stress_tail0", "batched_top_0", "batched_top_1",
+               "batched_top_2", "batched_top_3"]
 EVAL_CASES = ["eval_planted_knot", "eval_ties"]
 EVAL_MAX_TERMS = 16
 
@@ -66,6 +67,9 @@ def fit_case(name):
         # the full precision-stress workload at the reference's default tail span
         X, y, kw = workloads.precision_stress()
         kw["tail_span"] = 0.02
+    elif name == "precision_stress_tail0":
+        # the same workload with cuts scored down to the last rows (tail_span 0)
+        X, y, kw = workloads.precision_stress()
     elif name.startswith("batched_top_"):
         k = int(name.rsplit("_", 1)[1])
         X, y, kw = workloads.batched_fits_top(4)[k]
