@@ -29,6 +29,7 @@
  *                              mars::cuda::orthonormalize  cuda/mars_cuda.h:127-131
  *    mars_gpu_orthonormalize_col  mars::orthonormalize_col  kernels.h:91-96
  *    mars_gpu_expand(_backward)   mars.expand (numpy)        mars.py:423-450
+ *    mars_gpu_gram                mars.gram (numpy)          mars.py:456-490
  */
 #ifndef MARS_GPU_H
 #define MARS_GPU_H
@@ -268,6 +269,20 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
                                        const float *Bo, size_t ldBo, const float *y, double tol,
                                        int use_tc, int passes, float *T, float *Bx,
                                        double *s_out, double *ybx_out, float *ms_out);
+
+/*
+ *  mars_gpu_gram: out (ka x kb, row-major) = A^T B for A (n, ka) and B (n, kb)
+ *  column-major f32 host arrays (column strides lda, ldb >= n), in the
+ *  arithmetic of mars.gram (mars.py:456-490): per 128-row chunk a fused
+ *  multiply-add chain in f32 over the rows in order, the chunk results added
+ *  in float64 in chunk order. The Gram matrices of the backward pass
+ *  (mars.prune, mars.py:622-695).
+ */
+MARS_GPU_API int mars_gpu_gram(size_t n, const float *A, size_t lda, size_t ka, const float *B,
+                               size_t ldb, size_t kb, double *out);
+/* The same for float64 inputs (the chunk chains in float64). */
+MARS_GPU_API int mars_gpu_gram_f64(size_t n, const double *A, size_t lda, size_t ka,
+                                   const double *B, size_t ldb, size_t kb, double *out);
 
 /*
  *  Bytes currently handed out by the library's stream-ordered memory pool on

@@ -12,6 +12,7 @@ filter (mars.py:237-239, 319-323), first-maximum argmax over (input, parent)
 (mars.py:342-343), the GCV choice between a linear term and a hinge pair
 (mars.py:349-357), and the stop rules (mars.py:393-406).
 """
+import io
 import os
 import sys
 import time
@@ -21,7 +22,8 @@ import numpy as np
 from . import marslib
 
 __version__ = marslib.__version__
-__all__ = ["fit", "expand", "pprint", "__version__"]
+__all__ = ["fit", "expand", "pprint", "gram", "prune", "compact", "dumps", "loads", "save",
+           "load", "__version__"]
 
 MODEL_DTYPE = np.dtype(
     [
@@ -271,6 +273,194 @@ def expand(X, model):
         else:
             assert False, "unknown basis type %r" % kind
     return B
+
+
+# ---------------------------------------------------------------------------
+# Backward pass (mars.py:456-695): Gram matrices on the GPU, then backward
+# elimination by rank-1 Schur downdates of the inverse Gram matrix.
+# ---------------------------------------------------------------------------
+def gram(A, B=None):
+    """A.T @ B (A.T @ A when B is None) with float64 accumulation over
+    128-row chunks, on the GPU in the reference's arithmetic (mars.py:456-490;
+    mars_gpu_gram, or mars_gpu_gram_f64 for float64 inputs). 1-D
+    arguments are columns; the result is a float when both are 1-D, 1-D when
+    one is, else 2-D."""
+    if B is None:
+        B = A
+    A = np.asarray(A)
+    B = np.asarray(B)
+    if len(A) != len(B):
+        raise ValueError("shapes are not aligned: %s x %s" % (A.shape, B.shape))
+    A2 = A.reshape(len(A), -1) if A.ndim == 1 else A
+    B2 = B.reshape(len(B), -1) if B.ndim == 1 else B
+    out = marslib.gram(A2, B2)
+    if A.ndim == 1 and B.ndim == 1:
+        return float(out[0, 0])
+    if A.ndim == 1:
+        return out[0]
+    if B.ndim == 1:
+        return out[:, 0]
+    return out
+
+
+def _cholesky_inverse(XX, XY, YY, idx, ridge):
+    """(H, beta, SSE) on the active columns idx: H the inverse of the loaded
+    Gram block, beta = H XY, SSE = YY - XY . beta (mars.py:496-544). A block
+    that is not numerically positive definite gets a last-resort diagonal
+    jitter, so H stays a true inverse."""
+    import scipy.linalg
+
+    m = len(idx)
+    if m == 0:
+        return np.zeros((0, 0)), np.zeros(0), float(YY)
+    G = XX[np.ix_(idx, idx)]
+    g = XY[idx]
+    if ridge > 0:
+        G = G + ridge * np.eye(m)
+    try:
+        L = np.linalg.cholesky(G)
+    except np.linalg.LinAlgError:
+        L = np.linalg.cholesky(G + 1e-8 * (np.trace(G) / m + 1.0) * np.eye(m))
+    factor = (L, True)
+    beta = scipy.linalg.cho_solve(factor, g)
+    H = scipy.linalg.cho_solve(factor, np.eye(m))
+    return H, beta, max(float(YY - g @ beta), 0.0)
+
+
+def _eliminate(XX, XY, YY, mask, penalty, n_true, ridge=0.0):
+    """Backward stepwise selection (mars.py:547-619): repeatedly drop the
+    active column with the least SSE increase beta_j^2 / H_jj (never the
+    intercept, global column 0), downdating H and beta by a rank-1 Schur
+    complement, refreshing them from a Cholesky every max(64, M/4) drops,
+    and keep the subset with the best GCV seen."""
+    M = len(XX)
+    idx = np.flatnonzero(mask)
+    if len(idx) == 0:
+        return mask.copy()
+    H, beta, sse = _cholesky_inverse(XX, XY, YY, idx, ridge)
+
+    def gcv(v, m):
+        d = 1.0 - (m + penalty * (m - 1)) / n_true
+        return v / (d * d) if d > 0 else np.inf
+
+    best, keep = gcv(sse, len(idx)), mask.copy()
+    cur = mask.copy()
+    refresh, since = max(64, M // 4), 0
+    while len(idx):
+        h = np.diag(H)
+        floor = 1e-12 * max(float(h.max()), 1.0)
+        cost = np.full(len(beta), np.inf)
+        np.divide(beta * beta, h, out=cost, where=h > floor)
+        if idx[0] == 0:
+            cost[0] = np.inf  # the intercept stays
+        j = int(np.argmin(cost))
+        if not np.isfinite(cost[j]):
+            break
+        sse += max(float(cost[j]), 0.0)
+        col = H[:, j]
+        v = col / H[j, j]
+        beta = beta - beta[j] * v
+        H = H - np.outer(v, col)
+        H = 0.5 * (H + H.T)
+        np.fill_diagonal(H, np.maximum(np.diag(H), 0.0))
+        beta = np.delete(beta, j)
+        H = np.delete(np.delete(H, j, axis=0), j, axis=1)
+        cur[idx[j]] = False
+        idx = np.delete(idx, j)
+        since += 1
+        if since >= refresh and len(idx):
+            H, beta, sse = _cholesky_inverse(XX, XY, YY, idx, ridge)
+            since = 0
+        g = gcv(sse, len(idx))
+        if g < best:
+            best, keep = g, cur.copy()
+    return keep
+
+
+def prune(B, y, w=None, n_true=None, penalty=3.0, ridge=0.0, mask=None):
+    """Coefficients of the basis B (n, M) by backward stepwise selection with
+    GCV (mars.py:622-695; Friedman 1991, section 3.4): the intercept column 0
+    is never dropped, columns are standardised to a unit Gram diagonal (so
+    `ridge` acts alike on every column), pruned terms get coefficient 0, and
+    the result is in the original scale. The Gram matrices run on the GPU."""
+    B = np.asarray(B)
+    y = np.asarray(y)
+    n, M = B.shape
+    if n_true is None:
+        n_true = n
+    bad = ~np.isfinite(y)
+    if bad.any():
+        w = np.ones(len(y), dtype=B.dtype) if w is None else np.asarray(w)
+        w = np.where(bad, 0, w)
+        y = np.where(bad, 0, y)
+    if w is not None:
+        root = np.sqrt(np.asarray(w, dtype=B.dtype))
+        B = B * root[:, None]
+        y = y * root
+    XX = gram(B)
+    XY = gram(B, y)
+    YY = gram(y, y)
+    d = np.sqrt(np.diag(XX))
+    live = d > 0
+    scale = np.where(live, d, 1.0)
+    XX = XX / scale / scale[:, None]
+    XY = XY / scale
+    mask = (np.array(mask) if mask is not None else np.ones(M, dtype=bool)) & live
+    chosen = _eliminate(XX, XY, YY, mask, penalty, n_true, ridge)
+    if ridge > 0:
+        XX = XX + ridge * np.eye(M)
+    beta = np.zeros(M)
+    if chosen.any():
+        beta[chosen] = np.linalg.lstsq(XX[np.ix_(chosen, chosen)], XY[chosen], rcond=None)[0]
+    return beta / scale
+
+
+# ---------------------------------------------------------------------------
+# Model surgery and storage (mars.py:701-735; the model dtype, mars.py:261-274)
+# ---------------------------------------------------------------------------
+def compact(model):
+    """The model without its pruned terms (beta == 0), keeping every ancestor
+    a kept term needs (with its beta, possibly 0) and renumbering the parent
+    pointers (mars.py:701-735)."""
+    keep = np.asarray(model["beta"]) != 0
+    for i in range(len(model) - 1, 0, -1):  # parents precede their children
+        if keep[i] and model[i]["type"] != b"i":
+            keep[model[i]["basis"]] = True
+    where = np.full(len(model), -1, dtype="i4")
+    where[keep] = np.arange(int(keep.sum()), dtype="i4")
+    out = model[keep].copy()
+    out["basis"] = where[out["basis"]]
+    return out
+
+
+def _checked(model):
+    model = np.asarray(model)
+    if model.dtype != MODEL_DTYPE or model.ndim != 1:
+        raise ValueError("not a MARS model array (dtype %s)" % (model.dtype,))
+    return model
+
+
+def dumps(model):
+    """The model as bytes: the .npy encoding of its structured array (the
+    model dtype, little-endian), no pickling."""
+    buf = io.BytesIO()
+    np.save(buf, np.ascontiguousarray(_checked(model)), allow_pickle=False)
+    return buf.getvalue()
+
+
+def loads(data):
+    """A model from dumps() bytes; the dtype is checked."""
+    return _checked(np.load(io.BytesIO(data), allow_pickle=False))
+
+
+def save(path, model):
+    with open(path, "wb") as f:
+        f.write(dumps(model))
+
+
+def load(path):
+    with open(path, "rb") as f:
+        return loads(f.read())
 
 
 def pprint(model, beta=None, labels=None):

@@ -89,6 +89,8 @@ def load():
         "mars_gpu_orthonormalize_noalloc": (i, [sz, sz, sz, vp, sz, sz, vp, ip, vp, sz, vp, sz,
                                                 vp, d, vp, lp]),
         "mars_gpu_pool_used_bytes": (i, [ctypes.POINTER(sz)]),
+        "mars_gpu_gram": (i, [sz, fp, sz, sz, fp, sz, sz, dp]),
+        "mars_gpu_gram_f64": (i, [sz, dp, sz, sz, dp, sz, sz, dp]),
         "mars_gpu_fast_project": (i, [sz, sz, sz, fp, sz, sz, fp, sz, sz, fp, ip, ip, fp, sz, fp,
                                       d, i, i, fp, fp, dp, dp, fp]),
     }
@@ -296,6 +298,27 @@ def fast_project(B, X, s, cand_x, cand_b, Bo, m, y, tol, use_tc=True, passes=2, 
     if passes == 1:
         return T, Bx, None, None
     return T, Bx, so, yo
+
+
+def gram(A, B):
+    """A.T @ B (A: (n, ka), B: (n, kb), 2-D) with FP64 accumulation on the
+    GPU: float32 inputs (exact FP64 products, mars_gpu_gram) unless either is
+    float64 (mars_gpu_gram_f64)."""
+    L = load()
+    wide = np.asarray(A).dtype == np.float64 or np.asarray(B).dtype == np.float64
+    dt, ct = (np.float64, ctypes.c_double) if wide else (np.float32, ctypes.c_float)
+    fn = L.mars_gpu_gram_f64 if wide else L.mars_gpu_gram
+    A = np.asfortranarray(A, dtype=dt)
+    B = np.asfortranarray(B, dtype=dt)
+    if A.ndim != 2 or B.ndim != 2 or A.shape[0] != B.shape[0]:
+        raise ValueError("shapes are not aligned: %s x %s" % (A.shape, B.shape))
+    n, ka = A.shape
+    kb = B.shape[1]
+    out = np.zeros((ka, kb))
+    if ka and kb:
+        check(fn(n, _p(A, ct), max(n, 1), ka, _p(B, ct), max(n, 1), kb,
+                 _p(out, ctypes.c_double)))
+    return out
 
 
 def pool_used_bytes():

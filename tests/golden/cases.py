@@ -31,6 +31,10 @@ FIT_CASES = [
 LARGE_CASES = ["precision_stress", "precision_stress_tail0", "batched_top_0", "batched_top_1",
                "batched_top_2", "batched_top_3"]
 EVAL_CASES = ["eval_planted_knot", "eval_ties"]
+# Backward-pass (prune) fixtures: the reference's prune on the expanded golden
+# models, and on small scenarios.
+PRUNE_MODEL_CASES = ["hinge_search", "precision_stress_small", "weighted_nan"]
+PRUNE_CASES = ["prune_" + c for c in PRUNE_MODEL_CASES] + ["prune_scenarios"]
 EVAL_MAX_TERMS = 16
 
 
@@ -123,3 +127,55 @@ def eval_mask(p, m, i):
         mask[:, m // 2] = False
         mask[p - 1, 0] = False
     return mask
+
+
+def model_from_rows(rows):
+    """The model array (the forward pass's dtype) from a fit fixture's rows."""
+    from mars_gb300.mars import MODEL_DTYPE
+
+    model = np.zeros(len(rows), dtype=MODEL_DTYPE)
+    for i, r in enumerate(rows):
+        model[i] = (r["type"].encode(), r["basis"], r["input"],
+                    np.nan if r["hinge"] is None else r["hinge"], np.nan, r["r2"],
+                    r["r2_cv"], r["order"], 0.0)
+    return model
+
+
+def prune_variants(M):
+    """(name, kwargs) of the prune calls each model fixture pins."""
+    mask = np.ones(M, dtype=bool)
+    mask[-3:] = False
+    return [("default", {}), ("ridge", dict(ridge=1e-3)), ("mask", dict(mask=mask)),
+            ("penalty2", dict(penalty=2.0))]
+
+
+def prune_scenarios():
+    """Small backward-pass problems (float64 B, as a user may pass): an exact
+    fit, tiny noise columns, a zero-variance column, a masked term, a ridge, an
+    intercept alone, observation weights, two nearly equal noise columns.
+    Returns a list of (B, y, w or None, kwargs)."""
+    rng = np.random.default_rng(31)
+    out = []
+    n = 200
+    x = rng.standard_normal((n, 4))
+    B = np.column_stack([np.ones(n), x[:, 0], x[:, 1]])
+    out.append((B, B @ np.array([1.0, 3.0, -2.0]), None, dict(n_true=n)))
+    B = np.column_stack([np.ones(n), x[:, 0], 0.01 * x[:, 1], 0.01 * x[:, 2]])
+    out.append((B, 5.0 + 3.0 * x[:, 0], None, dict(n_true=n)))
+    B = np.column_stack([np.ones(n), x[:, 0], np.zeros(n)])
+    out.append((B, 2.0 + 4.0 * x[:, 0], None, {}))
+    B = np.column_stack([np.ones(n), x[:, 0], x[:, 1]])
+    out.append((B, 1.0 + 2.0 * x[:, 0] + 3.0 * x[:, 1], None,
+                dict(mask=np.array([True, True, False]))))
+    B = np.column_stack([np.ones(n), x[:, 2]])
+    out.append((B, B @ np.array([5.0, 10.0]), None, dict(ridge=0.5)))
+    out.append((np.ones((100, 1)), np.full(100, 3.0), None, {}))
+    B = np.column_stack([np.ones(300), rng.standard_normal((300, 2))])
+    out.append((B, 1.0 + 2.0 * B[:, 1] - 0.5 * B[:, 2], rng.uniform(0.1, 2.0, 300), {}))
+    n = 50
+    shared = 0.15 * rng.standard_normal(n)
+    B = np.column_stack([np.ones(n), rng.standard_normal((n, 2)),
+                         shared + 0.01 * rng.standard_normal(n),
+                         shared + 0.01 * rng.standard_normal(n)])
+    out.append((B, 1.0 + 2.0 * B[:, 1] - 1.5 * B[:, 2], None, {}))
+    return out

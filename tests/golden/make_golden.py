@@ -96,12 +96,37 @@ def eval_fixture(ref_marslib, name):
     print("%-24s eval fixture (%d evals)" % (name, len(evals)))
 
 
+def prune_fixture(ref_mars, name):
+    """The reference's prune (mars.py:622-695) on the expanded golden model
+    of a fit case, or on the small scenarios."""
+    res = {}
+    if name == "prune_scenarios":
+        for i, (B, y, w, kw) in enumerate(cases.prune_scenarios()):
+            res["beta_%d" % i] = ref_mars.prune(B, y, w, **kw)
+        res["digest"] = np.array(workloads.digest(
+            *[a for B, y, w, _ in cases.prune_scenarios() for a in (B, y)]))
+    else:
+        fit = name[len("prune_"):]
+        with open(os.path.join(HERE, fit + ".json")) as f:
+            rows = json.load(f)["model"]
+        X, y, w, _ = cases.fit_case(fit)
+        model = cases.model_from_rows(rows)
+        B = ref_mars.expand(X, model)
+        for tag, kw in cases.prune_variants(len(model)):
+            res["beta_" + tag] = ref_mars.prune(B, y, w, **kw)
+        res["digest"] = np.array(workloads.digest(B, y))
+    np.savez(os.path.join(HERE, name + ".npz"), **res)
+    print("%-24s prune fixture" % name)
+
+
 def main(argv):
     ref_mars, ref_marslib = _import_reference()
-    names = argv or (cases.FIT_CASES + cases.EVAL_CASES)
+    names = argv or (cases.FIT_CASES + cases.EVAL_CASES + cases.PRUNE_CASES)
     for name in names:
         if name in cases.FIT_CASES:
             fit_fixture(ref_mars, name)
+        elif name in cases.PRUNE_CASES:
+            prune_fixture(ref_mars, name)
         else:
             eval_fixture(ref_marslib, name)
 
