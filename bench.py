@@ -89,6 +89,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the FP64 comparator fits when timing the mixed path")
+    ap.add_argument("--profile-epochs", action="store_true",
+                    help="end the fit once the timed epochs are done and print only their "
+                         "timing (short runs for ncu captures)")
     ap.add_argument("--shard", action="store_true",
                     help="under torchrun: one fit sharded by input column over the ranks "
                          "(mars_gb300/shard.py) instead of one replica per rank")
@@ -542,6 +545,10 @@ STAT_KEYS = ("ms_project", "ms_sweep", "ms_dgks", "ms_normalize", "ms_append", "
              "h2d_bytes", "d2h_bytes", "knot_evals", "dgks_fired")
 
 
+class StopFit(Exception):
+    """Raised from the fit's callback to end a profiling run early."""
+
+
 class EpochSteps:
     """Step boundaries at the epochs of one or more fits.
 
@@ -551,8 +558,9 @@ class EpochSteps:
     wall time and the counters are accumulated, handle by handle when the
     region spans two fits."""
 
-    def __init__(self, warmup, steps, on_open=None, on_close=None):
+    def __init__(self, warmup, steps, on_open=None, on_close=None, stop_when_closed=False):
         self.W, self.K = warmup, steps
+        self.stop_when_closed = stop_when_closed
         self.on_open, self.on_close = on_open, on_close
         self.done = 0
         self.timing = False
@@ -606,6 +614,8 @@ class EpochSteps:
             self.closed = True
             if self.on_close:
                 self.on_close()
+            if self.stop_when_closed:
+                raise StopFit()
 
 
 def epoch_fit(X, y, kw, precision, steps, shard=False):
@@ -630,7 +640,10 @@ def epoch_fit(X, y, kw, precision, steps, shard=False):
 
         fit_lib = sharded(lib)
     t0 = time.perf_counter()
-    model = forward_pass(fit_lib, X, y, None, callback=lambda *a: steps.epoch(), **kw)
+    try:
+        model = forward_pass(fit_lib, X, y, None, callback=lambda *a: steps.epoch(), **kw)
+    except StopFit:
+        return None, time.perf_counter() - t0, lib.algo.stats(), lib.knot_evals
     wall = time.perf_counter() - t0
     st = lib.algo.stats()
     st["orth_max"], st["rss"] = lib.algo.orth_error()
@@ -781,11 +794,20 @@ def run_epoch_steps(args):
         if tdist is not None:
             tdist.barrier()
 
-    steps = EpochSteps(args.warmup, args.steps, opened, closed)
+    steps = EpochSteps(args.warmup, args.steps, opened, closed, args.profile_epochs)
     shard = args.shard and tdist is not None
     fits = []
     while not steps.closed:
         fits.append(epoch_fit(X, y, kw, args.precision, steps, shard))
+    if args.profile_epochs:
+        acc = steps.acc
+        if RANK == 0:
+            print(json.dumps({"profile_epochs": [args.warmup, args.warmup + args.steps - 1],
+                              "ms_per_step": steps.span_ms / args.steps,
+                              "phase_ms_per_step": {k[3:]: acc[k] / args.steps for k in STAT_KEYS
+                                                    if k.startswith("ms_")},
+                              "gpu_launches": int(acc["kernel_launches"])}))
+        return 0
         if len(fits) > 1 + (args.warmup + args.steps) // 2:
             raise RuntimeError("the fit stops before its epochs reach the timed region")
     clk = clk.get("v")

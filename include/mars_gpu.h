@@ -275,14 +275,17 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
  *  column-major f32 host arrays (column strides lda, ldb >= n), in the
  *  arithmetic of mars.gram (mars.py:456-490): per 128-row chunk a fused
  *  multiply-add chain in f32 over the rows in order, the chunk results added
- *  in float64 in chunk order. The Gram matrices of the backward pass
- *  (mars.prune, mars.py:622-695).
+ *  in float64 in chunk order. exact = 1 instead widens every product exactly
+ *  and runs the chunk chains in FP64 (for the matrix-vector products, which
+ *  the reference's BLAS forms in another order). The Gram matrices of the
+ *  backward pass (mars.prune, mars.py:622-695).
  */
 MARS_GPU_API int mars_gpu_gram(size_t n, const float *A, size_t lda, size_t ka, const float *B,
-                               size_t ldb, size_t kb, double *out);
+                               size_t ldb, size_t kb, int exact, double *out);
 /* The same for float64 inputs (the chunk chains in float64). */
 MARS_GPU_API int mars_gpu_gram_f64(size_t n, const double *A, size_t lda, size_t ka,
-                                   const double *B, size_t ldb, size_t kb, double *out);
+                                   const double *B, size_t ldb, size_t kb, int exact,
+                                   double *out);
 
 /*
  *  Bytes currently handed out by the library's stream-ordered memory pool on

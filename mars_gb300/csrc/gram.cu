@@ -10,7 +10,11 @@
 // 1e-8 flips a pruning decision of the hinge-search golden fit -- so this
 // kernel reproduces that arithmetic: per entry, per 128-row chunk, an FMA
 // chain in the input dtype, then the FP64 chunk-order total. One thread per
-// entry, the chunk's rows staged in shared memory.
+// entry, the chunk's rows staged in shared memory. The reference forms its
+// matrix-vector and vector-vector products (X^T y, y^T y) with other BLAS
+// kernels that keep several partial sums; those run here with `exact` set:
+// products widened exactly, FP64 chains (closer to any such order than an
+// f32 chain is).
 #include "../../include/mars_gpu.h"
 #include "common.cuh"
 
@@ -25,7 +29,10 @@ constexpr int GR_CHUNK = 128;  // the reference's chunk of rows
 __device__ __forceinline__ float fma_e(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fma_e(double a, double b, double c) { return __fma_rn(a, b, c); }
 
-template <class E>
+// Acc = E: the reference's chunk chains; Acc = double: every product widened
+// exactly and the chunk chain in FP64 (the matrix-vector products, whose
+// reference BLAS order is not a plain chain).
+template <class E, class Acc>
 __global__ void __launch_bounds__(GR_T *GR_T)
     k_gram(const E *__restrict__ A, size_t lda, int ka, const E *__restrict__ B, size_t ldb,
            int kb, int n, double *__restrict__ out)
@@ -43,9 +50,9 @@ __global__ void __launch_bounds__(GR_T *GR_T)
             sB[rr][c] = (rr < rows && j0 + c < kb) ? B[(size_t)(j0 + c) * ldb + r] : E(0);
         }
         __syncthreads();
-        E acc = E(0);
+        Acc acc = Acc(0);
         for (int rr = 0; rr < rows; ++rr) {
-            acc = fma_e(sA[rr][ty], sB[rr][tx], acc);
+            acc = fma_e((Acc)sA[rr][ty], (Acc)sB[rr][tx], acc);
         }
         total = __dadd_rn(total, (double)acc);
         __syncthreads();
@@ -58,7 +65,7 @@ __global__ void __launch_bounds__(GR_T *GR_T)
 
 template <class E>
 int gram_impl(size_t n, const E *A, size_t lda, size_t ka, const E *B, size_t ldb, size_t kb,
-              double *out)
+              int exact, double *out)
 {
     try {
         verify(mars_gpu_device_count() > 0, "no CUDA device is visible", MARS_GPU_ECUDA);
@@ -91,8 +98,14 @@ int gram_impl(size_t n, const E *A, size_t lda, size_t ka, const E *B, size_t ld
         const size_t cnt = ka * kb;
         dOut.ensure(sizeof(double) * cnt);
         const dim3 grid((unsigned)ceil_div(ka, GR_T), (unsigned)ceil_div(kb, GR_T));
-        k_gram<E><<<grid, GR_T * GR_T, 0, st>>>(dA.as<E>(), n, (int)ka, dB.as<E>(), n, (int)kb,
-                                                (int)n, dOut.as<double>());
+        if (exact) {
+            k_gram<E, double><<<grid, GR_T * GR_T, 0, st>>>(dA.as<E>(), n, (int)ka, dB.as<E>(),
+                                                            n, (int)kb, (int)n,
+                                                            dOut.as<double>());
+        } else {
+            k_gram<E, E><<<grid, GR_T * GR_T, 0, st>>>(dA.as<E>(), n, (int)ka, dB.as<E>(), n,
+                                                       (int)kb, (int)n, dOut.as<double>());
+        }
         LAUNCH_CHECK();
         CUDA_CHECK(cudaMemcpyAsync(out, dOut.ptr, sizeof(double) * cnt, cudaMemcpyDeviceToHost,
                                    st));
@@ -113,15 +126,16 @@ int gram_impl(size_t n, const E *A, size_t lda, size_t ka, const E *B, size_t ld
 extern "C" {
 
 MARS_GPU_API int mars_gpu_gram(size_t n, const float *A, size_t lda, size_t ka, const float *B,
-                               size_t ldb, size_t kb, double *out)
+                               size_t ldb, size_t kb, int exact, double *out)
 {
-    return mgpu::gram_impl(n, A, lda, ka, B, ldb, kb, out);
+    return mgpu::gram_impl(n, A, lda, ka, B, ldb, kb, exact, out);
 }
 
 MARS_GPU_API int mars_gpu_gram_f64(size_t n, const double *A, size_t lda, size_t ka,
-                                   const double *B, size_t ldb, size_t kb, double *out)
+                                   const double *B, size_t ldb, size_t kb, int exact,
+                                   double *out)
 {
-    return mgpu::gram_impl(n, A, lda, ka, B, ldb, kb, out);
+    return mgpu::gram_impl(n, A, lda, ka, B, ldb, kb, exact, out);
 }
 
 }  // extern "C"

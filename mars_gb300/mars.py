@@ -293,7 +293,9 @@ def gram(A, B=None):
         raise ValueError("shapes are not aligned: %s x %s" % (A.shape, B.shape))
     A2 = A.reshape(len(A), -1) if A.ndim == 1 else A
     B2 = B.reshape(len(B), -1) if B.ndim == 1 else B
-    out = marslib.gram(A2, B2)
+    # matrix-matrix products in the reference's chunk arithmetic; products with
+    # a vector (its BLAS uses another order there) exactly, in FP64
+    out = marslib.gram(A2, B2, exact=A.ndim == 1 or B.ndim == 1)
     if A.ndim == 1 and B.ndim == 1:
         return float(out[0, 0])
     if A.ndim == 1:

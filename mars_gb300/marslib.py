@@ -89,8 +89,8 @@ def load():
         "mars_gpu_orthonormalize_noalloc": (i, [sz, sz, sz, vp, sz, sz, vp, ip, vp, sz, vp, sz,
                                                 vp, d, vp, lp]),
         "mars_gpu_pool_used_bytes": (i, [ctypes.POINTER(sz)]),
-        "mars_gpu_gram": (i, [sz, fp, sz, sz, fp, sz, sz, dp]),
-        "mars_gpu_gram_f64": (i, [sz, dp, sz, sz, dp, sz, sz, dp]),
+        "mars_gpu_gram": (i, [sz, fp, sz, sz, fp, sz, sz, i, dp]),
+        "mars_gpu_gram_f64": (i, [sz, dp, sz, sz, dp, sz, sz, i, dp]),
         "mars_gpu_fast_project": (i, [sz, sz, sz, fp, sz, sz, fp, sz, sz, fp, ip, ip, fp, sz, fp,
                                       d, i, i, fp, fp, dp, dp, fp]),
     }
@@ -300,10 +300,11 @@ def fast_project(B, X, s, cand_x, cand_b, Bo, m, y, tol, use_tc=True, passes=2, 
     return T, Bx, so, yo
 
 
-def gram(A, B):
-    """A.T @ B (A: (n, ka), B: (n, kb), 2-D) with FP64 accumulation on the
-    GPU: float32 inputs (exact FP64 products, mars_gpu_gram) unless either is
-    float64 (mars_gpu_gram_f64)."""
+def gram(A, B, exact=False):
+    """A.T @ B (A: (n, ka), B: (n, kb), 2-D) with FP64 accumulation over
+    128-row chunks on the GPU: float32 inputs (mars_gpu_gram) unless either is
+    float64 (mars_gpu_gram_f64); `exact` widens the products and runs the
+    chunk chains in FP64."""
     L = load()
     wide = np.asarray(A).dtype == np.float64 or np.asarray(B).dtype == np.float64
     dt, ct = (np.float64, ctypes.c_double) if wide else (np.float32, ctypes.c_float)
@@ -316,7 +317,7 @@ def gram(A, B):
     kb = B.shape[1]
     out = np.zeros((ka, kb))
     if ka and kb:
-        check(fn(n, _p(A, ct), max(n, 1), ka, _p(B, ct), max(n, 1), kb,
+        check(fn(n, _p(A, ct), max(n, 1), ka, _p(B, ct), max(n, 1), kb, int(bool(exact)),
                  _p(out, ctypes.c_double)))
     return out
 

@@ -8,9 +8,9 @@ rounded to f32 (exact unless the sum needs more than 53 bits, which these
 inputs never do), so the bound is 1e-15 relative. prune is compared with the
 reference's own prune on the golden fits and scenarios: the same selected
 terms, coefficients within 1e-5 of the largest (the reference computes its
-matrix-vector Gram products with several partial sums of its BLAS build; they
-differ from the chunk chains here by ~1e-8 and move the coefficients by
-~1e-6).
+matrix-vector Gram products with several partial sums of its BLAS build,
+which cannot be followed; those run here exactly in FP64, ~1e-8 from the
+reference's, and move the coefficients by ~1e-6).
 """
 import json
 import os
@@ -61,7 +61,8 @@ def test_gram_shapes_and_accumulation(gpu):
     assert mars.gram(A, y).shape == (4,)
     assert mars.gram(y, A).shape == (4,)
     assert isinstance(mars.gram(y, y), float)
-    np.testing.assert_allclose(mars.gram(A, y), A.T.astype(np.float64) @ y, atol=1e-5)
+    # a product with a vector is exact: FP64 chains of exactly widened products
+    np.testing.assert_allclose(mars.gram(A, y), A.T.astype(np.float64) @ y, rtol=1e-13)
     half = np.full((100_000, 1), 0.5, dtype=np.float32)
     assert mars.gram(half)[0, 0] == 25_000.0
     D = rng.standard_normal((500, 3))
