@@ -257,7 +257,8 @@ MARS_GPU_API int mars_gpu_orthonormalize_noalloc(size_t n, size_t m, size_t p, c
  *  the first one's residual) and fills s_out = ||Bx||^2 and
  *  ybx_out = (Bx . y) / sqrt(s + tol) (both optional); passes = 1 stops after
  *  one. T (P x m, row j = candidate j) receives the last pass's coefficients,
- *  Bx (n x P column-major, ld n) the projected columns. use_tc = 1: the
+ *  Bx (n x P row-major, candidate j of row i at Bx[i P + j], the layout the
+ *  fast hinge sweep reads) the projected columns. use_tc = 1: the
  *  tensor-core kernels (tcgen05, split-TF32; m <= 128); use_tc = 0: the FP32
  *  SIMT kernels (passes = 2 only). ms_out (optional) receives the device time
  *  of the projection kernels (CUDA events on the call's stream), copies

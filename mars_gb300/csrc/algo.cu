@@ -222,6 +222,11 @@ struct mars_gpu_algo {
     // copied so far.
     DevBuf tcHiC, tcLoC, tcHiR, tcLoR, tcThi, tcTlo, tcErr, tcTab;
     size_t tc_cols = 0;
+    // Fast pass: the basis row-major (BR, ldbr; br_cols columns copied), the
+    // norms' partial sums, and the column-major candidates of the FP32 SIMT
+    // projection before they are laid out by rows.
+    DevBuf BR, fNpart, fBxc;
+    size_t ldbr = 0, br_cols = 0;
     DevBuf sort_keys, sort_vals, sort_tmp;
     // Mixed mode: the exact re-decision speculated for the previous eval's
     // contenders and for the columns appended since, beside the fast pass.
@@ -310,7 +315,7 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
                       &a->stasks, &a->scal, &a->part, &a->bsort, &a->bxsort, &a->fTp, &a->fT,
                       &a->fmom, &a->hflag, &a->sort_keys, &a->sort_vals, &a->sort_tmp,
                       &a->tcHiC, &a->tcLoC, &a->tcHiR, &a->tcLoR, &a->tcThi, &a->tcTlo,
-                      &a->tcErr, &a->tcTab}) {
+                      &a->tcErr, &a->tcTab, &a->BR, &a->fNpart, &a->fBxc}) {
         b->bind(a->st);
     }
     CUDA_CHECK(cudaEventCreate(&a->span_begin));
@@ -639,6 +644,34 @@ bool use_tc(size_t m)
     return m <= (size_t)TC_MAX_M && env_double("MARS_GPU_TC", 1.0) != 0.0;
 }
 
+__global__ void k_col_to_rowmajor(const float *__restrict__ col, int n, float *__restrict__ BR,
+                                  size_t ld, int c)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        BR[(size_t)i * ld + c] = col[i];
+    }
+}
+
+// The row-major copy of the basis B read by the fast pass, allocated on first
+// use and brought up to the live basis.
+void br_sync(mars_gpu_algo *a)
+{
+    if (!a->BR.ptr) {
+        a->ldbr = round_up(a->max_terms, 4);
+        a->BR.ensure(sizeof(float) * a->n * a->ldbr);
+        CUDA_CHECK(cudaMemsetAsync(a->BR.ptr, 0, a->BR.bytes, a->st));
+        a->br_cols = 0;
+    }
+    for (; a->br_cols < a->m; ++a->br_cols) {
+        k_col_to_rowmajor<<<(unsigned)ceil_div(a->n, 256), 256, 0, a->st>>>(
+            a->B.as<float>() + a->br_cols * a->n, (int)a->n, a->BR.as<float>(), a->ldbr,
+            (int)a->br_cols);
+        LAUNCH_CHECK();
+        a->stats.kernel_launches += 1;
+    }
+}
+
 // The split basis copies of the tensor-core projection, allocated on first
 // use (zero-filled: rows past n and columns past m are read as zeros) and
 // brought up to the live basis.
@@ -697,7 +730,9 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
     const double budget = block_budget();
     const double ngrid = linear_only ? 0.0 : (double)sweep_grid_rows(head, tail, min_span);
     (void)ngrid;
-    const double per = 4.0 * n + 4.0 * m * (ks + 1) + 64.0;
+    const bool tc = use_tc(a->m);
+    // the FP32 SIMT projection keeps a column-major copy of its candidates too
+    const double per = (tc ? 4.0 : 8.0) * n + 4.0 * m * (ks + 1) + 64.0;
     size_t cap = (size_t)std::max(1.0, budget / per);
     cap = std::min<size_t>(cap, 262144);
     const auto blocks = block_candidates(cx, cap);
@@ -705,12 +740,18 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
     for (auto &b : blocks) {
         maxPc = std::max<size_t>(maxPc, b.second - b.first);
     }
-    a->Bx.ensure(sizeof(float) * a->n * maxPc);
+    // candidates row-major (ld ldr, set per block), so that the sweep reads a
+    // sorted row's values of a block's candidates together
+    a->Bx.ensure(sizeof(float) * a->n * round_up(maxPc, 4));
+    a->fNpart.ensure(fast_norm_part_bytes(a->n, maxPc));
+    if (!tc) {
+        a->fBxc.ensure(sizeof(float) * a->n * maxPc);
+    }
+    br_sync(a);
     a->svec.ensure(sizeof(double) * maxPc);
     a->ybx.ensure(sizeof(double) * maxPc);
     a->hsse.ensure(sizeof(double) * 2 * maxPc);  // two sweep directions
     a->hrow.ensure(sizeof(int) * 2 * maxPc);
-    const bool tc = use_tc(a->m);
     TcBasis tb;
     if (tc) {
         tb = tc_basis(a);
@@ -794,17 +835,22 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         a->stats.project_flops += 4.0 * (double)n * (double)m * (double)Pc;
         cudaEvent_t t0 = a->timer.begin();
         FillSrc src{a->B.as<float>(), a->n, a->X.as<float>(), a->n, a->s.as<float>(), cx_d, cb_d};
+        const size_t ldr = round_up((size_t)Pc, 4);
         if (tc) {
+            const RowFillSrc rsrc{a->BR.as<float>(), a->ldbr, a->X.as<float>(), a->n,
+                                  a->s.as<float>(), cx_d, cb_d};
             const TcScratch ws{a->fTp.as<float>(), a->fT.as<float>(), a->tcThi.as<float>(),
-                               a->tcTlo.as<float>(), a->Bx.as<float>(), a->svec.as<double>(),
-                               a->ybx.as<double>(), a->fmom.as<double>(), a->tcErr.as<int>(),
-                               a->tcTab.ptr};
-            fast_project_tc(a->st, src, tb, n, m, Pc, a->y.as<float>(), a->tol, ws,
+                               a->tcTlo.as<float>(), a->Bx.as<float>(), ldr,
+                               a->svec.as<double>(), a->ybx.as<double>(), a->fmom.as<double>(),
+                               a->tcErr.as<int>(), a->tcTab.ptr, a->fNpart.as<double>()};
+            fast_project_tc(a->st, src, rsrc, tb, n, m, Pc, a->y.as<float>(), a->tol, ws,
                             &a->stats.kernel_launches);
         } else {
-            FastScratch ws{a->fTp.as<float>(), a->fT.as<float>(), a->Bx.as<float>(),
+            FastScratch ws{a->fTp.as<float>(), a->fT.as<float>(), a->fBxc.as<float>(),
                            a->svec.as<double>(), a->ybx.as<double>(), a->fmom.as<double>()};
             fast_project(a->st, src, a->BoC.as<float>(), n, m, Pc, a->y.as<float>(), a->tol, ws,
+                         &a->stats.kernel_launches);
+            fast_to_rows(a->st, a->fBxc.as<float>(), n, Pc, a->Bx.as<float>(), ldr,
                          &a->stats.kernel_launches);
         }
         a->timer.end(PH_PROJECT, t0);
@@ -839,8 +885,8 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
                                        sizeof(FastTaskRec) * tasks.size(), cudaMemcpyHostToDevice,
                                        a->st));
             a->stats.h2d_bytes += (long long)(sizeof(FastTaskRec) * tasks.size());
-            const FastSweepCols cols{a->B.as<float>(), a->n,       cb_d,
-                                     a->Bx.as<float>(), a->n, a->svec.as<double>()};
+            const FastSweepCols cols{a->BR.as<float>(), a->ldbr, cb_d,
+                                     a->Bx.as<float>(), ldr,     a->svec.as<double>()};
             fast_sweep(a->st, a->tasks.as<FastTaskRec>(), (int)tasks.size(), a->perm.as<int>(),
                        a->xsort.as<float>(), a->ysort.as<float>(), cols, a->BoF.as<float>(), a->ldbo,
                        a->ybo_d.as<double>(), a->ybx.as<double>(), a->fmom.as<double>(), n, m,

@@ -198,6 +198,76 @@ __global__ void __launch_bounds__(256) k_parent_moments(FillSrc src, int n, doub
     }
 }
 
+// s and ybx of row-major candidate columns, in two deterministic steps: block
+// (32 candidates, one chunk of FN_ROWS rows): lane = candidate, warp w takes
+// rows w, w + 8, ... of the chunk, FP32 per thread, FP64 across the warps in
+// a fixed order, into part[chunk][j][2]; then k_fast_norms_rows_done adds the
+// chunks in order.
+constexpr int FN_ROWS = 4096;
+
+__global__ void __launch_bounds__(256)
+    k_fast_norms_rows(const float *__restrict__ Bx, size_t ldr, int n, const float *__restrict__ y,
+                      int P, double *__restrict__ part)
+{
+    __shared__ double red[2][8][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int j = blockIdx.x * 32 + lane, ch = blockIdx.y;
+    const int r0 = ch * FN_ROWS, r1 = min(n, r0 + FN_ROWS);
+    float a = 0.f, b = 0.f;
+    if (j < P) {
+#pragma unroll 4
+        for (int i = r0 + w; i < r1; i += 8) {
+            const float v = Bx[(size_t)i * ldr + j];
+            a = fmaf(v, v, a);
+            b = fmaf(v, y[i], b);
+        }
+    }
+    red[0][w][lane] = (double)a;
+    red[1][w][lane] = (double)b;
+    __syncthreads();
+    if (w < 2 && j < P) {
+        double t = 0.0;
+        for (int q = 0; q < 8; ++q) {
+            t += red[w][q][lane];
+        }
+        part[((size_t)ch * P + j) * 2 + w] = t;
+    }
+}
+
+__global__ void k_fast_norms_rows_done(const double *__restrict__ part, int nch, int P,
+                                       double tol, double *__restrict__ s, double *__restrict__ ybx)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < P) {
+        double a = 0.0, b = 0.0;
+        for (int c = 0; c < nch; ++c) {
+            a += part[((size_t)c * P + j) * 2];
+            b += part[((size_t)c * P + j) * 2 + 1];
+        }
+        s[j] = a;
+        ybx[j] = (double)fast_scale(a, tol) * b;
+    }
+}
+
+// Column-major (ld n) candidate columns to the row-major layout (ld ldr).
+__global__ void k_fast_to_rows(const float *__restrict__ Bc, int n, int P, float *__restrict__ Br,
+                               size_t ldr)
+{
+    __shared__ float t[32][33];
+    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+    for (int q = threadIdx.y; q < 32; q += blockDim.y) {
+        const int i = i0 + threadIdx.x, j = j0 + q;
+        t[q][threadIdx.x] = (i < n && j < P) ? Bc[(size_t)j * n + i] : 0.f;
+    }
+    __syncthreads();
+    for (int q = threadIdx.y; q < 32; q += blockDim.y) {
+        const int i = i0 + q, j = j0 + threadIdx.x;
+        if (i < n && j < P) {
+            Br[(size_t)i * ldr + j] = t[threadIdx.x][q];
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Chunked sweep. Block = one input column, one direction and up to W
 // candidates (warps 0..W-1, lane = component) plus two loader warps that stage
@@ -440,9 +510,9 @@ __global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
         const int pi = ok ? pk[i] : 0;  // the row of sorted position i
         for (int cw = 0; cw < task.count; ++cw) {
             const int bc = __shfl_sync(0xffffffffu, pcol, cw);
-            cp_async4(rw + cw * FS_RS + lane, cols.B + (size_t)bc * cols.ldB + pi, ok);
+            cp_async4(rw + cw * FS_RS + lane, cols.BR + (size_t)pi * cols.ldBR + bc, ok);
             cp_async4(rw + (W + cw) * FS_RS + lane,
-                      cols.Bx + (size_t)(task.cand0 + cw) * cols.ldBx + pi, ok);
+                      cols.Bx + (size_t)pi * cols.ldr + task.cand0 + cw, ok);
         }
         cp_async4(rw + 2 * W * FS_RS + lane, ys + i, ok);
         cp_async4(rw + (2 * W + 1) * FS_RS + 1 + lane, xs + i, ok);
@@ -818,6 +888,42 @@ int fast_ksplit(int n) { return std::max(1, std::min(64, n / 2048)); }
 int fast_sweep_mid(int head, int tail, int n)
 {
     return std::max(0, std::min((head + tail) / 2, n - 1));
+}
+
+size_t fast_norm_part_bytes(size_t n, size_t P)
+{
+    return sizeof(double) * 2 * std::max<size_t>(P, 1) * ceil_div(std::max<size_t>(n, 1), FN_ROWS);
+}
+
+void fast_norms_rows(cudaStream_t st, const float *Bx, size_t ldr, int n, const float *y,
+                     double tol, int P, double *part, double *s, double *ybx,
+                     long long *launches)
+{
+    const int nch = (int)ceil_div((size_t)std::max(n, 1), FN_ROWS);
+    const dim3 g((unsigned)ceil_div((size_t)P, 32), (unsigned)nch);
+    k_fast_norms_rows<<<g, 256, 0, st>>>(Bx, ldr, n, y, P, part);
+    LAUNCH_CHECK();
+    k_fast_norms_rows_done<<<(unsigned)ceil_div((size_t)P, 256), 256, 0, st>>>(part, nch, P, tol,
+                                                                             s, ybx);
+    LAUNCH_CHECK();
+    *launches += 2;
+}
+
+void fast_parent_moments(cudaStream_t st, const FillSrc &src, int n, int P, double *mom,
+                         long long *launches)
+{
+    k_parent_moments<<<(unsigned)P, 256, 0, st>>>(src, n, mom);
+    LAUNCH_CHECK();
+    *launches += 1;
+}
+
+void fast_to_rows(cudaStream_t st, const float *Bc, int n, int P, float *Br, size_t ldr,
+                  long long *launches)
+{
+    const dim3 g((unsigned)ceil_div((size_t)n, 32), (unsigned)ceil_div((size_t)P, 32));
+    k_fast_to_rows<<<g, dim3(32, 8), 0, st>>>(Bc, n, P, Br, ldr);
+    LAUNCH_CHECK();
+    *launches += 1;
 }
 
 void fast_norms_moments(cudaStream_t st, const float *Bx, int n, const float *y, double tol,

@@ -34,6 +34,19 @@ void fast_norms_moments(cudaStream_t st, const float *Bx, int n, const float *y,
                         const FillSrc &src, int P, double *s, double *ybx, double *mom,
                         long long *launches);
 
+// s and ybx (as fast_norms_moments) of row-major candidate columns Bx (ld
+// ldr); part holds fast_norm_part_bytes(n, P) of partial sums.
+size_t fast_norm_part_bytes(size_t n, size_t P);
+void fast_norms_rows(cudaStream_t st, const float *Bx, size_t ldr, int n, const float *y,
+                     double tol, int P, double *part, double *s, double *ybx,
+                     long long *launches);
+// The parent moments alone (the last step of fast_norms_moments).
+void fast_parent_moments(cudaStream_t st, const FillSrc &src, int n, int P, double *mom,
+                         long long *launches);
+// Column-major candidate columns (ld n) to the row-major layout (ld ldr).
+void fast_to_rows(cudaStream_t st, const float *Bc, int n, int P, float *Br, size_t ldr,
+                  long long *launches);
+
 // Chunked FP32 / FP64-carry hinge sweep of every candidate, in two halves:
 // tasks with dir 0 sweep from the top and score the cuts up to
 // fast_sweep_mid(), tasks with dir 1 sweep the mirror hinge from the bottom
@@ -45,14 +58,16 @@ void fast_norms_moments(cudaStream_t st, const float *Bx, int n, const float *y,
 // row-major f32 basis (ldbo a multiple of 4).
 int fast_sweep_warps(int m, const std::vector<int> &group_sizes);  // candidates per input column
 // The sweep's per-candidate columns, read in each input's sorted order by the
-// sweep itself: the parent B[:, cand_b[j]] and the projected candidate column
-// Bx[:, j], normalised there by f32(1 / sqrt(s[j] + tol)).
+// sweep itself, both row-major so that a sorted row's values for the block's
+// candidates share one or two memory sectors: the parent BR[i * ldBR +
+// cand_b[j]] (the row-major copy of the basis) and the projected candidate
+// Bx[i * ldr + j], normalised there by f32(1 / sqrt(s[j] + tol)).
 struct FastSweepCols {
-    const float *B;
-    size_t ldB;
+    const float *BR;
+    size_t ldBR;
     const int *cand_b;
     const float *Bx;
-    size_t ldBx;
+    size_t ldr;
     const double *s;
 };
 int fast_sweep_mid(int head, int tail, int n);  // in [0, n - 1]

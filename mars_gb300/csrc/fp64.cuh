@@ -27,6 +27,49 @@ struct FillSrc {
     __device__ __forceinline__ const float *raw1(int j) const { return X + (size_t)cand_x[j] * ldX; }
     __device__ __forceinline__ float param(int j) const { return s[cand_x[j]]; }
     __device__ __forceinline__ static float combine(float b, float x, float sx) { return b * (x * sx); }
+    // element strides of raw0 / raw1 from one row to the next
+    __host__ __device__ static constexpr size_t stride0() { return 1; }
+    __host__ __device__ static constexpr size_t stride1() { return 1; }
+};
+
+// FillSrc with the basis read from a row-major copy BR (n, ldBR): the same
+// value, B[i, b] * (X[i, x] * s[x]), for kernels whose warps cover several
+// candidates of one row (their parents then lie in one row of BR).
+struct RowFillSrc {
+    const float *BR;
+    size_t ldBR;
+    const float *X;
+    size_t ldX;
+    const float *s;
+    const int *cand_x;
+    const int *cand_b;
+    __device__ __forceinline__ float operator()(size_t i, int j) const
+    {
+        const int xc = cand_x[j];
+        return BR[i * ldBR + cand_b[j]] * (X[i + (size_t)xc * ldX] * s[xc]);
+    }
+    static constexpr int kRaw = 2;
+    __device__ __forceinline__ const float *raw0(int j) const { return BR + cand_b[j]; }
+    __device__ __forceinline__ const float *raw1(int j) const { return X + (size_t)cand_x[j] * ldX; }
+    __device__ __forceinline__ float param(int j) const { return s[cand_x[j]]; }
+    __device__ __forceinline__ static float combine(float b, float x, float sx) { return b * (x * sx); }
+    __host__ __device__ size_t stride0() const { return ldBR; }
+    __host__ __device__ static constexpr size_t stride1() { return 1; }
+};
+
+// Candidate columns stored row-major: Bx[i * ldr + j] (the mixed fast pass's
+// layout, so that a row's candidates are contiguous for the hinge sweep).
+struct RowStoredSrc {
+    const float *Bx;
+    size_t ldr;
+    __device__ __forceinline__ float operator()(size_t i, int j) const { return Bx[i * ldr + j]; }
+    static constexpr int kRaw = 1;
+    __device__ __forceinline__ const float *raw0(int j) const { return Bx + j; }
+    __device__ __forceinline__ const float *raw1(int j) const { return Bx + j; }
+    __device__ __forceinline__ float param(int) const { return 0.f; }
+    __device__ __forceinline__ static float combine(float v, float, float) { return v; }
+    __host__ __device__ size_t stride0() const { return ldr; }
+    __host__ __device__ size_t stride1() const { return ldr; }
 };
 
 // Candidate column source: an already-stored f32 column Bx[:, col[j]] (col may be null).
@@ -47,6 +90,8 @@ struct StoredSrc {
     __device__ __forceinline__ const float *raw1(int j) const { return raw0(j); }
     __device__ __forceinline__ float param(int) const { return 0.f; }
     __device__ __forceinline__ static float combine(float v, float, float) { return v; }
+    __host__ __device__ static constexpr size_t stride0() { return 1; }
+    __host__ __device__ static constexpr size_t stride1() { return 1; }
 };
 
 // One block of the hinge sweep: up to 8 candidates that share an input column.

@@ -225,13 +225,15 @@ __device__ __forceinline__ uint32_t sw128_off(int r, int k)
     return (uint32_t)(r * 128 + ((((k >> 2) ^ (r & 7)) & 7) << 4) + ((k & 3) << 2));
 }
 
-// The raw columns and scale of each candidate's source (Src::raw0/raw1/param),
-// gathered once per call so the kernels read one table entry per candidate
-// instead of following the candidate's index arrays for every element.
+// The raw columns and scale of each candidate's source, gathered once per
+// call so the kernels read one table entry per candidate instead of following
+// the candidate's index arrays for every element: value at row i =
+// Src::combine(p0[i * s0], p1[i * s1], prm) (a single load when Src::kRaw is 1).
 struct SrcEntry {
     const float *p0;
     const float *p1;
     float prm;
+    int s0, s1;
 };
 
 template <class Src>
@@ -239,14 +241,17 @@ __global__ void k_tc_srctab(Src src, int P, SrcEntry *__restrict__ tab)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j < P) {
-        tab[j] = SrcEntry{src.raw0(j), src.raw1(j), src.param(j)};
+        tab[j] = SrcEntry{src.raw0(j), src.raw1(j), src.param(j), (int)src.stride0(),
+                          (int)src.stride1()};
     }
 }
 
 template <class Src>
 __device__ __forceinline__ float src_value(const SrcEntry &e, int i)
 {
-    return Src::kRaw == 2 ? Src::combine(e.p0[i], e.p1[i], e.prm) : e.p0[i];
+    return Src::kRaw == 2
+               ? Src::combine(e.p0[(size_t)i * e.s0], e.p1[(size_t)i * e.s1], e.prm)
+               : e.p0[(size_t)i * e.s0];
 }
 
 // ---------------------------------------------------------------------------
@@ -346,7 +351,7 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
     const int j0 = blockIdx.x * TG_M, split = blockIdx.y;
     if (threadIdx.x < TG_M) {
         const int j = j0 + threadIdx.x;
-        stab[threadIdx.x] = j < P ? tab[j] : SrcEntry{nullptr, nullptr, 0.f};
+        stab[threadIdx.x] = j < P ? tab[j] : SrcEntry{nullptr, nullptr, 0.f, 0, 0};
     }
     const int r0 = split * rps, r1 = min(n, r0 + rps);
     const int ksteps = r1 > r0 ? (r1 - r0 + TG_K - 1) / TG_K : 0;
@@ -381,17 +386,25 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
     const uint32_t tmem = *tmem_slot;
 
     if (warp < TG_PROD) {
-        // Producers: warp w forms candidates [16 w, 16 w + 16) of the tile,
-        // lane = row within the K step.
-        // The loads of step k + 1 are issued before step k is stored, so two
-        // steps of source values are in flight per warp.
+        // Producers: warp w forms rows [4 w, 4 w + 4) of the K step, lane =
+        // candidate (lane + 32 q): with row-major sources a warp's loads for
+        // one row are contiguous. The loads of step k + 1 are issued before
+        // step k is stored, so two steps of source values are in flight.
         float vn[16];
-        auto load = [&](int k) {
-            const int i = r0 + k * TG_K + lane;
+        SrcEntry es[4];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const SrcEntry e = stab[warp * 16 + q];
-                vn[q] = (i < r1 && e.p0 != nullptr) ? src_value<Src>(e, i) : 0.f;
+        for (int q = 0; q < 4; ++q) {
+            es[q] = stab[lane + 32 * q];
+        }
+        auto load = [&](int k) {
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const int i = r0 + k * TG_K + 4 * warp + rr;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    vn[4 * rr + q] =
+                        (i < r1 && es[q].p0 != nullptr) ? src_value<Src>(es[q], i) : 0.f;
+                }
             }
         };
         if (ksteps > 0) {
@@ -413,13 +426,15 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
             unsigned char *ahi = sm + (size_t)s * L.stage;
             unsigned char *alo = ahi + L.a_bytes;
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int r = warp * 16 + q;
-                float h, l;
-                split_tf32(v[q], h, l);
-                const uint32_t off = sw128_off(r, lane);
-                *reinterpret_cast<float *>(ahi + off) = h;
-                *reinterpret_cast<float *>(alo + off) = l;
+            for (int rr = 0; rr < 4; ++rr) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float h, l;
+                    split_tf32(v[4 * rr + q], h, l);
+                    const uint32_t off = sw128_off(lane + 32 * q, 4 * warp + rr);
+                    *reinterpret_cast<float *>(ahi + off) = h;
+                    *reinterpret_cast<float *>(alo + off) = l;
+                }
             }
             fence_proxy_async();
             __syncwarp();
@@ -602,7 +617,7 @@ __global__ void __launch_bounds__(TP_THREADS, 2)
     k_tc_project(const SrcEntry *__restrict__ tab, const __grid_constant__ CUtensorMap a_hi,
                  const __grid_constant__ CUtensorMap a_lo, const __grid_constant__ CUtensorMap b_hi,
                  const __grid_constant__ CUtensorMap b_lo, int n, int m, int P,
-                 float *__restrict__ Bx, size_t ldBx, int *__restrict__ err)
+                 float *__restrict__ Bx, size_t ldr, int *__restrict__ err)
 {
     extern __shared__ unsigned char smraw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(
@@ -757,7 +772,7 @@ __global__ void __launch_bounds__(TP_THREADS, 2)
                         const float d = q < 8 ? __fadd_rn(x0[q], y0[q])
                                               : __fadd_rn(x1[q - 8], y1[q - 8]);
                         if (j < P) {
-                            Bx[(size_t)j * ldBx + i] = __fsub_rn(v[q], d);
+                            Bx[(size_t)i * ldr + j] = __fsub_rn(v[q], d);
                         }
                     }
                 }
@@ -901,7 +916,7 @@ void p_pass(cudaStream_t st, const Src &src, const TcBasis &tb, int n, int m, in
     const long tiles = (long)ceil_div((size_t)n, TP_M) * (long)ceil_div((size_t)P, TP_N);
     const long grid = std::min<long>(tiles, 2L * sm_count());
     k_tc_project<Src><<<(unsigned)grid, TP_THREADS, smem, st>>>(static_cast<const SrcEntry *>(ws.tab), ah, al, bh, bl, n, m,
-                                                                P, ws.Bx, (size_t)n, ws.err);
+                                                                P, ws.Bx, ws.ldr, ws.err);
     LAUNCH_CHECK();
     *launches += 1;
 }
@@ -929,7 +944,7 @@ int tc_ksplit(int n, int P)
     return std::max(1, std::min(want, std::max(1, n / (8 * TG_K))));
 }
 
-void tc_project_pass(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int n, int m,
+void tc_project_pass(cudaStream_t st, const RowFillSrc &src, const TcBasis &tb, int n, int m,
                      int P, const TcScratch &ws, long long *launches)
 {
     verify(m >= 1 && m <= TC_MAX_M, "the tensor-core projection takes 1..128 basis columns");
@@ -940,23 +955,24 @@ void tc_project_pass(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int
     check_err(st, ws.err);
 }
 
-void fast_project_tc(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int n, int m,
-                     int P, const float *y, double tol, const TcScratch &ws,
-                     long long *launches)
+void fast_project_tc(cudaStream_t st, const FillSrc &src, const RowFillSrc &rsrc,
+                     const TcBasis &tb, int n, int m, int P, const float *y, double tol,
+                     const TcScratch &ws, long long *launches)
 {
     if (P <= 0) {
         return;
     }
     verify(m >= 1 && m <= TC_MAX_M, "the tensor-core projection takes 1..128 basis columns");
     CUDA_CHECK(cudaMemsetAsync(ws.err, 0, sizeof(int), st));
-    build_tab(st, src, P, static_cast<SrcEntry *>(ws.tab), launches);
-    t_pass(st, src, tb, n, m, P, ws, launches);
-    p_pass(st, src, tb, n, m, P, ws, launches);
-    const StoredSrc stored{ws.Bx, (size_t)n, nullptr};
+    build_tab(st, rsrc, P, static_cast<SrcEntry *>(ws.tab), launches);
+    t_pass(st, rsrc, tb, n, m, P, ws, launches);
+    p_pass(st, rsrc, tb, n, m, P, ws, launches);
+    const RowStoredSrc stored{ws.Bx, ws.ldr};
     build_tab(st, stored, P, static_cast<SrcEntry *>(ws.tab), launches);
     t_pass(st, stored, tb, n, m, P, ws, launches);
     p_pass(st, stored, tb, n, m, P, ws, launches);
-    fast_norms_moments(st, ws.Bx, n, y, tol, src, P, ws.s, ws.ybx, ws.mom, launches);
+    fast_norms_rows(st, ws.Bx, ws.ldr, n, y, tol, P, ws.npart, ws.s, ws.ybx, launches);
+    fast_parent_moments(st, src, n, P, ws.mom, launches);
     check_err(st, ws.err);
 }
 
@@ -997,9 +1013,10 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
             ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
         } guard{st};
         DevBuf dB, dX, ds, dcx, dcb, dBoC, dy, dTp, dT, dThi, dTlo, dBx, dS, dYbx, dMom, dErr,
-            hiC, loC, hiR, loR, dTab;
+            hiC, loC, hiR, loR, dTab, dBR, dNpart, dBxc;
         for (DevBuf *b : {&dB, &dX, &ds, &dcx, &dcb, &dBoC, &dy, &dTp, &dT, &dThi, &dTlo, &dBx,
-                          &dS, &dYbx, &dMom, &dErr, &hiC, &loC, &hiR, &loR, &dTab}) {
+                          &dS, &dYbx, &dMom, &dErr, &hiC, &loC, &hiR, &loR, &dTab, &dBR, &dNpart,
+                          &dBxc}) {
             b->bind(st);
         }
         dB.ensure(sizeof(float) * n * ncolB);
@@ -1019,7 +1036,9 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
                                      cudaMemcpyHostToDevice, st));
         dy.ensure(sizeof(float) * n);
         CUDA_CHECK(cudaMemcpyAsync(dy.ptr, y, sizeof(float) * n, cudaMemcpyHostToDevice, st));
-        dBx.ensure(sizeof(float) * n * P);
+        const size_t ldr = round_up(P, 4), ldbr = round_up(ncolB, 4);
+        dBx.ensure(sizeof(float) * n * ldr);
+        dBR.ensure(sizeof(float) * n * ldbr);
         dS.ensure(sizeof(double) * P);
         dYbx.ensure(sizeof(double) * P);
         dMom.ensure(sizeof(double) * 3 * P);
@@ -1027,6 +1046,9 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
         long long launches = 0;
         const FillSrc src{dB.as<float>(), n, dX.as<float>(), n, ds.as<float>(), dcx.as<int>(),
                           dcb.as<int>()};
+        fast_to_rows(st, dB.as<float>(), (int)n, (int)ncolB, dBR.as<float>(), ldbr, &launches);
+        const RowFillSrc rsrc{dBR.as<float>(), ldbr, dX.as<float>(), n, ds.as<float>(),
+                              dcx.as<int>(), dcb.as<int>()};
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         CUDA_CHECK(cudaEventCreate(&e0));
         CUDA_CHECK(cudaEventCreate(&e1));
@@ -1058,29 +1080,33 @@ MARS_GPU_API int mars_gpu_fast_project(size_t n, size_t m, size_t P, const float
             dTlo.ensure(sizeof(float) * P * tb.ldk);
             dErr.ensure(sizeof(int));
             dTab.ensure(tc_tab_bytes(P));
-            TcScratch ws{dTp.as<float>(), dT.as<float>(), dThi.as<float>(), dTlo.as<float>(),
-                         dBx.as<float>(), dS.as<double>(), dYbx.as<double>(), dMom.as<double>(),
-                         dErr.as<int>(), dTab.ptr};
+            dNpart.ensure(fast_norm_part_bytes(n, P));
+            TcScratch ws{dTp.as<float>(), dT.as<float>(),    dThi.as<float>(),
+                         dTlo.as<float>(), dBx.as<float>(),  ldr,
+                         dS.as<double>(),  dYbx.as<double>(), dMom.as<double>(),
+                         dErr.as<int>(),   dTab.ptr,          dNpart.as<double>()};
             CUDA_CHECK(cudaEventRecord(e0, st));
             if (passes == 1) {
-                tc_project_pass(st, src, tb, (int)n, (int)m, (int)P, ws, &launches);
+                tc_project_pass(st, rsrc, tb, (int)n, (int)m, (int)P, ws, &launches);
             } else {
-                fast_project_tc(st, src, tb, (int)n, (int)m, (int)P, dy.as<float>(), tol, ws,
-                                &launches);
+                fast_project_tc(st, src, rsrc, tb, (int)n, (int)m, (int)P, dy.as<float>(), tol,
+                                ws, &launches);
             }
         } else {
             const int ks = fast_ksplit((int)n);
             dTp.ensure(sizeof(float) * (size_t)ks * P * m);
-            FastScratch ws{dTp.as<float>(), dT.as<float>(), dBx.as<float>(), dS.as<double>(),
+            dBxc.ensure(sizeof(float) * n * P);
+            FastScratch ws{dTp.as<float>(), dT.as<float>(), dBxc.as<float>(), dS.as<double>(),
                            dYbx.as<double>(), dMom.as<double>()};
             CUDA_CHECK(cudaEventRecord(e0, st));
             fast_project(st, src, dBoC.as<float>(), (int)n, (int)m, (int)P, dy.as<float>(), tol,
                          ws, &launches);
+            fast_to_rows(st, dBxc.as<float>(), (int)n, (int)P, dBx.as<float>(), ldr, &launches);
         }
         CUDA_CHECK(cudaEventRecord(e1, st));
         CUDA_CHECK(cudaMemcpyAsync(T, dT.ptr, sizeof(float) * P * m, cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaMemcpyAsync(Bx, dBx.ptr, sizeof(float) * n * P, cudaMemcpyDeviceToHost,
-                                   st));
+        CUDA_CHECK(cudaMemcpy2DAsync(Bx, P * 4, dBx.ptr, ldr * 4, P * 4, n,
+                                     cudaMemcpyDeviceToHost, st));
         if (s_out && passes == 2) {
             CUDA_CHECK(cudaMemcpyAsync(s_out, dS.ptr, sizeof(double) * P, cudaMemcpyDeviceToHost,
                                        st));

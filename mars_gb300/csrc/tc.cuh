@@ -17,6 +17,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "fast.cuh"
 #include "fp64.cuh"
 
 namespace mgpu {
@@ -34,12 +35,14 @@ struct TcScratch {
     float *T;    // [P][m] (f32 coefficients of the last pass)
     float *Thi;  // [P][ldk] split of T, zero past m
     float *Tlo;
-    float *Bx;   // (n, P) column-major, ld n
+    float *Bx;   // (n, P) row-major: candidate j of row i at Bx[i * ldr + j]
+    size_t ldr;  // >= P
     double *s;   // [P] squared norms
     double *ybx; // [P]
     double *mom; // [3 P] parent moments (as the SIMT fast pass)
     int *err;    // one int: nonzero when a bounded wait inside a kernel gave up
     void *tab;   // tc_tab_bytes(P): per candidate, its source columns and scale
+    double *npart;  // fast_norm_part_bytes(n, P): partial sums of the norms
 };
 
 // Largest basis the tensor-core path takes: the T contraction keeps two
@@ -61,15 +64,17 @@ void tc_store_column(cudaStream_t st, const float *col, int n, int c, const TcBa
 // Split-K factor of the tensor-core T contraction for n rows and P candidates.
 int tc_ksplit(int n, int P);
 
-// The two-pass projection, then s = ||Bx||^2, ybx = scale(s) (Bx . y) and the
-// parent moments, as fast_project (fast.cuh) computes them. Throws
-// mgpu::Error(MARS_GPU_ETIMEOUT) when a bounded device wait gave up.
-void fast_project_tc(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int n, int m,
-                     int P, const float *y, double tol, const TcScratch &ws,
-                     long long *launches);
+// The two-pass projection into row-major Bx, then s = ||Bx||^2,
+// ybx = scale(s) (Bx . y) and the parent moments, as fast_project (fast.cuh)
+// computes them. src and rsrc are the same candidates (rsrc reading the
+// row-major basis copy). Throws mgpu::Error(MARS_GPU_ETIMEOUT) when a bounded
+// device wait gave up.
+void fast_project_tc(cudaStream_t st, const FillSrc &src, const RowFillSrc &rsrc,
+                     const TcBasis &tb, int n, int m, int P, const float *y, double tol,
+                     const TcScratch &ws, long long *launches);
 
-// One pass only, for tests: T = Bo^T src and Bx = src - Bo T (src: FillSrc).
-void tc_project_pass(cudaStream_t st, const FillSrc &src, const TcBasis &tb, int n, int m,
+// One pass only, for tests: T = Bo^T src and Bx = src - Bo T.
+void tc_project_pass(cudaStream_t st, const RowFillSrc &src, const TcBasis &tb, int n, int m,
                      int P, const TcScratch &ws, long long *launches);
 
 }  // namespace mgpu

@@ -269,7 +269,7 @@ def fast_project(B, X, s, cand_x, cand_b, Bo, m, y, tol, use_tc=True, passes=2, 
     """The fast pass's projection (mars_gpu_fast_project) on host arrays:
     candidate j = B[:, cand_b[j]] * (X[:, cand_x[j]] * s[cand_x[j]]), projected
     off the first m columns of Bo (n, >= m) column-major f32. Returns
-    (T (P, m) f32 of the last pass, Bx (n, P) f32 Fortran order, s, ybx);
+    (T (P, m) f32 of the last pass, Bx (n, P) f32 row-major, s, ybx);
     s and ybx are None for passes=1. `timing`, a list, receives the device
     milliseconds of the projection kernels."""
     L = load()
@@ -282,7 +282,7 @@ def fast_project(B, X, s, cand_x, cand_b, Bo, m, y, tol, use_tc=True, passes=2, 
     cb = np.ascontiguousarray(cand_b, dtype=np.int32)
     n, P = B.shape[0], len(cx)
     T = np.empty((P, m), dtype=np.float32)
-    Bx = np.empty((n, P), dtype=np.float32, order="F")
+    Bx = np.empty((n, P), dtype=np.float32)  # row-major, as the fast sweep reads it
     so = np.empty(P)
     yo = np.empty(P)
     ms = ctypes.c_float(0.0)
