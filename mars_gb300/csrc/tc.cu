@@ -748,10 +748,29 @@ __global__ void __launch_bounds__(TP_THREADS, 2)
             const int i = row0 + 32 * lg + lane;
             for (int g = 0; g < 2; ++g) {
                 float v[16];
+                const int jg = cand0 + 16 * g;  // a multiple of 16
+                if (Src::kRaw == 1) {
+                    // row-major stored columns: four 16-byte loads of this row
+                    // (rows are 16-byte aligned; the padding up to a multiple
+                    // of 4 candidates is in bounds)
+                    const float *row = tab[0].p0 + (size_t)i * tab[0].s0;
 #pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const int j = cand0 + 16 * g + q;
-                    v[q] = (i < n && j < P) ? src_value<Src>(tab[j], i) : 0.f;
+                    for (int k4 = 0; k4 < 4; ++k4) {
+                        const int j = jg + 4 * k4;
+                        const float4 w = (i < n && j < P)
+                                             ? *reinterpret_cast<const float4 *>(row + j)
+                                             : make_float4(0.f, 0.f, 0.f, 0.f);
+                        v[4 * k4] = w.x;
+                        v[4 * k4 + 1] = w.y;
+                        v[4 * k4 + 2] = w.z;
+                        v[4 * k4 + 3] = w.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const int j = jg + q;
+                        v[q] = (i < n && j < P) ? src_value<Src>(tab[j], i) : 0.f;
+                    }
                 }
                 if (g == 0) {
                     if (!mbar_wait_warp(&acc_full[b], (uint32_t)((u >> 1) & 1), abort_flag, err)) {
@@ -766,13 +785,21 @@ __global__ void __launch_bounds__(TP_THREADS, 2)
                 tmem_ld8x2(tm, tm + TP_N, x0, y0);
                 tmem_ld8x2(tm + 8, tm + TP_N + 8, x1, y1);
                 if (i < n) {
+                    float o[16];
 #pragma unroll
                     for (int q = 0; q < 16; ++q) {
-                        const int j = cand0 + 16 * g + q;
                         const float d = q < 8 ? __fadd_rn(x0[q], y0[q])
                                               : __fadd_rn(x1[q - 8], y1[q - 8]);
+                        o[q] = __fsub_rn(v[q], d);
+                    }
+                    // 16-byte stores; columns past P up to ldr are padding
+                    float *row = Bx + (size_t)i * ldr;
+#pragma unroll
+                    for (int k4 = 0; k4 < 4; ++k4) {
+                        const int j = jg + 4 * k4;
                         if (j < P) {
-                            Bx[(size_t)i * ldr + j] = __fsub_rn(v[q], d);
+                            *reinterpret_cast<float4 *>(row + j) =
+                                make_float4(o[4 * k4], o[4 * k4 + 1], o[4 * k4 + 2], o[4 * k4 + 3]);
                         }
                     }
                 }
