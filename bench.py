@@ -125,6 +125,8 @@ class Counting:
         self.algo = None
         self.knot_evals = 0
         self.candidates = 0
+        self.wall_eval = 0.0    # host wall seconds inside eval / append calls
+        self.wall_append = 0.0
 
     def MarsAlgo(self, X, y, w, max_terms):
         from mars_gb300 import workloads
@@ -138,13 +140,22 @@ class Counting:
                 return getattr(inner, k)
 
             def eval(self, mask, min_span, endspan, linear_only, threads, cuda=False):
+                t0 = time.perf_counter()
                 res = inner.eval(mask, min_span, endspan, linear_only, threads, cuda)
+                outer.wall_eval += time.perf_counter() - t0
                 c = int(mask.sum())
                 outer.candidates += c
                 if not linear_only:
                     outer.knot_evals += c * workloads.knot_evals(n, endspan, min_span)
                 return res
 
+        def append(self_, *a):
+            t0 = time.perf_counter()
+            r = inner.append(*a)
+            outer.wall_append += time.perf_counter() - t0
+            return r
+
+        Wrapped.append = append
         self.algo = inner
         return Wrapped()
 
@@ -572,6 +583,8 @@ class EpochSteps:
         self.acc = {k: 0.0 for k in STAT_KEYS}
         self.epoch_ms = []      # device ms of every epoch of the first fit
         self._prev_span = 0.0
+        self.lib = None         # the Counting module of the current fit
+        self.walls = None       # (eval, append) host seconds at the region's start
 
     def _sync(self):
         import torch
@@ -606,9 +619,14 @@ class EpochSteps:
             self.timing = True
             self._base = self.algo.stats()
             self._t0 = time.perf_counter()
+            if self.lib is not None:
+                self.walls = (self.lib.wall_eval, self.lib.wall_append)
         elif self.timing and self.done == self.W + self.K:
             self._sync()
             self.wall += time.perf_counter() - self._t0
+            if self.lib is not None and self.walls is not None:
+                self.walls = (self.lib.wall_eval - self.walls[0],
+                              self.lib.wall_append - self.walls[1])
             self._fold(self.algo)
             self.timing = False
             self.closed = True
@@ -634,6 +652,7 @@ def epoch_fit(X, y, kw, precision, steps, shard=False):
         return a
 
     lib = Counting(factory)
+    steps.lib = lib
     fit_lib = lib
     if shard:
         from mars_gb300.shard import sharded
@@ -778,6 +797,13 @@ def run_epoch_steps(args):
     from mars_gb300 import marslib
 
     marslib.load()
+    # bring up torch's CUDA context now: the first torch.cuda.synchronize()
+    # costs ~1 s, which would otherwise fall between two of the fit's device
+    # events at the opening of the timed region
+    import torch
+
+    torch.cuda.init()
+    torch.cuda.synchronize()
     X, y, kw = workload(args.workload)
     clocks = Clocks() if RANK == 0 else None
     clk = {}
@@ -806,6 +832,10 @@ def run_epoch_steps(args):
                               "ms_per_step": steps.span_ms / args.steps,
                               "phase_ms_per_step": {k[3:]: acc[k] / args.steps for k in STAT_KEYS
                                                     if k.startswith("ms_")},
+                              "host_ms_per_step": {
+                                  "eval_call": 1e3 * steps.walls[0] / args.steps,
+                                  "append_call": 1e3 * steps.walls[1] / args.steps,
+                                  "wall": 1e3 * steps.wall / args.steps},
                               "gpu_launches": int(acc["kernel_launches"])}))
         return 0
         if len(fits) > 1 + (args.warmup + args.steps) // 2:
