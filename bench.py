@@ -552,8 +552,9 @@ def run_expand(args):
 
 STAT_KEYS = ("ms_project", "ms_sweep", "ms_dgks", "ms_normalize", "ms_append", "ms_sort",
              "ms_redecide", "ms_gather", "ms_redecide_gpu", "project_flops", "sweep_bytes",
-             "evals", "candidates", "redecided", "redecided_flagged", "kernel_launches",
-             "h2d_bytes", "d2h_bytes", "knot_evals", "dgks_fired")
+             "evals", "candidates", "redecided", "redecided_flagged", "redecided_degenerate",
+             "kernel_launches", "h2d_bytes", "d2h_bytes", "knot_evals", "dgks_fired",
+             "evals_exact")
 
 
 class StopFit(Exception):
@@ -836,7 +837,11 @@ def run_epoch_steps(args):
                                   "eval_call": 1e3 * steps.walls[0] / args.steps,
                                   "append_call": 1e3 * steps.walls[1] / args.steps,
                                   "wall": 1e3 * steps.wall / args.steps},
-                              "gpu_launches": int(acc["kernel_launches"])}))
+                              "gpu_launches": int(acc["kernel_launches"]),
+                              "per_step": {k: acc[k] / args.steps for k in
+                                           ("candidates", "redecided", "redecided_flagged",
+                                            "redecided_degenerate", "dgks_fired",
+                                            "evals_exact")}}))
         return 0
         if len(fits) > 1 + (args.warmup + args.steps) // 2:
             raise RuntimeError("the fit stops before its epochs reach the timed region")

@@ -91,6 +91,8 @@ typedef struct {
     long long leftovers_flagged; /* ... of which carried a flag */
     long long evals_exact;      /* mixed mode: evals run on the exact path after a step that
                                    re-decided most of its candidates */
+    long long redecided_degenerate; /* mixed mode: flagged candidates whose projected column
+                                       is nearly in the span of the basis */
 } mars_gpu_stats;
 
 /* Message of the last failing call on this thread ("" if none). */

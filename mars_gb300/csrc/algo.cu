@@ -978,10 +978,11 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         // are re-decided too, since the reference's value there may be large.
         const double degen = env_double("MARS_GPU_MIXED_DEGEN_REL", 1e-6);
         for (int j = 0; j < P; ++j) {
-            if (fs[j] < degen * fmom[3 * (size_t)j + 2] || fflag[2 * (size_t)j] ||
-                fflag[2 * (size_t)j + 1]) {
+            const bool dg = fs[j] < degen * fmom[3 * (size_t)j + 2];
+            if (dg || fflag[2 * (size_t)j] || fflag[2 * (size_t)j + 1]) {
                 contend[j] = 2;
                 ++a->stats.redecided_flagged;
+                a->stats.redecided_degenerate += dg ? 1 : 0;
             }
         }
     }

@@ -20,6 +20,7 @@
 #include "fast.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 
 namespace mgpu {
 namespace {
@@ -402,8 +403,10 @@ struct FastSweepSmem {
     }
 };
 
-template <int CPL, int S>
-__global__ void __launch_bounds__(32 * (FS_MAXW + 2), 1)
+// RB: blocks of the largest size meant to reside per SM (the register cap
+// follows from it).
+template <int CPL, int S, int RB>
+__global__ void __launch_bounds__(32 * (FS_MAXW + 2), RB)
     k_fast_sweep(const FastTask *__restrict__ tasks, const int *__restrict__ perm,
                  const float *__restrict__ xsort, const float *__restrict__ ysort,
                  const FastSweepCols cols,
@@ -988,6 +991,19 @@ static size_t fast_sweep_smem(int m, int w, int stages) { return FastSweepSmem(m
 // (228 KB per SM, 1 KB of it reserved per block) and registers.
 static int fast_sweep_regs();
 
+// Register cap of the sweep: MARS_GPU_FS_RB = 2 (the default: at most ~100
+// registers, two of the largest blocks per SM; measured on the n = 1e6 fit,
+// the sweep phase went 172 -> 132 ms a step at 13 basis columns and
+// 422 -> 328 ms at 50 against the uncapped kernel), 1 (no cap) or 3.
+static int fast_sweep_rb()
+{
+    static const int rb = [] {
+        const char *v = std::getenv("MARS_GPU_FS_RB");
+        return v && (*v == '1' || *v == '3') ? *v - '0' : 2;
+    }();
+    return rb;
+}
+
 static int fast_sweep_bps(int m, int w, int stages)
 {
     const size_t sm = fast_sweep_smem(m, w, stages) + 1024;
@@ -1001,9 +1017,11 @@ static int fast_sweep_regs()
 {
     static const int regs = [] {
         cudaFuncAttributes fa;
-        const int r = cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4>) == cudaSuccess
-                          ? std::max(fa.numRegs, 32)
-                          : 168;
+        const int rb = fast_sweep_rb();
+        const cudaError_t e = rb == 2   ? cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4, 2>)
+                              : rb == 3 ? cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4, 3>)
+                                        : cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4, 1>);
+        const int r = e == cudaSuccess ? std::max(fa.numRegs, 32) : 168;
         cudaGetLastError();
         return r;
     }();
@@ -1062,12 +1080,22 @@ void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int
     verify(smem <= 227 * 1024, "too many basis functions for the fast hinge sweep");
     const int nc = m + 3;
     const int mid = fast_sweep_mid(head, tail, n);
-#define LAUNCH_FS(CPL, S)                                                                      \
+#define LAUNCH_FS_RB(CPL, S, RB)                                                               \
     do {                                                                                       \
-        allow_smem(k_fast_sweep<CPL, S>, smem);                                                \
-        k_fast_sweep<CPL, S><<<ntasks, 32 * (warps + 2), smem, st>>>(                          \
+        allow_smem(k_fast_sweep<CPL, S, RB>, smem);                                            \
+        k_fast_sweep<CPL, S, RB><<<ntasks, 32 * (warps + 2), smem, st>>>(                      \
             reinterpret_cast<const FastTask *>(tasks), perm, xsort, ysort, cols, BoR, ldbo,    \
             ybo, ybx, mom, n, m, head, tail, mid, min_span, tol, cut_rel, hsse, hrow, hflag);  \
+    } while (0)
+#define LAUNCH_FS(CPL, S)               \
+    do {                                \
+        if (fast_sweep_rb() == 2) {     \
+            LAUNCH_FS_RB(CPL, S, 2);    \
+        } else if (fast_sweep_rb() == 3) { \
+            LAUNCH_FS_RB(CPL, S, 3);    \
+        } else {                        \
+            LAUNCH_FS_RB(CPL, S, 1);    \
+        }                               \
     } while (0)
 #define LAUNCH_FS_CPL(CPL)      \
     do {                        \
@@ -1090,6 +1118,7 @@ void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int
     }
 #undef LAUNCH_FS_CPL
 #undef LAUNCH_FS
+#undef LAUNCH_FS_RB
     LAUNCH_CHECK();
     *launches += 1;
 }

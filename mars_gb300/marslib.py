@@ -50,6 +50,7 @@ class Stats(ctypes.Structure):
         ("leftovers", ctypes.c_longlong),
         ("leftovers_flagged", ctypes.c_longlong),
         ("evals_exact", ctypes.c_longlong),
+        ("redecided_degenerate", ctypes.c_longlong),
     ]
 
     def as_dict(self):
