@@ -87,7 +87,62 @@ def build(verbose=False, extra=()):
         out = subprocess.run(cmd, capture_output=True, text=True)
         if out.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), out.stderr))
+    build_marslib(verbose)
     return LIB
+
+
+PYBIND_SRC = os.path.join(HERE, "pybind", "marslib.cpp")
+
+
+def pybind_include():
+    """Directory holding pybind11/pybind11.h: the pybind11 package, else the
+    copy PyTorch ships with its C++ headers; None when neither is there."""
+    try:
+        import pybind11
+
+        return pybind11.get_include()
+    except ImportError:
+        pass
+    import importlib.util
+
+    spec = importlib.util.find_spec("torch")
+    if spec and spec.submodule_search_locations:
+        inc = os.path.join(list(spec.submodule_search_locations)[0], "include")
+        if os.path.isfile(os.path.join(inc, "pybind11", "pybind11.h")):
+            return inc
+    return None
+
+
+def marslib_path():
+    import sysconfig
+
+    return os.path.join(LIB_DIR, "marslib" + sysconfig.get_config_var("EXT_SUFFIX"))
+
+
+def build_marslib(verbose=False):
+    """The compiled `marslib` module (mars_gb300/pybind/marslib.cpp) beside
+    libmars_gpu.so, linked to it; skipped (returns None) without pybind11
+    headers."""
+    import sysconfig
+
+    inc = pybind_include()
+    if inc is None:
+        if verbose:
+            sys.stderr.write("pybind11 headers not found: compiled marslib skipped\n")
+        return None
+    out_path = marslib_path()
+    deps = [PYBIND_SRC, LIB, os.path.join(ROOT, "include", "mars_gpu.h")]
+    if os.path.isfile(out_path) and all(os.path.getmtime(out_path) >= os.path.getmtime(d)
+                                        for d in deps):
+        return out_path
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared",
+           "-fvisibility=hidden", "-I" + os.path.join(ROOT, "include"), "-I" + inc,
+           "-I" + sysconfig.get_paths()["include"], PYBIND_SRC, "-o", out_path,
+           "-L" + LIB_DIR, "-lmars_gpu", "-Wl,-rpath,$ORIGIN"]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("marslib build failed:\n%s\n%s" % (" ".join(cmd), out.stderr))
+    return out_path
 
 
 if __name__ == "__main__":

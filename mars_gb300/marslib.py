@@ -230,6 +230,25 @@ class MarsAlgo:
         return mx.value, rss.value
 
 
+def compiled():
+    """The compiled `marslib` extension (mars_gb300/pybind/marslib.cpp), the
+    reference's pybind11 module over this library's C ABI. Raises if it was
+    not built (no pybind11 headers at build time)."""
+    import importlib.machinery
+    import importlib.util
+    import sysconfig
+
+    path = os.path.join(_HERE, "lib", "marslib" + sysconfig.get_config_var("EXT_SUFFIX"))
+    if not os.path.isfile(path):
+        raise RuntimeError("the compiled marslib is not built: %s" % path)
+    load()  # libmars_gpu.so first, from this directory
+    loader = importlib.machinery.ExtensionFileLoader("marslib", path)
+    spec = importlib.util.spec_from_loader("marslib", loader)
+    mod = importlib.util.module_from_spec(spec)
+    loader.exec_module(mod)
+    return mod
+
+
 def device_count():
     return load().mars_gpu_device_count()
 
