@@ -807,9 +807,7 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
     std::vector<ExactResult> sp_res;
     std::exception_ptr sp_err;
     SpecJoin sp_join;
-    // The exact evaluation of the candidates in sp_j on the speculative lane
-    // (its own streams and scratch), from a host thread.
-    auto start_spec = [&] {
+    if (!sp_j.empty()) {
         std::vector<int> sx(sp_j.size()), sb(sp_j.size());
         for (size_t q = 0; q < sp_j.size(); ++q) {
             sx[q] = cx[sp_j[q]];
@@ -827,18 +825,7 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
                 sp_err = std::current_exception();
             }
         });
-    };
-    if (!sp_j.empty()) {
-        start_spec();
     }
-    // Early exact lane (MARS_GPU_MIXED_EARLY, default 1): the candidates whose
-    // projected column is nearly in the span of the basis are re-decided
-    // whatever the sweep finds, and they are known once the fast projection
-    // is done; their exact evaluation (with its DGKS pass, the longest exact
-    // path) starts then, beside the fast sweep, instead of after it.
-    const bool early = sp_j.empty() && !linear_only && !rank_only && blocks.size() == 1 &&
-                       env_double("MARS_GPU_MIXED_EARLY", 1.0) != 0.0;
-    const double degen_rel = env_double("MARS_GPU_MIXED_DEGEN_REL", 1e-6);
 
     std::vector<double> fybx(P), fh(P, 0.0), fh2(2 * (size_t)P, 0.0), fs(P), fmom(3 * (size_t)P);
     std::vector<int> frow(P, -1), frow2(2 * (size_t)P, -1), fflag(2 * (size_t)P, 0);
@@ -867,18 +854,6 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
                          &a->stats.kernel_launches);
         }
         a->timer.end(PH_PROJECT, t0);
-        if (early) {
-            CUDA_CHECK(cudaMemcpyAsync(fs.data() + c0, a->svec.ptr, sizeof(double) * Pc,
-                                       cudaMemcpyDeviceToHost, a->st));
-            CUDA_CHECK(cudaMemcpyAsync(fmom.data() + 3 * (size_t)c0, a->fmom.ptr,
-                                       sizeof(double) * 3 * Pc, cudaMemcpyDeviceToHost, a->st));
-            sync(a);
-            for (int j = c0; j < c0 + Pc; ++j) {
-                if (fs[j] < degen_rel * fmom[3 * (size_t)j + 2]) {
-                    sp_j.push_back(j);
-                }
-            }
-        }
         if (!linear_only) {
             t0 = a->timer.begin();
             std::vector<FastTaskRec> tasks;
@@ -920,9 +895,6 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
                        &a->stats.kernel_launches);
             a->timer.end(PH_SWEEP, t0);
             a->stats.knot_evals += (long long)Pc * sweep_grid_rows(head, tail, min_span);
-            if (early && !sp_j.empty()) {
-                start_spec();  // the sweep is queued: the exact lane runs beside it
-            }
             CUDA_CHECK(cudaMemcpyAsync(fh2.data() + 2 * (size_t)c0, a->hsse.ptr,
                                        sizeof(double) * 2 * Pc, cudaMemcpyDeviceToHost, a->st));
             CUDA_CHECK(cudaMemcpyAsync(frow2.data() + 2 * (size_t)c0, a->hrow.ptr,
