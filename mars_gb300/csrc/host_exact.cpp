@@ -37,12 +37,13 @@ constexpr double kDgksRatioSq = 9.0;  // kernels.h:17
 // columns, and appends while another append holds the pool, run in order on
 // the calling thread.
 //
-// The serial FP64 chains (the dot products and norms) stay in order unless
-// MARS_GPU_HOST_XCHAIN=1, which runs them chunked with the exact speculation of
-// xchain.cuh (guesses from plain FP64 partial sums, XC_RUNS + 1 speculative runs
-// per chunk of ~2,048 rows, an in-order walk). On the host the speculative runs'
-// bookkeeping costs ~3x a plain chain step per row, so the chunked form gains
-// little over eight x86 cores. Either way the results are the same bit for bit.
+// The serial FP64 chains (the dot products and norms) of those appends run
+// chunked with the exact speculation of xchain.cuh (guesses from plain FP64
+// partial sums, XC_RUNS + 1 speculative runs per chunk of ~2,048 rows, an
+// in-order walk) unless MARS_GPU_HOST_XCHAIN=0. On the 16 Grace cores of a
+// GB300 machine that halves an append of 10^6 rows (41 -> 20 ms at 13 basis
+// columns, 111 -> 53 ms at 50); on eight x86 cores it gained 5 %. Either way
+// the results are the same bit for bit.
 // ---------------------------------------------------------------------------
 
 // A process-wide pool of host threads. The caller takes part as worker 0; idle
@@ -149,7 +150,7 @@ size_t host_par_rows()
 bool host_xchain()
 {
     const char *v = std::getenv("MARS_GPU_HOST_XCHAIN");
-    return v && *v == '1';
+    return !(v && *v == '0');
 }
 
 // Runs the append's loops in order (pool == nullptr) or over the pool.
