@@ -84,11 +84,6 @@ typedef struct {
     double ms_redecide_gpu;     /* mixed mode: device time of re-decisions run on the GPU */
     long long redecided_flagged; /* mixed mode: candidates re-decided for a flag (degenerate
                                     column or unresolvable cut), whatever their rank */
-    long long speculated;       /* mixed mode: candidates evaluated exactly beside the fast
-                                   pass (the previous contenders, the new columns' candidates) */
-    long long redecided_spec;   /* mixed mode: re-decided candidates the speculation covered */
-    long long leftovers;        /* mixed mode: candidates evaluated exactly after the fast pass */
-    long long leftovers_flagged; /* ... of which carried a flag */
     long long evals_exact;      /* mixed mode: evals run on the exact path after a step that
                                    re-decided most of its candidates */
     long long redecided_degenerate; /* mixed mode: flagged candidates whose projected column

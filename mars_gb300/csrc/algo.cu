@@ -9,6 +9,7 @@
 #include "fp64.cuh"
 #include "host_exact.h"
 #include "tc.cuh"
+#include "xappend.cuh"
 
 #include <algorithm>
 #include <cfloat>
@@ -118,9 +119,7 @@ struct PhaseTimer {
     }
 };
 
-// The streams, counters and scratch one FP64 evaluation runs on: the handle's
-// own, or the speculative re-decision's (SpecLane), which runs beside the fast
-// pass of the mixed mode.
+// The streams, counters and scratch one FP64 evaluation runs on (the handle's).
 struct Fp64Ctx {
     cudaStream_t st, st2, st3;
     cudaEvent_t ev_fork, ev_join, ev_s, ev_ybx;
@@ -161,34 +160,6 @@ struct Fp64Streams {
     }
 };
 
-struct SpecLane {
-    Fp64Streams ss;
-    PhaseTimer timer;
-    double phase_ms[PH_N] = {0};
-    mars_gpu_stats stats{};
-    DevBuf Bx, T, svec, snew, ybx, hsse, hrow, fired, nfired, tasks, stasks, scal, bsort, bxsort,
-        cand, part;
-    void init()
-    {
-        if (!ss.st) {
-            ss.create();
-            timer.st = ss.st;
-            timer.redirect = PH_REDECIDE_GPU;
-            for (DevBuf *b : {&Bx, &T, &svec, &snew, &ybx, &hsse, &hrow, &fired, &nfired, &tasks,
-                              &stasks, &scal, &bsort, &bxsort, &cand, &part}) {
-                b->bind(ss.st);
-            }
-        }
-    }
-    Fp64Ctx ctx()
-    {
-        return {ss.st,  ss.st2, ss.st3, ss.ev_fork, ss.ev_join, ss.ev_s, ss.ev_ybx,
-                &timer, &stats, &Bx,    &T,         &svec,      &snew,   &ybx,
-                &hsse,  &hrow,  &fired, &nfired,    &tasks,     &stasks, &scal,
-                &bsort, &bxsort, &cand, &part};
-    }
-};
-
 }  // namespace
 
 struct mars_gpu_algo {
@@ -209,9 +180,9 @@ struct mars_gpu_algo {
 
     // Host copy of the basis, kept in the reference's exact arithmetic.
     HostBasis hb;
+    XaBufs xa;  // the exact append's buffers
     // Resident state.
     DevBuf X, s, y, B, Bo, BoF, BoC, ybo_d, perm, xsort, ysort;
-    std::vector<int32_t> perm_h;  // host copy of the sorted permutations (exact re-decision)
     std::vector<char> sorted;
     // Per-eval scratch (grow-only).
     DevBuf Bx, T, svec, snew, ybx, hsse, hrow, cand, fired, nfired, out, tasks, stasks, scal, part;
@@ -228,11 +199,6 @@ struct mars_gpu_algo {
     DevBuf BR, fNpart, fBxc;
     size_t ldbr = 0, br_cols = 0;
     DevBuf sort_keys, sort_vals, sort_tmp;
-    // Mixed mode: the exact re-decision speculated for the previous eval's
-    // contenders and for the columns appended since, beside the fast pass.
-    SpecLane spec;
-    std::vector<long long> prev_contend;  // sorted (xcol << 32 | bcol) keys
-    std::vector<long long> appended;      // (xcol << 32 | column) of appends since the last eval
     // Mixed mode: steps left to run on the exact path directly, after a step
     // that re-decided most of its candidates anyway.
     int mixed_skip = 0;
@@ -297,7 +263,8 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     verify(n < (size_t)INT32_MAX, "more rows than the GPU path supports (2^31 - 1)");
     // The weighted, normalised target, the intercept and the column scales in
     // the reference's arithmetic (marsalgo.cc:266-370), on the host.
-    a->hb.init(X, y, w, n, p, ldx, max_terms);
+    verify(max_terms >= 1, "max_terms must be >= 1");
+    a->hb.init(X, y, w, n, p, ldx);
     a->n = n;
     a->p = p;
     a->max_terms = max_terms;
@@ -305,7 +272,7 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     a->m = 1;
     a->tol = a->hb.tol;
     a->yvar = a->hb.yvar;
-    a->ybo = a->hb.ybo;
+    a->ybo.assign(1, a->hb.ybo0);
     std::memset(&a->stats, 0, sizeof(a->stats));
     a->ss.create();
     a->st = a->ss.st;
@@ -318,6 +285,7 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
                       &a->tcErr, &a->tcTab, &a->BR, &a->fNpart, &a->fBxc}) {
         b->bind(a->st);
     }
+    a->xa.bind(a->st);
     CUDA_CHECK(cudaEventCreate(&a->span_begin));
     CUDA_CHECK(cudaEventCreate(&a->span_end));
     a->timer.st = a->st;
@@ -343,9 +311,9 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     CUDA_CHECK(cudaMemsetAsync(a->Bo.ptr, 0, sizeof(double) * n * a->ldbo, a->st));
     a->BoF.ensure(sizeof(float) * n * a->ldbo);
     CUDA_CHECK(cudaMemsetAsync(a->BoF.ptr, 0, sizeof(float) * n * a->ldbo, a->st));
-    CUDA_CHECK(cudaMemcpyAsync(a->B.ptr, a->hb.B.data(), sizeof(float) * n,
+    CUDA_CHECK(cudaMemcpyAsync(a->B.ptr, a->hb.b0.data(), sizeof(float) * n,
                                cudaMemcpyHostToDevice, a->st));
-    CUDA_CHECK(cudaMemcpyAsync(a->BoC.ptr, a->hb.BoC.data(), sizeof(float) * n,
+    CUDA_CHECK(cudaMemcpyAsync(a->BoC.ptr, a->hb.b0.data(), sizeof(float) * n,
                                cudaMemcpyHostToDevice, a->st));
     k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(
         a->BoC.as<float>(), (int)n, a->Bo.as<double>(), a->BoF.as<float>(), a->ldbo, 0);
@@ -403,19 +371,6 @@ void ensure_sorted(mars_gpu_algo *a, const std::vector<int> &cols)
                  a->ysort.as<float>(), a->sort_keys, a->sort_vals, a->sort_tmp,
                  &a->stats.kernel_launches);
     a->timer.end(PH_SORT, t0);
-    if (a->precision == MARS_GPU_PREC_MIXED) {
-        // the host re-decision walks the same sorted order
-        if (a->perm_h.size() != np) {
-            a->perm_h.assign(np, 0);
-        }
-        for (int c : todo) {
-            CUDA_CHECK(cudaMemcpyAsync(a->perm_h.data() + (size_t)c * a->n,
-                                       a->perm.as<int>() + (size_t)c * a->n,
-                                       sizeof(int32_t) * a->n, cudaMemcpyDeviceToHost, a->st));
-            a->stats.d2h_bytes += (long long)(sizeof(int32_t) * a->n);
-        }
-        sync(a);
-    }
     for (int c : todo) {
         a->sorted[c] = 1;
     }
@@ -577,65 +532,6 @@ void eval_block_fp64(mars_gpu_algo *a, Fp64Ctx &c, int Pc, const int *cx_d, cons
     }
 }
 
-// The exact FP64 evaluation of the candidates sx/sb on the speculative lane
-// (its own streams and scratch); results to the host vectors.
-void run_spec(mars_gpu_algo *a, const std::vector<int> &sx, const std::vector<int> &sb,
-              int min_span, int head, int tail, std::vector<ExactResult> &out)
-{
-    SpecLane &L = a->spec;
-    Fp64Ctx c = L.ctx();
-    const int C = (int)sx.size();
-    const size_t n = a->n, m = a->m;
-    L.cand.ensure(sizeof(int) * 2 * (size_t)C);
-    L.Bx.ensure(sizeof(float) * n * C);
-    L.svec.ensure(sizeof(double) * C);
-    L.ybx.ensure(sizeof(double) * C);
-    L.hsse.ensure(sizeof(double) * C);
-    L.hrow.ensure(sizeof(int) * C);
-    L.bsort.ensure(sizeof(float) * n * C);
-    L.bxsort.ensure(sizeof(float) * n * C);
-    L.T.ensure(sizeof(double) * std::max<size_t>(1, m * C));
-    L.snew.ensure(sizeof(double) * C);
-    L.fired.ensure(sizeof(int) * C);
-    L.nfired.ensure(sizeof(int) * 4);
-    L.scal.ensure(sizeof(double) * 3 *
-                  std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
-    int *ecx = L.cand.as<int>(), *ecb = ecx + C;
-    const cudaStream_t st = L.ss.st;
-    CUDA_CHECK(cudaMemcpyAsync(ecx, sx.data(), sizeof(int) * C, cudaMemcpyHostToDevice, st));
-    CUDA_CHECK(cudaMemcpyAsync(ecb, sb.data(), sizeof(int) * C, cudaMemcpyHostToDevice, st));
-    L.stats.h2d_bytes += (long long)(sizeof(int) * 2 * (size_t)C);
-    eval_block_fp64(a, c, C, ecx, ecb, sx, 0, min_span, head, tail, false, false);
-    std::vector<double> ybx(C), hs(C);
-    std::vector<int> hr(C);
-    CUDA_CHECK(cudaMemcpyAsync(ybx.data(), L.ybx.ptr, sizeof(double) * C, cudaMemcpyDeviceToHost,
-                               st));
-    CUDA_CHECK(cudaMemcpyAsync(hs.data(), L.hsse.ptr, sizeof(double) * C, cudaMemcpyDeviceToHost,
-                               st));
-    CUDA_CHECK(cudaMemcpyAsync(hr.data(), L.hrow.ptr, sizeof(int) * C, cudaMemcpyDeviceToHost,
-                               st));
-    L.stats.d2h_bytes += (long long)(20 * (size_t)C);
-    CUDA_CHECK(cudaStreamSynchronize(st));
-    L.timer.resolve(L.phase_ms);
-    out.resize(C);
-    for (int q = 0; q < C; ++q) {
-        out[q].ybx = ybx[q];
-        out[q].hinge_sse = hs[q];
-        out[q].hinge_row = hr[q];
-        out[q].hinge_pos = hr[q] >= 0 ? 0 : -1;
-    }
-}
-
-// Joins the speculative evaluation on every exit path of eval_mixed.
-struct SpecJoin {
-    std::thread th;
-    ~SpecJoin()
-    {
-        if (th.joinable()) {
-            th.join();
-        }
-    }
-};
 
 // Whether the fast projection runs on the tensor cores (MARS_GPU_TC, default
 // 1; 0 selects the FP32 SIMT kernels).
@@ -776,56 +672,10 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
     CUDA_CHECK(cudaMemcpyAsync(cb_all, cb.data(), sizeof(int) * P, cudaMemcpyHostToDevice, a->st));
     a->stats.h2d_bytes += (long long)(sizeof(int) * 2 * (size_t)P);
 
-    // Speculative exact re-decision (MARS_GPU_MIXED_SPEC=1; off by default),
-    // beside the fast pass: the previous eval's contenders (an unresolvable cut
-    // or a degenerate column mostly stays so from one step to the next) and the
-    // candidates whose parent is a column appended since. Contenders it covers
-    // need no evaluation afterwards. It pays only when the contenders it misses
-    // are rare: each step that has any costs a full exact pass after the fast
-    // pass, and the concurrent FP64 kernels slow the fast pass down.
     // MARS_GPU_MIXED_RANK_ONLY=1: return the fast values as they are, with no
     // exact re-decision (to measure the fast pass's accuracy; not the
     // reference's decisions).
     const bool rank_only = env_double("MARS_GPU_MIXED_RANK_ONLY", 0.0) != 0.0;
-    std::vector<int> sp_j;
-    if (!linear_only && !rank_only && env_double("MARS_GPU_MIXED_SPEC", 0.0) != 0.0) {
-        for (int j = 0; j < P; ++j) {
-            const long long key = ((long long)cx[j] << 32) | (long long)(unsigned)cb[j];
-            if (std::binary_search(a->prev_contend.begin(), a->prev_contend.end(), key) ||
-                std::find(a->appended.begin(), a->appended.end(), key) != a->appended.end()) {
-                sp_j.push_back(j);
-            }
-        }
-        const double per_c = 12.0 * n + 24.0 * sweep_grid_rows(head, tail, min_span) + 64.0 * m;
-        const size_t spmax = (size_t)std::max(
-            0.0, std::min(env_double("MARS_GPU_MIXED_SPEC_MAX", 1024.0), budget / per_c));
-        if (sp_j.size() > spmax) {
-            sp_j.resize(spmax);
-        }
-    }
-    a->appended.clear();
-    std::vector<ExactResult> sp_res;
-    std::exception_ptr sp_err;
-    SpecJoin sp_join;
-    if (!sp_j.empty()) {
-        std::vector<int> sx(sp_j.size()), sb(sp_j.size());
-        for (size_t q = 0; q < sp_j.size(); ++q) {
-            sx[q] = cx[sp_j[q]];
-            sb[q] = cb[sp_j[q]];
-        }
-        int dev = 0;
-        CUDA_CHECK(cudaGetDevice(&dev));
-        a->spec.init();
-        a->stats.speculated += (long long)sp_j.size();
-        sp_join.th = std::thread([a, dev, sx, sb, min_span, head, tail, &sp_res, &sp_err] {
-            try {
-                CUDA_CHECK(cudaSetDevice(dev));
-                run_spec(a, sx, sb, min_span, head, tail, sp_res);
-            } catch (...) {
-                sp_err = std::current_exception();
-            }
-        });
-    }
 
     std::vector<double> fybx(P), fh(P, 0.0), fh2(2 * (size_t)P, 0.0), fs(P), fmom(3 * (size_t)P);
     std::vector<int> frow(P, -1), frow2(2 * (size_t)P, -1), fflag(2 * (size_t)P, 0);
@@ -986,93 +836,18 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
             }
         }
     }
-    {
-        std::vector<long long> keys;
-        for (int j = 0; j < P; ++j) {
-            if (contend[j]) {
-                keys.push_back(((long long)cx[j] << 32) | (long long)(unsigned)cb[j]);
-            }
-        }
-        std::sort(keys.begin(), keys.end());
-        a->prev_contend.swap(keys);
-    }
-
-    // the speculation's results
-    if (sp_join.th.joinable()) {
-        sp_join.th.join();
-    }
-    if (sp_err) {
-        std::rethrow_exception(sp_err);
-    }
-    std::vector<int> sp_of(P, -1);
-    for (size_t q = 0; q < sp_j.size(); ++q) {
-        sp_of[sp_j[q]] = (int)q;
-    }
-    // A ranked (not flagged) contender whose fast values are both below
-    // (1 - band) of the best exact values already known cannot be the first
-    // maximum: its exact value is within the band of its fast value (the
-    // premise of the band itself). Every speculated candidate is exact anyway.
-    if (!sp_j.empty()) {
-        double elb = -std::numeric_limits<double>::infinity(), ehb = elb;
-        for (const ExactResult &r : sp_res) {
-            const double l = r.ybx * r.ybx;
-            elb = std::max(elb, l);
-            if (r.hinge_pos >= 0) {
-                ehb = std::max(ehb, l + r.hinge_sse);
-            }
-        }
-        for (int j = 0; j < P; ++j) {
-            if (contend[j] == 1 && sp_of[j] < 0 && flin[j] < (1.0 - band) * elb &&
-                (linear_only || fhin[j] < (1.0 - band) * ehb)) {
-                contend[j] = 0;
-            }
-        }
-    }
-    std::vector<int> ex_j;
+    // the exact re-decision of the contenders: the FP64 GPU path over them
+    std::vector<int> ex_j, ex_x, ex_b;
     for (int j = 0; j < P; ++j) {
-        if (contend[j] || sp_of[j] >= 0) {
+        if (contend[j]) {
             ex_j.push_back(j);
+            ex_x.push_back(cx[j]);
+            ex_b.push_back(cb[j]);
         }
     }
-    if (!sp_j.empty()) {
-        SpecLane &L = a->spec;
-        a->stats.kernel_launches += L.stats.kernel_launches;
-        a->stats.h2d_bytes += L.stats.h2d_bytes;
-        a->stats.d2h_bytes += L.stats.d2h_bytes;
-        a->stats.dgks_fired += L.stats.dgks_fired;
-        L.stats = mars_gpu_stats{};
-        for (int ph = 0; ph < PH_N; ++ph) {
-            a->phase_ms[ph] += L.phase_ms[ph];
-            L.phase_ms[ph] = 0.0;
-        }
-    }
-    std::vector<ExactResult> ex(ex_j.size());
-    std::vector<int> lo_q, lo_x, lo_b;  // leftovers: contenders the speculation missed
-    std::vector<const int32_t *> lo_perm;
-    for (size_t q = 0; q < ex_j.size(); ++q) {
-        const int j = ex_j[q];
-        if (sp_of[j] >= 0) {
-            ex[q] = sp_res[sp_of[j]];
-            a->stats.redecided_spec += contend[j] ? 1 : 0;
-        } else {
-            lo_q.push_back((int)q);
-            a->stats.leftovers_flagged += contend[j] == 2 ? 1 : 0;
-            lo_x.push_back(cx[j]);
-            lo_b.push_back(cb[j]);
-            lo_perm.push_back(linear_only ? nullptr : a->perm_h.data() + (size_t)cx[j] * a->n);
-        }
-    }
-    std::vector<ExactResult> lo;
-    const int threads = usable_cores();
-    const int host_max = (int)env_double("MARS_GPU_MIXED_HOST_MAX", threads);
-    if ((int)lo_q.size() <= host_max) {
-        // few leftovers: the host cores, whose serial f64 chains are ~50x
-        // shorter in latency than the GPU's
-        exact_candidates(a->hb, lo_x, lo_b, lo_perm, min_span, head, tail, lo, threads);
-    } else {
-        // many: the FP64 GPU path over them (its time hardly depends on the
-        // candidate count)
-        const int C = (int)lo_q.size();
+    std::vector<ExactResult> ex;
+    if (!ex_j.empty()) {
+        const int C = (int)ex_j.size();
         a->cand.ensure(sizeof(int) * 2 * (size_t)C);
         a->Bx.ensure(sizeof(float) * a->n * C);
         a->svec.ensure(sizeof(double) * C);
@@ -1092,9 +867,9 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
                            std::max<size_t>(1, (size_t)C * sweep_grid_rows(head, tail, min_span)));
         }
         int *ecx = a->cand.as<int>(), *ecb = ecx + C;
-        CUDA_CHECK(cudaMemcpyAsync(ecx, lo_x.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
+        CUDA_CHECK(cudaMemcpyAsync(ecx, ex_x.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
                                    a->st));
-        CUDA_CHECK(cudaMemcpyAsync(ecb, lo_b.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
+        CUDA_CHECK(cudaMemcpyAsync(ecb, ex_b.data(), sizeof(int) * C, cudaMemcpyHostToDevice,
                                    a->st));
         a->stats.h2d_bytes += (long long)(sizeof(int) * 2 * (size_t)C);
         struct Redirect {
@@ -1103,7 +878,7 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         } guard{a->timer};
         a->timer.redirect = PH_REDECIDE_GPU;
         Fp64Ctx c = a->ctx();
-        eval_block_fp64(a, c, C, ecx, ecb, lo_x, 0, min_span, head, tail, linear_only, false);
+        eval_block_fp64(a, c, C, ecx, ecb, ex_x, 0, min_span, head, tail, linear_only, false);
         std::vector<double> eybx(C), ehs(C, 0.0);
         std::vector<int> ehr(C, -1);
         CUDA_CHECK(cudaMemcpyAsync(eybx.data(), a->ybx.ptr, sizeof(double) * C,
@@ -1116,21 +891,15 @@ void eval_mixed(mars_gpu_algo *a, const std::vector<int> &cx, const std::vector<
         }
         a->stats.d2h_bytes += (long long)(20 * (size_t)C);
         sync(a);
-        lo.resize(C);
+        ex.resize(C);
         for (int q = 0; q < C; ++q) {
-            lo[q].ybx = eybx[q];
-            lo[q].hinge_sse = ehs[q];
-            lo[q].hinge_row = ehr[q];
-            lo[q].hinge_pos = ehr[q] >= 0 ? 0 : -1;
+            ex[q].ybx = eybx[q];
+            ex[q].hinge_sse = ehs[q];
+            ex[q].hinge_row = ehr[q];
+            ex[q].hinge_pos = ehr[q] >= 0 ? 0 : -1;
         }
     }
-    for (size_t q = 0; q < lo_q.size(); ++q) {
-        ex[lo_q[q]] = lo[q];
-    }
-    for (int j : ex_j) {
-        a->stats.redecided += contend[j] ? 1 : 0;
-    }
-    a->stats.leftovers += (long long)lo_q.size();
+    a->stats.redecided += (long long)ex_j.size();
 
     // assemble: exact values for the contenders, fast values held below them for the rest
     double lbest = -std::numeric_limits<double>::infinity(), hbest = lbest;
@@ -1319,28 +1088,36 @@ double append_impl(mars_gpu_algo *a, char type, int xcol, int bcol, float h)
     verify(xcol >= 0 && (size_t)xcol < a->p, "invalid X column index");
     verify(type == 'l' || type == '+' || type == '-', "invalid basis type");
     const size_t n = a->n, m = a->m;
-    // The serial Gram-Schmidt of the reference, on the host (host_exact.h).
-    long dgks = 0;
-    const double mse = a->hb.append(type, xcol, bcol, h, &dgks);
-    a->stats.dgks_fired += dgks;
+    // The reference's Gram-Schmidt in its FP64 order, every chain exact and
+    // parallel on the GPU (xappend.cuh); the MSE test on the host.
     cudaEvent_t t0 = a->timer.begin();
-    CUDA_CHECK(cudaMemcpyAsync(a->B.as<float>() + m * n, a->hb.B.data() + m * n,
-                               sizeof(float) * n, cudaMemcpyHostToDevice, a->st));
-    a->stats.h2d_bytes += (long long)(sizeof(float) * n);
-    if (a->hb.m > m) {
-        CUDA_CHECK(cudaMemcpyAsync(a->BoC.as<float>() + m * n, a->hb.BoC.data() + m * n,
-                                   sizeof(float) * n, cudaMemcpyHostToDevice, a->st));
-        k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(
-            a->BoC.as<float>() + m * n, (int)n, a->Bo.as<double>(), a->BoF.as<float>(), a->ldbo,
-            (int)m);
-        LAUNCH_CHECK();
-        a->stats.kernel_launches += 1;
-        CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.as<double>() + m, &a->hb.ybo[m], sizeof(double),
-                                   cudaMemcpyHostToDevice, a->st));
-        a->stats.h2d_bytes += (long long)(sizeof(float) * n + sizeof(double));
-        a->appended.push_back(((long long)xcol << 32) | (long long)m);
-        a->m = a->hb.m;
-        a->ybo = a->hb.ybo;
+    const XaFit fit{(int)n, (int)m, (int)a->max_terms, a->X.as<float>(), n, a->s.as<float>(),
+                    a->y.as<float>(), a->B.as<float>(), a->BoC.as<float>(), a->tol};
+    const XaOutcome o = append_exact(a->st, fit, type, xcol, bcol, h, a->xa,
+                                     &a->stats.kernel_launches);
+    a->stats.dgks_fired += o.dgks ? 1 : 0;
+    a->stats.d2h_bytes += (long long)(sizeof(double) * (m + 4));
+    double mse = -1.0;
+    if (o.stored) {
+        // marsalgo.cc:859-870
+        double ybo_sq = o.ybo * o.ybo;
+        for (double e : a->ybo) {
+            ybo_sq = std::fma(e, e, ybo_sq);
+        }
+        const double r = (1. - ybo_sq) / (double)n;
+        if (r >= -a->tol) {
+            k_col_to_rows<<<(unsigned)ceil_div(n, 256), 256, 0, a->st>>>(
+                a->BoC.as<float>() + m * n, (int)n, a->Bo.as<double>(), a->BoF.as<float>(),
+                a->ldbo, (int)m);
+            LAUNCH_CHECK();
+            a->stats.kernel_launches += 1;
+            CUDA_CHECK(cudaMemcpyAsync(a->ybo_d.as<double>() + m, &o.ybo, sizeof(double),
+                                       cudaMemcpyHostToDevice, a->st));
+            a->stats.h2d_bytes += (long long)sizeof(double);
+            a->ybo.push_back(o.ybo);
+            a->m = m + 1;
+            mse = r < 0.0 ? 0.0 : r;
+        }
     }
     a->timer.end(PH_APPEND, t0);
     span_mark_end(a);
@@ -1634,39 +1411,26 @@ int mars_gpu_orthonormalize_col(size_t n, size_t m, double *v, const float *Bo, 
                 colmajor[j * n + i] = Bo[i * ldBo + j];
             }
         }
-        DevBuf dBoC, dv, dcoef, dscal;
+        DevBuf dBoC, dv;
         long long launches = 0;
         dBoC.ensure(sizeof(float) * colmajor.size());
         CUDA_CHECK(cudaMemcpyAsync(dBoC.ptr, colmajor.data(), sizeof(float) * colmajor.size(),
                                    cudaMemcpyHostToDevice, st));
         dv.ensure(sizeof(double) * n);
         CUDA_CHECK(cudaMemcpyAsync(dv.ptr, v, sizeof(double) * n, cudaMemcpyHostToDevice, st));
-        dcoef.ensure(sizeof(double) * (m + 1));
-        dscal.ensure(sizeof(double) * 8);
-        AppendScratch ws{dv.as<double>(), dcoef.as<double>(), dscal.as<double>()};
-        double scal[2];
-        mgs_pass(st, dBoC.as<float>(), (int)n, (int)m, ws, &launches);
-        CUDA_CHECK(cudaMemcpyAsync(scal, ws.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaStreamSynchronize(st));
-        double vn = scal[1];
-        if (vn > tol && vn * 9.0 < scal[0]) {
-            mgs_pass(st, dBoC.as<float>(), (int)n, (int)m, ws, &launches);
-            CUDA_CHECK(cudaMemcpyAsync(scal, ws.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-            CUDA_CHECK(cudaStreamSynchronize(st));
-            vn = scal[1];
-            if (dgks) {
+        double w = 0.0;
+        {
+            XaBufs xa;
+            bool fired = false;
+            w = orthonormalize_col_exact(st, (int)n, (int)m, dBoC.as<float>(), dv.as<double>(),
+                                         tol, xa, &launches, &fired);
+            if (dgks && fired) {
                 *dgks += 1;
             }
+            CUDA_CHECK(cudaMemcpyAsync(v, dv.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
         }
-        CUDA_CHECK(cudaMemcpyAsync(v, dv.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaStreamSynchronize(st));
         cudaStreamDestroy(st);
-        const double w = std::sqrt(vn);
-        if (w * w > tol) {
-            for (size_t i = 0; i < n; ++i) {
-                v[i] /= w;
-            }
-        }
         if (w_out) {
             *w_out = w;
         }

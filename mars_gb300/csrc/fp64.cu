@@ -1314,200 +1314,8 @@ __global__ void k_assemble(int P, const int *__restrict__ cx, const int *__restr
     }
 }
 
-// ---------------------------------------------------------------------------
-// Append: each block owns a contiguous row range; partial sums are reduced in
-// block order by every block that needs them (no atomics, deterministic).
-// ---------------------------------------------------------------------------
-constexpr int AP_THREADS = 256;
-
-
-// ---------------------------------------------------------------------------
-// Serial chains of the append, in the reference's row order
-// (kernels.cc:194-281, marsalgo.cc:829-861). One block: thread 0 runs the
-// fused-multiply-add chain out of shared memory while the other threads stage
-// the next chunk of rows and write the previous chunk's updated v back.
-// ---------------------------------------------------------------------------
-constexpr int SER_THREADS = 256, SER_CH = 1024;
-
-// Modified Gram-Schmidt pass j = 0..m: v <- v - c_{j-1} Bo[:, j-1] (fused),
-// then c_j = sum_i Bo[i,j] v[i] (j < m) or ||v||^2 (j == m), rows in order.
-// Leaves c_j in coef, sum_j c_j^2 in scal[0] and ||v||^2 in scal[1].
-__global__ void __launch_bounds__(SER_THREADS)
-    k_mgs_serial(const float *__restrict__ BoC, int n, int m, double *__restrict__ v,
-                 double *__restrict__ coef, double *__restrict__ scal)
-{
-    __shared__ double sv[2][SER_CH];
-    __shared__ float sp[2][SER_CH], sc[2][SER_CH];
-    __shared__ double s_coef;
-    const int t = threadIdx.x;
-    const int nch = (n + SER_CH - 1) / SER_CH;
-    double proj = 0.0;
-    for (int j = 0; j <= m; ++j) {
-        const float *prev = BoC + (size_t)(j > 0 ? j - 1 : 0) * n;
-        const float *cur = BoC + (size_t)(j < m ? j : 0) * n;
-        const double cprev = (j > 0) ? s_coef : 0.0;
-        auto load = [&](int ch, int b) {
-            const int base = ch * SER_CH, cnt = min(SER_CH, n - base);
-            for (int e = t - 1; e < cnt; e += SER_THREADS - 1) {
-                sv[b][e] = v[base + e];
-                sp[b][e] = prev[base + e];
-                sc[b][e] = cur[base + e];
-            }
-        };
-        auto store = [&](int ch, int b) {
-            const int base = ch * SER_CH, cnt = min(SER_CH, n - base);
-            for (int e = t - 1; e < cnt; e += SER_THREADS - 1) {
-                v[base + e] = sv[b][e];
-            }
-        };
-        if (t > 0) {
-            load(0, 0);
-        }
-        __syncthreads();
-        double acc = 0.0;
-        for (int ch = 0; ch < nch; ++ch) {
-            const int b = ch & 1;
-            if (t == 0) {
-                const int cnt = min(SER_CH, n - ch * SER_CH);
-                for (int e = 0; e < cnt; ++e) {
-                    double vi = sv[b][e];
-                    if (j > 0) {
-                        vi = fma(-cprev, (double)sp[b][e], vi);
-                        sv[b][e] = vi;
-                    }
-                    acc = (j < m) ? fma((double)sc[b][e], vi, acc) : fma(vi, vi, acc);
-                }
-            } else {
-                if (ch > 0 && j > 0) {
-                    store(ch - 1, b ^ 1);
-                }
-                if (ch + 1 < nch) {
-                    load(ch + 1, b ^ 1);
-                }
-            }
-            __syncthreads();
-        }
-        if (t > 0 && j > 0) {
-            store(nch - 1, (nch - 1) & 1);
-        }
-        if (t == 0) {
-            if (j < m) {
-                coef[j] = acc;
-                s_coef = acc;
-                proj = fma(acc, acc, proj);
-            } else {
-                scal[0] = proj;
-                scal[1] = acc;
-            }
-        }
-        __syncthreads();
-    }
-}
-
-// out = sum_i a_i b_i as one fused chain over the rows in order.
-struct VSq {  // (v, v)
-    const double *v;
-    __device__ __forceinline__ void operator()(int i, double &a, double &b) const
-    {
-        a = v[i];
-        b = v[i];
-    }
-};
-struct ColDotY {  // ((double)Q[i], (double)y[i])
-    const float *q;
-    const float *y;
-    __device__ __forceinline__ void operator()(int i, double &a, double &b) const
-    {
-        a = (double)q[i];
-        b = (double)y[i];
-    }
-};
-
-template <class Op>
-__global__ void __launch_bounds__(SER_THREADS)
-    k_serial_dot(Op op, int n, double *__restrict__ out)
-{
-    __shared__ double sa[2][SER_CH], sb[2][SER_CH];
-    const int t = threadIdx.x;
-    const int nch = (n + SER_CH - 1) / SER_CH;
-    auto load = [&](int ch, int b) {
-        const int base = ch * SER_CH, cnt = min(SER_CH, n - base);
-        for (int e = t - 1; e < cnt; e += SER_THREADS - 1) {
-            op(base + e, sa[b][e], sb[b][e]);
-        }
-    };
-    if (t > 0) {
-        load(0, 0);
-    }
-    __syncthreads();
-    double acc = 0.0;
-    for (int ch = 0; ch < nch; ++ch) {
-        const int b = ch & 1;
-        if (t == 0) {
-            const int cnt = min(SER_CH, n - ch * SER_CH);
-            for (int e = 0; e < cnt; ++e) {
-                acc = fma(sa[b][e], sb[b][e], acc);
-            }
-        } else if (ch + 1 < nch) {
-            load(ch + 1, b ^ 1);
-        }
-        __syncthreads();
-    }
-    if (t == 0) {
-        *out = acc;
-    }
-}
-
-__global__ void __launch_bounds__(AP_THREADS)
-    k_append_fill(char type, const float *__restrict__ X, size_t ldX, const float *__restrict__ s,
-                  int xcol, float *__restrict__ B, size_t ldB, int bcol, int m, float h, int n,
-                  double *__restrict__ v)
-{
-    const float sx = s[xcol];
-    for (int i = blockIdx.x * AP_THREADS + threadIdx.x; i < n; i += gridDim.x * AP_THREADS) {
-        const float xp = X[(size_t)i + (size_t)xcol * ldX];
-        const float bp = B[(size_t)i + (size_t)bcol * ldB];
-        float val;
-        if (type == 'l') {
-            val = sx * bp * xp;
-        } else {
-            const float t = (type == '+') ? xp - h : h - xp;
-            val = sx * bp * ((t < 0.0f) ? 0.0f : t);  // std::max(t, 0.0f)
-        }
-        B[(size_t)i + (size_t)m * ldB] = val;
-        v[i] = (double)val;
-    }
-}
-
-// B[:, m] /= f32(sqrt(raw2)) (marsalgo.cc:829-836).
-__global__ void __launch_bounds__(AP_THREADS)
-    k_append_scale(float *__restrict__ B, size_t ldB, int m, int n, const double *__restrict__ raw2)
-{
-    const float raw = (float)sqrt(*raw2);
-    for (int i = blockIdx.x * AP_THREADS + threadIdx.x; i < n; i += gridDim.x * AP_THREADS) {
-        B[(size_t)i + (size_t)m * ldB] /= raw;
-    }
-}
-
-// v /= w; column m of Bo (row-major) and BoC = f32(v) (kernels.cc:274-279,
-// marsalgo.cc:846-850).
-__global__ void __launch_bounds__(AP_THREADS)
-    k_append_store(double w, double *__restrict__ v, float *__restrict__ Bo, size_t ldbo,
-                   float *__restrict__ BoC, int n, int m)
-{
-    for (int i = blockIdx.x * AP_THREADS + threadIdx.x; i < n; i += gridDim.x * AP_THREADS) {
-        const double vi = v[i] / w;
-        v[i] = vi;
-        const float vf = (float)vi;
-        Bo[(size_t)i * ldbo + m] = vf;
-        BoC[(size_t)m * n + i] = vf;
-    }
-}
-
-
 }  // namespace
 
-int append_blocks(int n) { return (int)std::max<size_t>(1, std::min<size_t>(608, ceil_div(n, 2048))); }
 
 template <class Src, class BoT>
 void tgemm_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, int n, int m, int P,
@@ -1912,39 +1720,6 @@ void assemble_outputs(cudaStream_t st, int P, const int *cand_x, const int *cand
                                                          X, ldX, linear_only, lin, hin, cut);
     LAUNCH_CHECK();
     *launches += 1;
-}
-
-void append_fill(cudaStream_t st, char type, const float *X, size_t ldX, const float *s,
-                 int xcol, float *B, size_t ldB, int bcol, int m, float h, int n,
-                 const AppendScratch &ws, long long *launches)
-{
-    const int nb = append_blocks(n);
-    k_append_fill<<<nb, AP_THREADS, 0, st>>>(type, X, ldX, s, xcol, B, ldB, bcol, m, h, n, ws.v);
-    LAUNCH_CHECK();
-    k_serial_dot<VSq><<<1, SER_THREADS, 0, st>>>(VSq{ws.v}, n, ws.scal + 3);
-    LAUNCH_CHECK();
-    k_append_scale<<<nb, AP_THREADS, 0, st>>>(B, ldB, m, n, ws.scal + 3);
-    LAUNCH_CHECK();
-    *launches += 3;
-}
-
-void mgs_pass(cudaStream_t st, const float *BoC, int n, int m, const AppendScratch &ws,
-              long long *launches)
-{
-    k_mgs_serial<<<1, SER_THREADS, 0, st>>>(BoC, n, m, ws.v, ws.coef, ws.scal);
-    LAUNCH_CHECK();
-    *launches += 1;
-}
-
-void append_store(cudaStream_t st, double w, float *Bo, size_t ldbo, float *BoC, int n, int m,
-                  const float *y, const AppendScratch &ws, long long *launches)
-{
-    k_append_store<<<append_blocks(n), AP_THREADS, 0, st>>>(w, ws.v, Bo, ldbo, BoC, n, m);
-    LAUNCH_CHECK();
-    k_serial_dot<ColDotY><<<1, SER_THREADS, 0, st>>>(ColDotY{BoC + (size_t)m * n, y}, n,
-                                                     ws.scal + 2);
-    LAUNCH_CHECK();
-    *launches += 2;
 }
 
 // sum_i X[i,j]^2 per column as the reference's sequential fused chain

@@ -205,27 +205,6 @@ void assemble_outputs(cudaStream_t st, int P, const int *cand_x, const int *cand
 void fill_outputs(cudaStream_t st, int rows, int m, double *lin, double *hin, double *cut,
                   long long *launches);
 
-// --- append (marsalgo.cc:760-875 and kernels.cc:194-281) -------------------
-struct AppendScratch {
-    double *v;     // n
-    double *coef;  // max_terms
-    double *scal;  // result slots: 0 sum c^2, 1 ||v||^2, 2 ybo_m, 3 raw norm^2
-};
-int append_blocks(int n);
-// Bm = s * B[:,bcol] * f(X[:,xcol]) into B[:, m]; v = (double)Bm; then
-// Bm /= f32(sqrt(sum v^2)). type: 'l', '+', '-'.
-void append_fill(cudaStream_t st, char type, const float *X, size_t ldX, const float *s,
-                 int xcol, float *B, size_t ldB, int bcol, int m, float h, int n,
-                 const AppendScratch &ws, long long *launches);
-// One modified Gram-Schmidt pass of v against BoC[:, 0:m] (column-major, ld n),
-// every reduction one fused chain over the rows in order; leaves sum(c^2) in
-// scal[0] and ||v||^2 in scal[1].
-void mgs_pass(cudaStream_t st, const float *BoC, int n, int m, const AppendScratch &ws,
-              long long *launches);
-// v /= w; store f32(v) as column m of Bo (row-major) and BoC; ybo_m -> scal[2].
-void append_store(cudaStream_t st, double w, float *Bo, size_t ldbo, float *BoC, int n, int m,
-                  const float *y, const AppendScratch &ws, long long *launches);
-
 // Column sums of squares sum_i X[i,j]^2 in FP64 (for s = 1/rms).
 void column_sumsq(cudaStream_t st, const float *X, size_t ldX, int n, int p, double *out,
                   long long *launches);

@@ -99,16 +99,17 @@ struct XcChunk {
 };
 
 // Margin of one run. h0 is the high word of its start; [hmin, hmax] the range of
-// the high words of the values it produced (unsigned order: the order of
-// magnitudes for one sign); edge is set when one of those values had the 20
-// mantissa bits of its high word all zero or all one, i.e. lay within 2^(e-20) of
-// an edge of its binade [2^e, 2^(e+1)). Otherwise every value keeps 2^(e_lo - 20)
-// from the edges of its own binade (e_lo the lowest binade visited), and a shift
-// by d keeps each exact sum in the binade of the unshifted one when
-// |d| <= 2^(e_lo - 20) - 2 U, U = 2^(e_hi - 52) the largest ulp visited. The run
-// may end at most one binade above its start (U <= 2 ulps of the start), so that
-// the residue modulo 4 ulps makes d a multiple of 2 U. An empty run vouches for
-// any d.
+// the magnitude high words (sign bit cleared) of the values it produced; edge is
+// set when one of those values had the 20 mantissa bits of its high word all zero
+// or all one, i.e. lay within 2^(e-20) of an edge of its binade [2^e, 2^(e+1)) in
+// magnitude. Otherwise every value keeps 2^(e_lo - 20) from the edges of its own
+// binade (e_lo the lowest binade visited), zero included, and a shift by d keeps
+// each exact sum in the binade of the unshifted one -- same sign, same exponent --
+// when |d| <= 2^(e_lo - 20) - 2 U, U = 2^(e_hi - 52) the largest ulp visited. The
+// values may change sign: no shifted sum crosses zero, since every one keeps
+// farther than |d| from it. The run may end at most one binade above its start
+// (U <= 2 ulps of the start), so that the residue modulo 4 ulps makes d a
+// multiple of 2 U. An empty run vouches for any d.
 XC_HD double xc_margin(uint32_t h0, uint32_t hmin, uint32_t hmax, bool edge, bool empty)
 {
     if (empty) {
@@ -116,11 +117,11 @@ XC_HD double xc_margin(uint32_t h0, uint32_t hmin, uint32_t hmax, bool edge, boo
     }
     const uint32_t E0 = (h0 >> 20) & 0x7ffu, Elo = (hmin >> 20) & 0x7ffu,
                    Ehi = (hmax >> 20) & 0x7ffu;
-    if (edge || ((hmin ^ h0) >> 31) != 0u || ((hmax ^ h0) >> 31) != 0u || E0 < 64u ||
-        Elo < 64u || Ehi > 2045u || Ehi > E0 + 1u) {
+    if (edge || E0 < 64u || Elo < 64u || Ehi > 2045u || Ehi > E0 + 1u || Ehi < Elo) {
         return -1.0;
     }
-    return xc_words((Elo - 20u) << 20, 0u) - xc_words((Ehi - 51u) << 20, 0u);
+    const double m = xc_words((Elo - 20u) << 20, 0u) - xc_words((Ehi - 51u) << 20, 0u);
+    return m >= 0.0 ? m : -1.0;
 }
 
 // The XC_RUNS speculative runs of one chain through one chunk: begin() from the
@@ -150,7 +151,7 @@ XC_UNROLL
 XC_UNROLL
         for (int r = 0; r < XC_RUNS; ++r) {
             a[r] = fma(x, y, a[r]);
-            const uint32_t h = xc_hi(a[r]);
+            const uint32_t h = xc_hi(a[r]) & 0x7fffffffu;
             mn[r] = xc_umin(mn[r], h);
             mx[r] = xc_umax(mx[r], h);
             ed[r] |= (uint32_t)(((h + 1u) & 0xfffffu) < 2u);
@@ -266,3 +267,243 @@ struct XcGuess {
     }
     XC_HD double value() const { return (double)hi + (double)lo; }
 };
+
+// ---------------------------------------------------------------------------
+// Records of a range of rows, composed level by level
+//
+// A record states what the chain does over its rows. For an entry t in the
+// binade of `start` (same sign and exponent) whose last two mantissa bits are r,
+// with |t - (start + r ulps)| <= margin[r], the chain leaves the rows at
+// end[r] + (t - (start + r ulps)), exactly; from the entry +0 it leaves at
+// zero_end when zero_ok. An empty record (no rows) leaves every entry as it is.
+//
+// A chunk's record comes from its speculative runs (XcSpecR). Consecutive
+// records compose into one (xc_compose_lane): walk them from start + r ulps,
+// translating through each. The composite vouches for a shift D of its entry
+// (a multiple of 4 ulps of its start) when every record it walked vouches for
+// the walk's own offset there plus D -- then every value of the shifted chain
+// keeps the binade of the walked one -- and when no value of the walk lies more
+// than one binade above the composite's start, so that D is a multiple of twice
+// every ulp the shifted chain rounds to and every rounding, ties included, is
+// translated. hmax[r] carries that largest magnitude up the levels.
+// ---------------------------------------------------------------------------
+struct XcRec {
+    double start;
+    double end[XC_RUNS];
+    double margin[XC_RUNS];
+    double zero_end;
+    uint32_t hmax[XC_RUNS];  // largest magnitude high word visited from start + r ulps
+    int zero_ok;
+    int empty;
+};
+
+// The XC_RUNS residue runs of one chunk, and the run from +0 when asked for
+// (a chunk whose guessed entry is exactly 0).
+struct XcSpecR {
+    double a[XC_RUNS], z;
+    uint32_t mn[XC_RUNS], mx[XC_RUNS], ed[XC_RUNS];
+    uint32_t h0, l0;
+    bool zero;
+    XC_HD void begin(double guess, bool with_zero)
+    {
+        zero = with_zero;
+        z = 0.0;
+        h0 = xc_hi(guess);
+        l0 = xc_lo(guess) & ~(uint32_t)(XC_RUNS - 1);
+XC_UNROLL
+        for (int r = 0; r < XC_RUNS; ++r) {
+            a[r] = xc_words(h0, l0 | (uint32_t)r);
+            mn[r] = 0xffffffffu;
+            mx[r] = 0u;
+            ed[r] = 0u;
+        }
+    }
+    XC_HD void step(double x, double y)
+    {
+        if (zero) {
+            z = fma(x, y, z);
+        }
+XC_UNROLL
+        for (int r = 0; r < XC_RUNS; ++r) {
+            a[r] = fma(x, y, a[r]);
+            const uint32_t h = xc_hi(a[r]) & 0x7fffffffu;
+            mn[r] = xc_umin(mn[r], h);
+            mx[r] = xc_umax(mx[r], h);
+            ed[r] |= (uint32_t)(((h + 1u) & 0xfffffu) < 2u);
+        }
+    }
+    XC_HD void finish(XcRec &c, bool empty) const
+    {
+        c.start = xc_words(h0, l0);
+        c.zero_end = z;
+        c.zero_ok = (zero || empty) ? 1 : 0;
+        c.empty = empty ? 1 : 0;
+XC_UNROLL
+        for (int r = 0; r < XC_RUNS; ++r) {
+            c.end[r] = a[r];
+            c.margin[r] = xc_margin(h0, mn[r], mx[r], ed[r] != 0u, empty);
+            c.hmax[r] = xc_umax(h0 & 0x7fffffffu, mx[r]);
+        }
+    }
+};
+
+XC_HD bool xc_is_pzero(double t) { return xc_hi(t) == 0u && xc_lo(t) == 0u; }
+
+// What a shift D of a walk's entry may be: every value of the walk keeps its
+// binade under it while |D| <= M, and H is the largest magnitude high word the
+// walk visited; ok is cleared where some value lies too near an edge of its
+// binade (or zero) to allow any shift. A through() that cannot carry the walk
+// (its records out of reach) sets lost instead.
+struct XcTrack {
+    double M;
+    uint32_t H;
+    bool ok;
+    bool lost;  // a through() gave up: the walk's value is not the chain's
+    XC_HD void init(uint32_t h)
+    {
+        M = 1.0e300;
+        H = h & 0x7fffffffu;
+        ok = true;
+        lost = false;
+    }
+};
+
+// Extends a walk at t through record c, if c vouches for t.
+XC_HD bool xc_track(const XcRec &c, double &t, XcTrack &tr)
+{
+    if (c.empty) {
+        return true;
+    }
+    if (xc_is_pzero(t)) {
+        if (!c.zero_ok) {
+            return false;
+        }
+        t = c.zero_end;  // a walk from another entry that reached +0 has lost its margin already
+        return true;
+    }
+    const uint32_t hc = xc_hi(c.start);
+    if ((xc_hi(t) >> 20) != (hc >> 20)) {
+        return false;
+    }
+    const uint32_t r = xc_lo(t) & (uint32_t)(XC_RUNS - 1);
+    const double d = t - xc_words(hc, xc_lo(c.start) | r);  // exact: one binade
+    const double md = c.margin[r];
+    if (!(fabs(d) <= md)) {
+        return false;
+    }
+    tr.M = fmin(tr.M, md - fabs(d));  // exact: multiples of the start's ulp, < 2^33 of them
+    tr.H = xc_umax(tr.H, c.hmax[r]);
+    t = c.end[r] + d;  // exact: the shifted end keeps its binade
+    return true;
+}
+
+// Extends a walk at t through rows [i0, i1) run in order; term(i, x, y) yields
+// row i's two FP64 factors. The values are tracked like a run's: a shift by D
+// keeps every exact sum in its binade when |D| <= 2^(e_lo - 20) - 2 U.
+template <class Term>
+XC_HD void xc_run_track(const Term &term, int i0, int i1, double &t, XcTrack &tr)
+{
+    if (i1 <= i0) {
+        return;
+    }
+    uint32_t mn = 0xffffffffu, mx = 0u, ed = 0u;
+XC_UNROLL4
+    for (int i = i0; i < i1; ++i) {
+        double x, y;
+        term(i, x, y);
+        t = fma(x, y, t);
+        const uint32_t h = xc_hi(t) & 0x7fffffffu;
+        mn = xc_umin(mn, h);
+        mx = xc_umax(mx, h);
+        ed |= (uint32_t)(((h + 1u) & 0xfffffu) < 2u);
+    }
+    const uint32_t Elo = (mn >> 20) & 0x7ffu, Ehi = (mx >> 20) & 0x7ffu;
+    if (ed || Elo < 64u || Ehi > 2045u || Ehi < Elo) {
+        tr.ok = false;
+    } else {
+        const double m = xc_words((Elo - 20u) << 20, 0u) - xc_words((Ehi - 51u) << 20, 0u);
+        if (m >= 0.0) {
+            tr.M = fmin(tr.M, m);
+        } else {
+            tr.ok = false;
+        }
+    }
+    tr.H = xc_umax(tr.H, mx);
+}
+
+// The walk at t through the consecutive records rec(0 .. K-1); where a record
+// cannot vouch for the walk's value, through(k, t, tr) carries the walk across
+// that record's rows another way (its sub-records, or the rows in order) and
+// tracks it. The walk ends at the true chain value unless a through() gave up.
+template <class RecAt, class Through>
+XC_HD double xc_walk(const RecAt &rec, int K, double t, XcTrack &tr, const Through &through)
+{
+    for (int k = 0; k < K; ++k) {
+        if (!xc_track(rec(k), t, tr)) {
+            through(k, t, tr);
+        }
+    }
+    return t;
+}
+
+// One lane of the composition of the consecutive records rec(0 .. K-1): lane
+// r < XC_RUNS walks from start + r ulps and fills end[r], margin[r], hmax[r];
+// lane XC_RUNS walks from +0 (when the start is +0) and fills zero_end and
+// zero_ok; lane 0 also sets
+// start and empty. The lanes write disjoint fields of `out`. A walked value is
+// the true chain from its entry (through() re-runs what no record vouches for,
+// or gives up, and the lane's result is then marked invalid); the composite
+// vouches for a shift D of the entry when every value kept its binade under it
+// and no value lay more than one binade above the start.
+template <class RecAt, class Through>
+XC_HD void xc_compose_lane(const RecAt &rec, int K, int lane, const Through &through, XcRec &out)
+{
+    int k0 = 0;
+    while (k0 < K && rec(k0).empty) {
+        ++k0;
+    }
+    if (k0 == K) {  // no rows at all
+        if (lane == 0) {
+            out.start = 0.0;
+            out.empty = 1;
+        }
+        if (lane < XC_RUNS) {
+            out.end[lane] = 0.0;
+            out.margin[lane] = 1.0e300;
+            out.hmax[lane] = 0u;
+        } else {
+            out.zero_end = 0.0;
+            out.zero_ok = 1;
+        }
+        return;
+    }
+    const double S = rec(k0).start;
+    const uint32_t hs = xc_hi(S);
+    if (lane == 0) {
+        out.start = S;
+        out.empty = 0;
+    }
+    const uint32_t Es = (hs >> 20) & 0x7ffu;
+    XcTrack tr;
+    tr.init(hs);
+    if (lane >= XC_RUNS) {
+        // Only a composite guessed to start at exactly 0 (every term before it
+        // summed to 0) is likely to be entered at +0; other ones are descended
+        // into when that happens.
+        const bool z = xc_is_pzero(S);
+        out.zero_end = z ? xc_walk(rec, K, 0.0, tr, through) : 0.0;
+        out.zero_ok = (z && !tr.lost) ? 1 : 0;
+        return;
+    }
+    if (Es < 64u) {  // a start this small vouches for no shift
+        out.end[lane] = S;
+        out.hmax[lane] = hs & 0x7fffffffu;
+        out.margin[lane] = -1.0;
+        return;
+    }
+    const double t = xc_walk(rec, K, xc_words(hs, xc_lo(S) | (uint32_t)lane), tr, through);
+    const uint32_t Eh = (tr.H >> 20) & 0x7ffu;
+    out.end[lane] = t;
+    out.hmax[lane] = tr.H;
+    out.margin[lane] = (tr.ok && !tr.lost && Eh <= Es + 1u) ? tr.M : -1.0;
+}

@@ -45,10 +45,6 @@ class Stats(ctypes.Structure):
         ("ms_gather", ctypes.c_double),
         ("ms_redecide_gpu", ctypes.c_double),
         ("redecided_flagged", ctypes.c_longlong),
-        ("speculated", ctypes.c_longlong),
-        ("redecided_spec", ctypes.c_longlong),
-        ("leftovers", ctypes.c_longlong),
-        ("leftovers_flagged", ctypes.c_longlong),
         ("evals_exact", ctypes.c_longlong),
         ("redecided_degenerate", ctypes.c_longlong),
     ]

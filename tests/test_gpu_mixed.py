@@ -98,19 +98,6 @@ def test_mixed_matches_fp64_on_a_fit_with_default_tail(gpu):
     assert stats["mixed"]["redecided"] < stats["mixed"]["candidates"] // 2
 
 
-@pytest.mark.parametrize("name", ["hinge_search_small", "precision_stress_small", "default_tail",
-                                  "batched_small_1"])
-def test_mixed_with_speculation_keeps_golden_path(name, gpu, monkeypatch):
-    """MARS_GPU_MIXED_SPEC=1: the previous contenders are evaluated exactly
-    beside the fast pass; the term path must not change."""
-    monkeypatch.setenv("MARS_GPU_PRECISION", "mixed")
-    monkeypatch.setenv("MARS_GPU_MIXED_SPEC", "1")
-    g = load_fit(name)
-    X, y, w, kw = cases.fit_case(name)
-    model = mars.fit(X, y, w, **kw)
-    assert_same_path(model, g)
-
-
 def test_rank_only_values_track_fp64(gpu, monkeypatch):
     """MARS_GPU_MIXED_RANK_ONLY=1 returns the fast values as they are (NaN cut
     where a candidate is flagged). Unflagged candidates within half of the best

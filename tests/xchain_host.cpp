@@ -3,6 +3,7 @@
 // chunk layout and phase order, against the recurrences run in order.
 #include "../mars_gb300/csrc/xhinge.cuh"
 
+#include <functional>
 #include <type_traits>
 #include <vector>
 
@@ -15,9 +16,126 @@ struct Term {
         y = b[i];
     }
 };
+// Terms with a double second factor (the append's Gram-Schmidt chains: an f32
+// basis value times the f64 working column).
+struct TermD {
+    const float *a;
+    const double *b;
+};
+
+double run_d(const TermD &t, int i0, int i1, double acc)
+{
+    for (int i = i0; i < i1; ++i) {
+        acc = fma((double)t.a[i], t.b[i], acc);
+    }
+    return acc;
+}
 }  // namespace
 
 extern "C" {
+
+double xc_host_sequential_d(const float *a, const double *b, int n)
+{
+    return run_d(TermD{a, b}, 0, n, 0.0);
+}
+
+// The composed form: K chunk records (XcSpecR) composed level by level with the
+// fan-outs fan[0 .. nlev-1] (xc_compose_lane, one call per lane), then the top
+// level walked from 0 with descents into the sub-records where a record cannot
+// vouch for its entry, and the rows of a chunk re-run in order at the bottom.
+// guess_mode as in xc_host_chunked. *redone counts the chunks the final walk
+// re-ran, *descents the composite records it could not take as they are;
+// built[0..1] the same counts while the levels were composed.
+double xc_host_composed(const float *a, const double *b, int n, int K, const int *fan, int nlev,
+                        int guess_mode, double scale, int *redone, int *descents, int *built)
+{
+    const TermD term{a, b};
+    const int L = n > 0 ? (n + K - 1) / K : 0;
+    auto lo = [&](int c) { return c * L < n ? c * L : n; };
+    auto hi = [&](int c) { return lo(c) + L < n ? lo(c) + L : n; };
+    std::vector<double> sums(K);
+    for (int c = 0; c < K; ++c) {
+        XcGuess g;
+        for (int i = lo(c); i < hi(c); ++i) {
+            const float vh = (float)b[i];
+            g.add_scaled(a[i], vh, (float)(b[i] - (double)vh));
+        }
+        sums[c] = g.value();
+    }
+    std::vector<std::vector<XcRec>> lev(1, std::vector<XcRec>(K));
+    lev.reserve(nlev + 1);
+    double pre = 0.0, tru = 0.0;
+    for (int c = 0; c < K; ++c) {
+        double guess = pre;
+        if (guess_mode == 1) {
+            guess = pre * (1.0 + scale);
+        } else if (guess_mode == 2) {
+            const uint32_t E = (xc_hi(tru) >> 20) & 0x7ffu;
+            const double u = E > 52u ? xc_words((E - 52u) << 20, 0u) : 0.0;
+            guess = tru + scale * u;
+        } else if (guess_mode == 3) {
+            guess = scale;
+        }
+        XcSpecR sp;
+        sp.begin(guess, guess == 0.0);
+        for (int i = lo(c); i < hi(c); ++i) {
+            sp.step((double)a[i], b[i]);
+        }
+        sp.finish(lev[0][c], hi(c) <= lo(c));
+        pre += sums[c];
+        tru = run_d(term, lo(c), hi(c), tru);
+    }
+    int nre = 0, nde = 0;
+    // through(l, k, t, tr): across record k of level l another way
+    std::function<void(int, int, double &, XcTrack &)> through = [&](int l, int k, double &t,
+                                                                     XcTrack &tr) {
+        if (l == 0) {
+            ++nre;
+            xc_run_track([&](int i, double &x, double &y) {
+                x = (double)a[i];
+                y = b[i];
+            }, lo(k), hi(k), t, tr);
+            return;
+        }
+        ++nde;
+        const int F = fan[l - 1], c0 = k * F, sz = (int)lev[l - 1].size();
+        t = xc_walk([&](int q) -> const XcRec & { return lev[l - 1][c0 + q]; },
+                    sz - c0 < F ? sz - c0 : F, t, tr,
+                    [&](int q, double &v, XcTrack &tq) { through(l - 1, c0 + q, v, tq); });
+    };
+    for (int l = 0; l < nlev; ++l) {
+        const std::vector<XcRec> &sub = lev.back();
+        const int F = fan[l], G = ((int)sub.size() + F - 1) / F;
+        std::vector<XcRec> up(G);
+        for (int g = 0; g < G; ++g) {
+            const int c0 = g * F, cnt = (int)sub.size() - c0 < F ? (int)sub.size() - c0 : F;
+            for (int lane = 0; lane <= XC_RUNS; ++lane) {
+                xc_compose_lane([&](int k) -> const XcRec & { return sub[c0 + k]; }, cnt, lane,
+                                [&](int k, double &v, XcTrack &tq) { through(l, c0 + k, v, tq); },
+                                up[g]);
+            }
+        }
+        lev.push_back(up);
+    }
+    const int built_re = nre, built_de = nde;
+    nre = nde = 0;
+    XcTrack tr;
+    tr.init(0u);
+    const double t = xc_walk([&](int k) -> const XcRec & { return lev[nlev][k]; },
+                             (int)lev[nlev].size(), 0.0, tr,
+                             [&](int k, double &v, XcTrack &tq) { through(nlev, k, v, tq); });
+    if (built) {
+        built[0] = built_re;
+        built[1] = built_de;
+    }
+    if (redone) {
+        *redone = nre;
+    }
+    if (descents) {
+        *descents = nde;
+    }
+    return t;
+}
 
 // The recurrence as written.
 double xc_host_sequential(const float *a, const float *b, int n)
