@@ -443,7 +443,8 @@ void eval_block_fp64(mars_gpu_algo *a, Fp64Ctx &c, int Pc, const int *cx_d, cons
     }
     cudaEvent_t t0 = c.timer->begin();
     FillSrc src{a->B.as<float>(), a->n, a->X.as<float>(), a->n, a->s.as<float>(), cx_d, cb_d};
-    project_fp64(c.st, src, a->Bo.as<double>(), a->ldbo, n, m, Pc, nullptr, Bx, a->n, s, ws,
+    project_fp64(c.st, src, a->Bo.as<double>(), a->ldbo, a->BoC.as<float>(), &a->xa, n, m, Pc,
+                 nullptr, Bx, a->n, s, ws,
                  &c.stats->kernel_launches);
     c.timer->end(PH_PROJECT, t0);
 
@@ -455,7 +456,8 @@ void eval_block_fp64(mars_gpu_algo *a, Fp64Ctx &c, int Pc, const int *cx_d, cons
     CUDA_CHECK(cudaStreamSynchronize(c.st));
     if (nf > 0) {
         StoredSrc src2{Bx, a->n, c.fired->as<int>()};
-        project_fp64(c.st, src2, a->Bo.as<double>(), a->ldbo, n, m, nf, c.fired->as<int>(), Bx,
+        project_fp64(c.st, src2, a->Bo.as<double>(), a->ldbo, a->BoC.as<float>(), &a->xa, n, m,
+                     nf, c.fired->as<int>(), Bx,
                      a->n, c.snew->as<double>(), ws, &c.stats->kernel_launches);
         scatter_s(c.st, c.fired->as<int>(), nf, c.snew->as<double>(), s,
                   &c.stats->kernel_launches);
@@ -1367,7 +1369,8 @@ int mars_gpu_orthonormalize(size_t n, size_t m, size_t p, const float *B, size_t
         ProjectScratch ws{dT.as<double>()};
         FillSrc src{dB.as<float>(), n, dx.as<float>(), n, dsx.as<float>(), dcand.as<int>(),
                     dcand.as<int>() + p};
-        project_fp64(st, src, dBo.as<float>(), ldbo, (int)n, (int)m, (int)p, nullptr,
+        project_fp64(st, src, dBo.as<float>(), ldbo, nullptr, nullptr, (int)n, (int)m, (int)p,
+                     nullptr,
                      dBx.as<float>(), n, ds.as<double>(), ws, &launches);
         dgks_gate(st, dT.as<double>(), (int)m, (int)p, ds.as<double>(), tol, dfired.as<int>(),
                   dnf.as<int>(), &launches);
@@ -1376,7 +1379,8 @@ int mars_gpu_orthonormalize(size_t n, size_t m, size_t p, const float *B, size_t
         CUDA_CHECK(cudaStreamSynchronize(st));
         if (nf > 0) {
             StoredSrc s2{dBx.as<float>(), n, dfired.as<int>()};
-            project_fp64(st, s2, dBo.as<float>(), ldbo, (int)n, (int)m, nf, dfired.as<int>(),
+            project_fp64(st, s2, dBo.as<float>(), ldbo, nullptr, nullptr, (int)n, (int)m, nf,
+                         dfired.as<int>(),
                          dBx.as<float>(), n, dsn.as<double>(), ws, &launches);
             scatter_s(st, dfired.as<int>(), nf, dsn.as<double>(), ds.as<double>(), &launches);
         }

@@ -284,17 +284,15 @@ __global__ void __launch_bounds__(CC_THREADS) k_colchain(Op op, int n, int P, do
 // chain k_colchain runs, bit for bit.
 constexpr int XC_MAXK = 512;
 
+// The terms of column chain j of a chain op (column(j) through value(), and
+// ycolumn() or the value again).
 template <class Op>
-__global__ void __launch_bounds__(XC_MAXK) k_xchain(Op op, int n, int L, double *__restrict__ out)
-{
-    __shared__ XcChunk ch[XC_MAXK];
-    __shared__ double wsum[XC_MAXK / 32];
-    const int j = blockIdx.x, t = threadIdx.x, K = blockDim.x;
-    const int lane = t & 31, warp = t >> 5, nw = K >> 5;
-    const float *col = op.column(j);
-    const float *yc = op.ycolumn();
-    const float prm = op.param(j);
-    const auto term = [&](int i, float &a, float &b) {
+struct ColTerms {
+    const float *col, *yc;
+    float prm;
+    Op op;
+    __device__ __forceinline__ void operator()(int i, float &a, float &b) const
+    {
         const float v = op.value(__ldg(col + i), prm);
         a = v;
         if constexpr (Op::kUsesY) {
@@ -302,7 +300,26 @@ __global__ void __launch_bounds__(XC_MAXK) k_xchain(Op op, int n, int L, double 
         } else {
             b = v;
         }
-    };
+    }
+};
+template <class Op>
+struct ColChains {
+    Op op;
+    __device__ __forceinline__ ColTerms<Op> chain(int j) const
+    {
+        return {op.column(j), op.ycolumn(), op.param(j), op};
+    }
+};
+
+template <class Chains>
+__global__ void __launch_bounds__(XC_MAXK) k_xchain(Chains chains, int n, int L,
+                                                    double *__restrict__ out)
+{
+    __shared__ XcChunk ch[XC_MAXK];
+    __shared__ double wsum[XC_MAXK / 32];
+    const int j = blockIdx.x, t = threadIdx.x, K = blockDim.x;
+    const int lane = t & 31, warp = t >> 5, nw = K >> 5;
+    const auto term = chains.chain(j);
     const int i0 = (int)min((long long)n, (long long)t * L), i1 = min(n, i0 + L);
 
     XcGuess g;
@@ -1359,13 +1376,14 @@ TG_INST(StoredSrc, float)
 TG_INST(StoredSrc, double)
 #undef TG_INST
 
-// Chunks per chain for k_xchain, or 0 where k_colchain is the faster form.
-// Costs in SM cycles over the GPU: a chain as written takes ~70 cycles a row;
-// FP64 throughput is ~2 FMAs per cycle per SM; k_xchain issues XC_RUNS + 1 FMAs
-// per element (the runs from the guess and from zero) and its walk takes ~450
-// cycles a chunk. MARS_GPU_XCHAIN = 0 or 1
-// forces either kernel.
-int xchain_chunks(int n, int P)
+// Chunks per chain for k_xchain, or 0 where the chains as written (k_colchain,
+// k_tgemm) are the faster form. Costs in SM cycles over the GPU: a chain as
+// written takes plain_step cycles a row (~70 for a column chain, ~86 for a T
+// chain with its operand load); FP64 throughput is ~2 FMAs per cycle per SM;
+// k_xchain issues XC_RUNS + 1 FMAs per element (the runs from the guess and
+// from zero) and its walk takes ~450 cycles a chunk. MARS_GPU_XCHAIN = 0 or 1
+// forces either form.
+int xchain_chunks(int n, int P, double plain_step)
 {
     const char *fv = std::getenv("MARS_GPU_XCHAIN");
     const int force = fv && *fv ? std::atoi(fv) : -1;
@@ -1381,7 +1399,7 @@ int xchain_chunks(int n, int P)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     }
     const double fp64 = 2.0 * std::max(1, sms);
-    const double plain = std::max(70.0 * n, (double)P * n / fp64);
+    const double plain = std::max(plain_step * n, (double)P * n / fp64);
     const double chunked = (XC_RUNS + 1.0) * P * n / fp64 + 450.0 * K;
     return chunked < 0.7 * plain ? K : 0;
 }
@@ -1392,9 +1410,10 @@ void colchain(cudaStream_t st, const Op &op, int n, int P, double *out, long lon
     if (P <= 0) {
         return;
     }
-    const int K = xchain_chunks(n, P);
+    const int K = xchain_chunks(n, P, 70.0);
     if (K > 0) {
-        k_xchain<Op><<<(unsigned)P, (unsigned)K, 0, st>>>(op, n, (int)ceil_div(n, K), out);
+        k_xchain<ColChains<Op>><<<(unsigned)P, (unsigned)K, 0, st>>>(ColChains<Op>{op}, n,
+                                                                    (int)ceil_div(n, K), out);
     } else {
         k_colchain<Op><<<(unsigned)ceil_div(P, CC_COLS), CC_THREADS, 0, st>>>(op, n, P, out);
     }
@@ -1403,14 +1422,27 @@ void colchain(cudaStream_t st, const Op &op, int n, int P, double *out, long lon
 }
 
 template <class Src, class BoT>
-void project_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, int n, int m, int P,
-                  const int *out_col, float *Bx, size_t ldBx, double *s_out,
-                  const ProjectScratch &ws, long long *launches)
+void project_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, const float *BoC,
+                  XaBufs *xa, int n, int m, int P, const int *out_col, float *Bx, size_t ldBx,
+                  double *s_out, const ProjectScratch &ws, long long *launches)
 {
     if (P <= 0) {
         return;
     }
-    tgemm_fp64(st, src, Bo, ldbo, n, m, P, ws.T, launches);
+    // A chain as written costs ~86 cycles a row whatever the number of chains.
+    // The exact parallel form reads both columns of every chain (no reuse
+    // across chains) with strided per-thread rows: measured at 10^6 rows, 1,012
+    // chains take 39 ms against 57 ms as written and 1,472 take 56 ms, so it
+    // is taken up to 1,200 chains.
+    bool done = false;
+    if constexpr (std::is_same<Src, StoredSrc>::value) {
+        if (BoC && xa && m > 0 && n >= 65536 && (long long)P * m <= 1200) {
+            done = tgemm_exact(st, n, m, P, BoC, src.Bx, src.ldBx, src.col, ws.T, *xa, launches);
+        }
+    }
+    if (!done) {
+        tgemm_fp64(st, src, Bo, ldbo, n, m, P, ws.T, launches);
+    }
     const int rb = (int)ceil_div(n, PJ_THREADS);
     const size_t smem = sizeof(double) * PJ_COLS * std::max(m, 1);
     if (smem > 48 * 1024) {
@@ -1425,9 +1457,10 @@ void project_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, i
 }
 
 #define PJ_INST(SRC, BOT)                                                                      \
-    template void project_fp64<SRC, BOT>(cudaStream_t, const SRC &, const BOT *, size_t, int,   \
-                                         int, int, const int *, float *, size_t, double *,      \
-                                         const ProjectScratch &, long long *);
+    template void project_fp64<SRC, BOT>(cudaStream_t, const SRC &, const BOT *, size_t,       \
+                                         const float *, XaBufs *, int, int, int, const int *,   \
+                                         float *, size_t, double *, const ProjectScratch &,     \
+                                         long long *);
 PJ_INST(FillSrc, float)
 PJ_INST(FillSrc, double)
 PJ_INST(StoredSrc, float)

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "xappend.cuh"
 
 namespace mgpu {
 
@@ -111,10 +112,14 @@ struct ProjectScratch {
 };
 
 // Bo may be stored as f64 (the fit state) or f32 (the kernel-level entry points).
+// BoC and xa, when given, are the same basis as f32 columns (column stride n)
+// and scratch: with few entries (P m, a DGKS re-pass over stored columns) T is
+// then formed by the exact parallel chains of tgemm_exact (xappend.cuh), which
+// give the values of the chains run in order.
 template <class Src, class BoT>
-void project_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, int n, int m,
-                  int P, const int *out_col, float *Bx, size_t ldBx, double *s_out,
-                  const ProjectScratch &ws, long long *launches);
+void project_fp64(cudaStream_t st, const Src &src, const BoT *Bo, size_t ldbo, const float *BoC,
+                  XaBufs *xa, int n, int m, int P, const int *out_col, float *Bx, size_t ldBx,
+                  double *s_out, const ProjectScratch &ws, long long *launches);
 
 // T[j][c] = sum_i Bo[i,c] * src(i, j) only, each entry one fused chain over
 // the rows in order (the reference's accumulation order).

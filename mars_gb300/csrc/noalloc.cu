@@ -93,7 +93,8 @@ int mars_gpu_orthonormalize_noalloc(size_t n, size_t m, size_t p, const float *B
         const size_t ldbo = m == 0 ? 1 : ldBo;
         ProjectScratch ws{T};
         FillSrc src{B, ldB, x, n, one, cand_x, cand_b};
-        project_fp64(st, src, Bo, ldbo, (int)n, (int)m, (int)p, nullptr, Bx, ldBx, sv, ws,
+        project_fp64(st, src, Bo, ldbo, nullptr, nullptr, (int)n, (int)m, (int)p, nullptr, Bx, ldBx,
+                     sv, ws,
                      &launches);
         dgks_gate(st, T, (int)m, (int)p, sv, tol, fired, nfired, &launches);
         int nf = 0;
@@ -101,7 +102,8 @@ int mars_gpu_orthonormalize_noalloc(size_t n, size_t m, size_t p, const float *B
         CUDA_CHECK(cudaStreamSynchronize(st));
         if (nf > 0) {
             StoredSrc s2{Bx, ldBx, fired};
-            project_fp64(st, s2, Bo, ldbo, (int)n, (int)m, nf, fired, Bx, ldBx, snew, ws,
+            project_fp64(st, s2, Bo, ldbo, nullptr, nullptr, (int)n, (int)m, nf, fired, Bx, ldBx,
+                         snew, ws,
                          &launches);
             scatter_s(st, fired, nf, snew, sv, &launches);
         }

@@ -39,6 +39,8 @@ constexpr int XA_GRP = 16;            // blocks per group of the final walk
 constexpr int XA_MAXG = XA_T;         // blocks per launch at most (their records fit in s_rc)
 constexpr int XA_LMIN = 16;           // rows per chunk at least, below XA_MAXG blocks
 constexpr int XA_TILE = 8;            // rows whose loads a thread issues together
+constexpr long long XA_MAX_CHAINS = 65535;  // side-by-side chains per launch (grid y)
+constexpr size_t XA_REC_BUDGET = 1ull << 30;  // bytes of records for side-by-side chains
 constexpr int XA_LANES = XC_RUNS + 1;
 
 // result slots
@@ -52,6 +54,7 @@ enum : int {  // aggregates of the next chain's terms, as polynomials a0 + a1 c 
     XN_QY,      // (stored f32 column) y
     XN_QV_UPD,  // q_next (v - c q):  a0 = q_next v, a1 = -q_next q
     XN_SQ_UPD,  // (v - c q)^2:       a0 = v v, a1 = -2 v q, a2 = q q
+    XN_AB,      // q y: the terms of this launch's own XA_QY chains (their guesses)
 };
 
 struct XaArgs {
@@ -85,6 +88,13 @@ struct XaArgs {
     const float *q_next;
     const double *g_in;  // this chain's block entry guesses
     double *g_out;       // the next chain's
+    // Independent chains side by side, blockIdx.y = chain c (one chain: c = 0):
+    // its q column q + (c % qk) qld, its y column y + ycol[c / qk] yld (ycol
+    // null: c / qk), and its records, aggregates, guesses, ticket and result
+    // (res[res_slot + c]) at per-chain offsets.
+    int qk;
+    size_t qld, yld;
+    const int *ycol;
     // scratch
     double *res;
     XcRec *rc, *rs, *rw, *rb;
@@ -93,19 +103,8 @@ struct XaArgs {
 };
 
 // GB300 runs conversions to and from f64 on its narrow FP64 pipe, which the
-// chains' fused multiply-adds already keep busy; these two build the values
-// from their bit fields on the integer pipe instead.
-// The f64 value of an f32 (exact; subnormal floats, which the fits do not
-// produce, take the FP64 conversion).
-__device__ __forceinline__ double f2d(float f)
-{
-    const uint32_t b = __float_as_uint(f), e = (b >> 23) & 0xffu, mant = b & 0x7fffffu;
-    if (e == 0u && mant != 0u) {
-        return (double)f;
-    }
-    const uint32_t de = e == 0u ? 0u : (e == 0xffu ? 0x7ffu : e + 896u);
-    return __hiloint2double((int)((b & 0x80000000u) | (de << 20) | (mant >> 3)), (int)(mant << 29));
-}
+// chains' fused multiply-adds already keep busy: xc_f2d (xchain.cuh) and this
+// build the values from their bit fields on the integer pipe instead.
 
 // An approximate float-float split of an f64 (for guesses only): h its
 // leading 24 significant bits, l most of the rest; 0 where the value is
@@ -135,12 +134,12 @@ struct XaTerm {
     __device__ __forceinline__ void operator()(int i, double &a, double &b) const
     {
         if (kind == XA_QY) {
-            a = f2d(q[i]);
-            b = f2d(y[i]);
+            a = xc_f2d(q[i]);
+            b = xc_f2d(y[i]);
             return;
         }
         const double vi = cg ? __ldcg(v + i) : v[i];
-        a = kind == XA_SQ ? vi : f2d(q[i]);
+        a = kind == XA_SQ ? vi : xc_f2d(q[i]);
         b = vi;
     }
 };
@@ -204,7 +203,18 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
     __shared__ int s_last, s_ok;
 
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5, b = blockIdx.x, G = gridDim.x;
-    const int n = A.n, L = A.L;
+    const int n = A.n, L = A.L, ch = blockIdx.y;
+    const float *const Aq = A.q ? A.q + (size_t)(ch % A.qk) * A.qld : nullptr;
+    const float *const Ay =
+        A.y ? A.y + (size_t)(A.ycol ? A.ycol[ch / A.qk] : ch / A.qk) * A.yld : nullptr;
+    XcRec *const Arc = A.rc + (size_t)ch * G * XA_T;
+    XcRec *const Ars = A.rs + (size_t)ch * G * XA_NS;
+    XcRec *const Arw = A.rw + (size_t)ch * G * XA_NW;
+    XcRec *const Arb = A.rb + (size_t)ch * G;
+    double *const Aagg = A.agg + (size_t)ch * 3 * G;
+    const double *const Ag_in = A.g_in + (size_t)ch * G;
+    double *const Ag_out = A.g_out + (size_t)ch * G;
+    unsigned *const Aticket = A.ticket + ch;
     auto rows_lo = [&](int gt) { return (int)min((long long)n, (long long)gt * L); };
     auto rows_hi = [&](int gt) { return (int)min((long long)n, (long long)gt * L + L); };
     const int gt = b * XA_T + t, i0 = rows_lo(gt), i1 = rows_hi(gt);
@@ -220,8 +230,8 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
     const float *Xc = A.X + (size_t)A.xcol * A.ldX;
     XcGuess gs, g0, g1, g2;
     const bool need_q = chain && A.kind != XA_SQ;  // this chain's column (QV, QY)
-    const bool need_y = A.kind == XA_QY || A.next == XN_QY;
-    const bool need_qc = need_q || A.next == XN_QV_UPD || A.next == XN_SQ_UPD;
+    const bool need_y = A.kind == XA_QY || A.next == XN_QY || A.next == XN_AB;
+    const bool need_qc = need_q || A.next == XN_QV_UPD || A.next == XN_SQ_UPD || A.next == XN_AB;
     // Tiles of XA_TILE rows: every load of a tile is issued before its rows are
     // used (the rows of a thread are consecutive, so a warp's loads are strided).
     for (int base = i0; base < i1; base += XA_TILE) {
@@ -244,13 +254,13 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
                 qp[u] = A.q_prev[i];
             }
             if (need_qc) {
-                qc[u] = A.q[i];
+                qc[u] = Aq[i];
             }
             if (A.next == XN_QV || A.next == XN_QV_UPD) {
                 qn[u] = A.q_next[i];
             }
             if (need_y) {
-                ys[u] = A.y[i];
+                ys[u] = Ay[i];
             }
         }
 #pragma unroll
@@ -269,12 +279,12 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
                     val = sx * bs[u] * ((d < 0.0f) ? 0.0f : d);  // std::max(d, 0.0f)
                 }
                 Bm[i] = val;
-                v = f2d(val);
+                v = xc_f2d(val);
             } else if (A.scale) {
                 Bm[i] = bm[u] / raw;
             }
             if (A.upd) {
-                v = fma(-cprev, f2d(qp[u]), v);
+                v = fma(-cprev, xc_f2d(qp[u]), v);
             }
             float qo = 0.0f;
             if (A.norm) {
@@ -308,6 +318,9 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
             case XN_QY:
                 g0.add_product(qo, ys[u]);
                 break;
+            case XN_AB:
+                g0.add_product(qc[u], ys[u]);
+                break;
             case XN_QV_UPD:
                 g0.add_scaled(qn[u], vh, vl);
                 g1.add_product(-qn[u], qc[u]);
@@ -338,7 +351,7 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
         for (int q = 0; q < XA_NW; ++q) {
             r += s_agg[t][q];
         }
-        A.agg[(size_t)b * 3 + t] = r;
+        Aagg[(size_t)b * 3 + t] = r;
     }
 
     // 2. chunk guesses and speculative runs
@@ -346,8 +359,8 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
     if (chain) {
         double total;
         const double ex = block_excl(gs.value(), s_sh, total);
-        const double guess = A.g_in[b] + ex;
-        const XaTerm tm{A.kind, A.q, A.y, vsrc, false};
+        const double guess = Ag_in[b] + ex;
+        const XaTerm tm{A.kind, Aq, Ay, vsrc, false};
         XcSpecR sp;
         sp.begin(guess, guess == 0.0);
         for (int base = i0; base < i1; base += XA_TILE) {
@@ -364,11 +377,11 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
             }
         }
         sp.finish(s_rc[t], i1 <= i0);
-        A.rc[gt] = s_rc[t];
+        Arc[gt] = s_rc[t];
         __syncthreads();
 
         // 3. composition: sub-groups, warps, the block
-        const XaTerm tl{A.kind, A.q, A.y, vsrc, false};
+        const XaTerm tl{A.kind, Aq, Ay, vsrc, false};
         auto rerun_local = [&](int c, double &v, XcTrack &tr) {  // chunk c of this block
             xc_run_track(tl, rows_lo(b * XA_T + c), rows_hi(b * XA_T + c), v, tr);
         };
@@ -404,11 +417,11 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
         }
         __syncthreads();
         if (t < XA_NS) {
-            A.rs[(size_t)b * XA_NS + t] = s_rs[t];
+            Ars[(size_t)b * XA_NS + t] = s_rs[t];
         } else if (t < XA_NS + XA_NW) {
-            A.rw[(size_t)b * XA_NW + t - XA_NS] = s_rw[t - XA_NS];
+            Arw[(size_t)b * XA_NW + t - XA_NS] = s_rw[t - XA_NS];
         } else if (t == XA_NS + XA_NW) {
-            A.rb[b] = s_rb;
+            Arb[b] = s_rb;
         }
     }
 
@@ -416,7 +429,7 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
     __threadfence();
     __syncthreads();
     if (t == 0) {
-        s_last = atomicAdd(A.ticket, 1u) == (unsigned)G - 1u;
+        s_last = atomicAdd(Aticket, 1u) == (unsigned)G - 1u;
     }
     __syncthreads();
     if (!s_last) {
@@ -425,7 +438,7 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
     __threadfence();
     double c = 0.0;
     if (chain) {
-        const XaTerm tg{A.kind, A.q, A.y, vsrc, true};
+        const XaTerm tg{A.kind, Aq, Ay, vsrc, true};
         const int ngrp = (G + XA_GRP - 1) / XA_GRP;
         // the blocks' records into shared memory (this block's chunk records are done with)
         auto copy_recs = [&](XcRec *dst, const XcRec *src, int count) {
@@ -435,7 +448,7 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
                 dp[k] = __ldcg(sp + k);
             }
         };
-        copy_recs(s_rc, A.rb, G);
+        copy_recs(s_rc, Arb, G);
         __syncthreads();
         // groups of XA_GRP blocks; a lane meeting a block that cannot vouch for
         // its value gives up (the final walk descends there instead)
@@ -479,9 +492,9 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
                 if (step(s_rc[bk])) {
                     continue;
                 }
-                copy_recs(d_rw, A.rw + (size_t)bk * XA_NW, XA_NW);
-                copy_recs(d_rs, A.rs + (size_t)bk * XA_NS, XA_NS);
-                copy_recs(d_rc, A.rc + (size_t)bk * XA_T, XA_T);
+                copy_recs(d_rw, Arw + (size_t)bk * XA_NW, XA_NW);
+                copy_recs(d_rs, Ars + (size_t)bk * XA_NS, XA_NS);
+                copy_recs(d_rc, Arc + (size_t)bk * XA_T, XA_T);
                 __syncthreads();
                 if (t == 0) {
                     XcTrack tr;
@@ -506,7 +519,7 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
         }
         c = s_t;
         if (t == 0) {
-            A.res[A.res_slot] = c;
+            A.res[A.res_slot + ch] = c;
         }
     }
     if (A.next != XN_NONE) {
@@ -517,20 +530,20 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
             const int k = base + t;
             double a = 0.0;
             if (k < G) {
-                const double a0 = __ldcg(A.agg + (size_t)k * 3), a1 = __ldcg(A.agg + (size_t)k * 3 + 1),
-                             a2 = __ldcg(A.agg + (size_t)k * 3 + 2);
+                const double a0 = __ldcg(Aagg + (size_t)k * 3), a1 = __ldcg(Aagg + (size_t)k * 3 + 1),
+                             a2 = __ldcg(Aagg + (size_t)k * 3 + 2);
                 a = a0 + c * (a1 + c * a2);
             }
             double total;
             const double ex = block_excl(a, s_sh, total);
             if (k < G) {
-                A.g_out[k] = carry + ex;
+                Ag_out[k] = carry + ex;
             }
             carry += total;
         }
     }
     if (t == 0) {
-        *A.ticket = 0u;  // for the next launch (stream order)
+        *Aticket = 0u;  // for the next launch (stream order)
     }
 }
 
@@ -598,6 +611,7 @@ struct XaRun {
         XaArgs a{};
         a.n = n;
         a.L = L;
+        a.qk = 1;
         a.mcol = m;
         a.res = res;
         a.rc = bf.rc.as<XcRec>();
@@ -795,6 +809,69 @@ double orthonormalize_col_exact(cudaStream_t st, int n, int m, const float *BoC,
     CUDA_CHECK(cudaMemcpyAsync(v, run.vb[run.cur], sizeof(double) * n, cudaMemcpyDeviceToDevice,
                                st));
     return w;
+}
+
+// T = Bo^T Bx for few candidates (kernels.cc:327-335): the chain of entry
+// q = j m + k is sum_i BoC[i, k] Bx[i, col(j)], rows in order, for all of them
+// side by side (blockIdx.y), each evaluated exactly in parallel. Two launches:
+// the blocks' sums of the terms (entry guesses), then the chains.
+bool tgemm_exact(cudaStream_t st, int n, int m, int P, const float *BoC, const float *Bx,
+                 size_t ldBx, const int *col, double *T, XaBufs &bf, long long *launches)
+{
+    const long long chains = (long long)P * m;
+    if (n <= 0 || chains <= 0 || chains > XA_MAX_CHAINS) {
+        return false;
+    }
+    // blocks per chain: at least 16 rows a chunk; records of all chains
+    // within XA_REC_BUDGET bytes
+    const size_t per_block = sizeof(XcRec) * (XA_T + XA_NS + XA_NW + 1);
+    const long long gmax =
+        std::max<long long>(1, (long long)(XA_REC_BUDGET / ((size_t)chains * per_block)));
+    const int G = (int)std::max<long long>(1, std::min<long long>(xa_blocks(n), gmax));
+    const int L = (int)ceil_div((size_t)n, (size_t)G * XA_T);
+    const size_t cg = (size_t)chains * G;
+    bf.rc.ensure(sizeof(XcRec) * cg * XA_T);
+    bf.rs.ensure(sizeof(XcRec) * cg * XA_NS);
+    bf.rw.ensure(sizeof(XcRec) * cg * XA_NW);
+    bf.rb.ensure(sizeof(XcRec) * cg);
+    bf.agg.ensure(sizeof(double) * 3 * cg);
+    bf.g0.ensure(sizeof(double) * cg);
+    bf.g1.ensure(sizeof(double) * cg);
+    if (bf.ticket.bytes < sizeof(unsigned) * (size_t)chains) {
+        bf.ticket.ensure(sizeof(unsigned) * (size_t)chains);
+        CUDA_CHECK(cudaMemsetAsync(bf.ticket.ptr, 0, bf.ticket.bytes, st));
+    }
+    XaArgs a{};
+    a.n = n;
+    a.L = L;
+    a.q = BoC;
+    a.qk = m;
+    a.qld = (size_t)n;
+    a.y = Bx;
+    a.yld = ldBx;
+    a.ycol = col;
+    a.res = T;
+    a.rc = bf.rc.as<XcRec>();
+    a.rs = bf.rs.as<XcRec>();
+    a.rw = bf.rw.as<XcRec>();
+    a.rb = bf.rb.as<XcRec>();
+    a.agg = bf.agg.as<double>();
+    a.ticket = bf.ticket.as<unsigned>();
+    const dim3 grid((unsigned)G, (unsigned)chains);
+    allow_smem(k_xappend, xa_smem_bytes());
+    a.next = XN_AB;  // the guesses
+    a.g_out = bf.g0.as<double>();
+    k_xappend<<<grid, XA_T, xa_smem_bytes(), st>>>(a);
+    LAUNCH_CHECK();
+    a.next = XN_NONE;  // the chains
+    a.kind = XA_QY;
+    a.res_slot = 0;
+    a.g_in = bf.g0.as<double>();
+    a.g_out = bf.g1.as<double>();
+    k_xappend<<<grid, XA_T, xa_smem_bytes(), st>>>(a);
+    LAUNCH_CHECK();
+    *launches += 2;
+    return true;
 }
 
 }  // namespace mgpu

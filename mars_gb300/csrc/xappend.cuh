@@ -56,4 +56,13 @@ XaOutcome append_exact(cudaStream_t st, const XaFit &fit, char type, int xcol, i
 double orthonormalize_col_exact(cudaStream_t st, int n, int m, const float *BoC, double *v,
                                 double tol, XaBufs &bufs, long long *launches, bool *dgks);
 
+// T[j m + k] = sum_i BoC[i, k] * Bx[i, col(j)] (col null: j) for P candidates
+// and m basis columns, every entry the reference's chain over the rows in order
+// (kernels.cc:327-335) evaluated exactly in parallel, all entries side by side.
+// Pays where the entries are few (a DGKS re-pass): the chains as written take
+// n dependent FMA latencies whatever their number. Returns false (nothing
+// launched) when there are more than 65535 entries.
+bool tgemm_exact(cudaStream_t st, int n, int m, int P, const float *BoC, const float *Bx,
+                 size_t ldBx, const int *col, double *T, XaBufs &bufs, long long *launches);
+
 }  // namespace mgpu

@@ -85,6 +85,24 @@ XC_HD double xc_words(uint32_t hi, uint32_t lo)
 #endif
 }
 
+// The f64 value of an f32, exactly. On the device it is built from the bit
+// fields on the integer pipe: GB300 issues conversions to f64 on its narrow
+// FP64 pipe, which the chains' fused multiply-adds keep busy. Subnormal floats
+// take the conversion.
+XC_HD double xc_f2d(float f)
+{
+#ifdef __CUDA_ARCH__
+    const uint32_t b = __float_as_uint(f), e = (b >> 23) & 0xffu, mant = b & 0x7fffffu;
+    if (e == 0u && mant != 0u) {
+        return (double)f;
+    }
+    const uint32_t de = e == 0u ? 0u : (e == 0xffu ? 0x7ffu : e + 896u);
+    return __hiloint2double((int)((b & 0x80000000u) | (de << 20) | (mant >> 3)), (int)(mant << 29));
+#else
+    return (double)f;
+#endif
+}
+
 XC_HD uint32_t xc_umin(uint32_t a, uint32_t b) { return a < b ? a : b; }
 XC_HD uint32_t xc_umax(uint32_t a, uint32_t b) { return a > b ? a : b; }
 
@@ -180,7 +198,7 @@ XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         float x, y;
         term(i, x, y);
-        sp.step((double)x, (double)y);
+        sp.step(xc_f2d(x), xc_f2d(y));
     }
     sp.finish(c, i1 <= i0);
 }
@@ -193,7 +211,7 @@ XC_UNROLL4
     for (int i = i0; i < i1; ++i) {
         float x, y;
         term(i, x, y);
-        t = fma((double)x, (double)y, t);
+        t = fma(xc_f2d(x), xc_f2d(y), t);
     }
     return t;
 }
