@@ -991,18 +991,11 @@ static size_t fast_sweep_smem(int m, int w, int stages) { return FastSweepSmem(m
 // (228 KB per SM, 1 KB of it reserved per block) and registers.
 static int fast_sweep_regs();
 
-// Register cap of the sweep: MARS_GPU_FS_RB = 2 (the default: at most ~100
-// registers, two of the largest blocks per SM; measured on the n = 1e6 fit,
-// the sweep phase went 172 -> 132 ms a step at 13 basis columns and
-// 422 -> 328 ms at 50 against the uncapped kernel), 1 (no cap) or 3.
-static int fast_sweep_rb()
-{
-    static const int rb = [] {
-        const char *v = std::getenv("MARS_GPU_FS_RB");
-        return v && (*v == '1' || *v == '3') ? *v - '0' : 2;
-    }();
-    return rb;
-}
+// The sweep is compiled for two of its largest blocks per SM (at most ~100
+// registers): measured on the n = 1e6 fit, the sweep phase went 172 -> 132 ms
+// a step at 13 basis columns and 422 -> 328 ms at 50 against the uncapped
+// kernel; a cap for three blocks (~64 registers) spilled and was slower.
+constexpr int FS_RB = 2;
 
 static int fast_sweep_bps(int m, int w, int stages)
 {
@@ -1017,10 +1010,7 @@ static int fast_sweep_regs()
 {
     static const int regs = [] {
         cudaFuncAttributes fa;
-        const int rb = fast_sweep_rb();
-        const cudaError_t e = rb == 2   ? cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4, 2>)
-                              : rb == 3 ? cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4, 3>)
-                                        : cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4, 1>);
+        const cudaError_t e = cudaFuncGetAttributes(&fa, k_fast_sweep<1, 4, FS_RB>);
         const int r = e == cudaSuccess ? std::max(fa.numRegs, 32) : 168;
         cudaGetLastError();
         return r;
@@ -1028,10 +1018,14 @@ static int fast_sweep_regs()
     return regs;
 }
 
-// The stage depth: four unless two lets more blocks reside.
+// The stage depth: the deepest ring (4, 3 or 2 stages of 32 rows) that lets
+// as many blocks reside as the shallowest. With two stages the loaders wait
+// for the stage they have just issued; with three the load of a stage has a
+// whole stage of compute to land in.
 static int fast_sweep_stages(int m, int w)
 {
-    return fast_sweep_bps(m, w, 2) > fast_sweep_bps(m, w, 4) ? 2 : 4;
+    const int b2 = fast_sweep_bps(m, w, 2);
+    return fast_sweep_bps(m, w, 4) >= b2 ? 4 : fast_sweep_bps(m, w, 3) >= b2 ? 3 : 2;
 }
 
 int fast_sweep_warps(int m, const std::vector<int> &group_sizes)
@@ -1087,23 +1081,15 @@ void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int
             reinterpret_cast<const FastTask *>(tasks), perm, xsort, ysort, cols, BoR, ldbo,    \
             ybo, ybx, mom, n, m, head, tail, mid, min_span, tol, cut_rel, hsse, hrow, hflag);  \
     } while (0)
-#define LAUNCH_FS(CPL, S)               \
-    do {                                \
-        if (fast_sweep_rb() == 2) {     \
-            LAUNCH_FS_RB(CPL, S, 2);    \
-        } else if (fast_sweep_rb() == 3) { \
-            LAUNCH_FS_RB(CPL, S, 3);    \
-        } else {                        \
-            LAUNCH_FS_RB(CPL, S, 1);    \
-        }                               \
-    } while (0)
-#define LAUNCH_FS_CPL(CPL)      \
-    do {                        \
-        if (stages == 4) {      \
-            LAUNCH_FS(CPL, 4);  \
-        } else {                \
-            LAUNCH_FS(CPL, 2);  \
-        }                       \
+#define LAUNCH_FS_CPL(CPL)                   \
+    do {                                     \
+        if (stages == 4) {                   \
+            LAUNCH_FS_RB(CPL, 4, FS_RB);     \
+        } else if (stages == 3) {            \
+            LAUNCH_FS_RB(CPL, 3, FS_RB);     \
+        } else {                             \
+            LAUNCH_FS_RB(CPL, 2, FS_RB);     \
+        }                                    \
     } while (0)
     if (nc <= 32) {
         LAUNCH_FS_CPL(1);
@@ -1117,7 +1103,6 @@ void fast_sweep(cudaStream_t st, const FastTaskRec *tasks, int ntasks, const int
         throw Error(1, "the fast hinge sweep supports at most 253 basis functions");
     }
 #undef LAUNCH_FS_CPL
-#undef LAUNCH_FS
 #undef LAUNCH_FS_RB
     LAUNCH_CHECK();
     *launches += 1;
