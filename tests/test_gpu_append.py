@@ -7,8 +7,9 @@ exact parallel evaluation of the reference's sequential chain: chunk records,
 composed by sub-group, warp and block, walked by the last block with descents
 wherever a record cannot vouch for its entry. The results must equal the
 oracle's: w and v of orthonormalize_col, the MSE of every append (and its
-rejection), dsse, and the eval outputs after the appends, from a handful of
-rows (one partly empty block) to 10^6 rows (hundreds of blocks).
+rejection), dsse, and the eval outputs after the appends -- whose DGKS
+re-pass runs on the same exact chains, side by side -- from a handful of rows
+(one partly empty block) to 10^6 rows (hundreds of blocks).
 """
 import numpy as np
 import pytest
@@ -91,7 +92,12 @@ def test_append_sequence_bit_exact(gpu, n, p, seed):
         assert g.nbasis() == c.nbasis(), k
     assert _bits(g.dsse()) == _bits(c.dsse())
     mask = np.ones((p, g.nbasis()), bool)
+    fired = g.stats()["dgks_fired"]
     out_g = g.eval(mask, 1, 0, False, 1)
     out_c = c.eval(mask, 1, 0, False, 0)
     for a, b in zip(out_g[1:], out_c[1:]):
         np.testing.assert_array_equal(a, b)
+    if n >= 65536:
+        # the eval's DGKS re-pass (near-duplicate inputs 0 and 1) formed T with
+        # the side-by-side exact chains (few entries, long columns)
+        assert g.stats()["dgks_fired"] > fired
