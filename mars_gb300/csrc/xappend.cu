@@ -37,7 +37,7 @@ constexpr int XA_SUB = 8;             // chunks per sub-group
 constexpr int XA_NS = XA_T / XA_SUB;  // sub-groups per block (4 per warp)
 constexpr int XA_GRP = 16;            // blocks per group of the final walk
 constexpr int XA_MAXG = XA_T;         // blocks per launch at most (their records fit in s_rc)
-constexpr int XA_LMIN = 16;           // rows per chunk at least, below XA_MAXG blocks
+constexpr int XA_LMIN = 8;            // rows per chunk at least, below XA_MAXG blocks
 constexpr int XA_TILE = 8;            // rows whose loads a thread issues together
 constexpr long long XA_MAX_CHAINS = 65535;  // side-by-side chains per launch (grid y)
 constexpr size_t XA_REC_BUDGET = 1ull << 30;  // bytes of records for side-by-side chains
