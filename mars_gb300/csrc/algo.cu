@@ -605,8 +605,8 @@ TcBasis tc_basis(mars_gpu_algo *a)
 // MARS_GPU_MIXED_TOPK (default 4) by linear and by hinge delta SSE, and any
 // within MARS_GPU_MIXED_BAND (default 2%) of the best fast value -- and the
 // numerically unreliable ones (below) are
-// re-evaluated on the host cores in the reference's exact FP64 order
-// (host_exact.cpp), and the decisions come from those exact values: the
+// re-evaluated on the FP64 GPU path in the reference's exact FP64 order, and
+// the decisions come from those exact values: the
 // re-decided candidates carry their exact delta SSE and knot, every other one
 // its fast value, held strictly below the best exact value so the first
 // maximum (mars.py:342-343) is always an exactly evaluated candidate.
