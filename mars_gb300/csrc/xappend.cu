@@ -244,6 +244,7 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
             if (A.fill) {
                 xs[u] = Xc[i];
                 bs[u] = Bp[i];
+                vin[u] = 0.0;
             } else {
                 vin[u] = A.v_in ? A.v_in[i] : 0.0;
                 if (A.scale) {
