@@ -465,58 +465,69 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
             s_t = 0.0;
         }
         __syncthreads();
-        // The walk from the true start 0, thread 0 stepping and the block
-        // loading a block's sub-records for it where the block's record cannot
-        // vouch for the walk's value.
-        auto step = [&](const XcRec &r) {  // thread 0; s_ok = whether r vouched
+        // The walk from the true start 0: thread 0 steps through the group
+        // records, and through a group's block records where the group's
+        // cannot vouch for its value, on its own; where a block's record cannot
+        // either, the block loads that block's sub-records for it and thread 0
+        // walks them, re-running rows at the bottom.
+        int pos_g = 0, pos_b = -1;  // thread 0: the group, the block in it (-1: none yet)
+        for (;;) {
             if (t == 0) {
+                int fail = -1;
                 double v = s_t;
                 XcTrack tr;
                 tr.init(0u);
-                s_ok = xc_track(r, v, tr) ? 1 : 0;
-                if (s_ok) {
-                    s_t = v;
+                while (fail < 0 && pos_g < ngrp) {
+                    const int b0 = pos_g * XA_GRP, cnt = min(XA_GRP, G - b0);
+                    if (pos_b < 0) {
+                        if (xc_track(s_rg[pos_g], v, tr)) {
+                            ++pos_g;
+                            continue;
+                        }
+                        pos_b = 0;
+                    }
+                    while (pos_b < cnt && xc_track(s_rc[b0 + pos_b], v, tr)) {
+                        ++pos_b;
+                    }
+                    if (pos_b < cnt) {
+                        fail = b0 + pos_b++;
+                    }
+                    if (pos_b >= cnt) {
+                        ++pos_g;
+                        pos_b = -1;
+                    }
                 }
+                s_t = v;
+                s_ok = fail;
             }
             __syncthreads();
-            const int ok = s_ok;
+            const int bk = s_ok;
+            if (bk < 0) {
+                break;
+            }
+            copy_recs(d_rw, Arw + (size_t)bk * XA_NW, XA_NW);
+            copy_recs(d_rs, Ars + (size_t)bk * XA_NS, XA_NS);
+            copy_recs(d_rc, Arc + (size_t)bk * XA_T, XA_T);
             __syncthreads();
-            return ok;
-        };
-        for (int g = 0; g < ngrp; ++g) {
-            if (step(s_rg[g])) {
-                continue;
+            if (t == 0) {
+                XcTrack tr;
+                tr.init(0u);
+                s_t = xc_walk(
+                    [&](int w) -> const XcRec & { return d_rw[w]; }, XA_NW, s_t, tr,
+                    [&](int w, double &u, XcTrack &tq) {
+                        u = xc_walk(
+                            [&](int q) -> const XcRec & { return d_rs[w * 4 + q]; }, 4, u, tq,
+                            [&](int q, double &z, XcTrack &tz) {
+                                const int c0 = (w * 4 + q) * XA_SUB;
+                                z = xc_walk([&](int r) -> const XcRec & { return d_rc[c0 + r]; },
+                                            XA_SUB, z, tz, [&](int r, double &e, XcTrack &te) {
+                                                const int gch = bk * XA_T + c0 + r;
+                                                xc_run_track(tg, rows_lo(gch), rows_hi(gch), e, te);
+                                            });
+                            });
+                    });
             }
-            const int b0 = g * XA_GRP, cnt = min(XA_GRP, G - b0);
-            for (int k = 0; k < cnt; ++k) {
-                const int bk = b0 + k;
-                if (step(s_rc[bk])) {
-                    continue;
-                }
-                copy_recs(d_rw, Arw + (size_t)bk * XA_NW, XA_NW);
-                copy_recs(d_rs, Ars + (size_t)bk * XA_NS, XA_NS);
-                copy_recs(d_rc, Arc + (size_t)bk * XA_T, XA_T);
-                __syncthreads();
-                if (t == 0) {
-                    XcTrack tr;
-                    tr.init(0u);
-                    s_t = xc_walk(
-                        [&](int w) -> const XcRec & { return d_rw[w]; }, XA_NW, s_t, tr,
-                        [&](int w, double &u, XcTrack &tq) {
-                            u = xc_walk(
-                                [&](int q) -> const XcRec & { return d_rs[w * 4 + q]; }, 4, u, tq,
-                                [&](int q, double &z, XcTrack &tz) {
-                                    const int c0 = (w * 4 + q) * XA_SUB;
-                                    z = xc_walk([&](int r) -> const XcRec & { return d_rc[c0 + r]; },
-                                                XA_SUB, z, tz, [&](int r, double &e, XcTrack &te) {
-                                                    const int gch = bk * XA_T + c0 + r;
-                                                    xc_run_track(tg, rows_lo(gch), rows_hi(gch), e, te);
-                                                });
-                                });
-                        });
-                }
-                __syncthreads();
-            }
+            __syncthreads();
         }
         c = s_t;
         if (t == 0) {
