@@ -36,12 +36,22 @@ constexpr int XA_NW = XA_T / 32;      // warps per block
 constexpr int XA_SUB = 8;             // chunks per sub-group
 constexpr int XA_NS = XA_T / XA_SUB;  // sub-groups per block (4 per warp)
 constexpr int XA_GRP = 16;            // blocks per group of the final walk
-constexpr int XA_MAXG = XA_T;         // blocks per launch at most (their records fit in s_rc)
+constexpr int XA_MAXG = XA_T;         // blocks per launch at most
 constexpr int XA_LMIN = 8;            // rows per chunk at least, below XA_MAXG blocks
 constexpr int XA_TILE = 8;            // rows whose loads a thread issues together
 constexpr long long XA_MAX_CHAINS = 65535;  // side-by-side chains per launch (grid y)
 constexpr size_t XA_REC_BUDGET = 1ull << 30;  // bytes of records for side-by-side chains
 constexpr int XA_LANES = XC_RUNS + 1;
+// Block and group records carry more residues than the chunks': a walk from the
+// true start crosses them where a 4-residue record, allowed one binade of rise
+// above its start, would send it down into the block's sub-records.
+constexpr int XA_RB = 8;
+constexpr int XA_LANES_B = XA_RB + 1;
+using XcRecB = XcRecT<XA_RB>;
+// bytes of dynamic shared memory for a block's own records, which the last
+// block reuses for the blocks' records
+constexpr size_t XA_SMEM_OWN =
+    (std::max(sizeof(XcRec) * (XA_T + XA_NS + XA_NW), sizeof(XcRecB) * XA_MAXG) + 15) / 16 * 16;
 
 // result slots
 constexpr int R_RAW2 = 0, R_VN = 1, R_VN2 = 2, R_YBO = 3, R_C = 4;
@@ -97,7 +107,8 @@ struct XaArgs {
     const int *ycol;
     // scratch
     double *res;
-    XcRec *rc, *rs, *rw, *rb;
+    XcRec *rc, *rs, *rw;
+    XcRecB *rb;
     double *agg;
     unsigned *ticket;
 };
@@ -192,11 +203,12 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
     XcRec *const s_rc = reinterpret_cast<XcRec *>(xa_smem);
     XcRec *const s_rs = s_rc + XA_T;
     XcRec *const s_rw = s_rs + XA_NS;
-    XcRec *const d_rc = s_rw + XA_NW;
+    XcRecB *const s_rbk = reinterpret_cast<XcRecB *>(xa_smem);
+    XcRec *const d_rc = reinterpret_cast<XcRec *>(xa_smem + XA_SMEM_OWN);
     XcRec *const d_rs = d_rc + XA_T;
     XcRec *const d_rw = d_rs + XA_NS;
-    __shared__ XcRec s_rb;
-    __shared__ XcRec s_rg[XA_MAXG / XA_GRP];
+    __shared__ XcRecB s_rb;
+    __shared__ XcRecB s_rg[XA_MAXG / XA_GRP];
     __shared__ double s_sh[XA_NW + 1];
     __shared__ double s_agg[3][XA_NW];
     __shared__ double s_t;
@@ -210,7 +222,7 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
     XcRec *const Arc = A.rc + (size_t)ch * G * XA_T;
     XcRec *const Ars = A.rs + (size_t)ch * G * XA_NS;
     XcRec *const Arw = A.rw + (size_t)ch * G * XA_NW;
-    XcRec *const Arb = A.rb + (size_t)ch * G;
+    XcRecB *const Arb = A.rb + (size_t)ch * G;
     double *const Aagg = A.agg + (size_t)ch * 3 * G;
     const double *const Ag_in = A.g_in + (size_t)ch * G;
     double *const Ag_out = A.g_out + (size_t)ch * G;
@@ -407,7 +419,7 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
                             s_rw[warp]);
         }
         __syncthreads();
-        if (warp == 0 && lane < XA_LANES) {
+        if (warp == 0 && lane < XA_LANES_B) {
             xc_compose_lane(
                 [&](int k) -> const XcRec & { return s_rw[k]; }, XA_NW, lane,
                 [&](int k, double &u, XcTrack &tq) {
@@ -442,22 +454,23 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
         const XaTerm tg{A.kind, Aq, Ay, vsrc, true};
         const int ngrp = (G + XA_GRP - 1) / XA_GRP;
         // the blocks' records into shared memory (this block's chunk records are done with)
-        auto copy_recs = [&](XcRec *dst, const XcRec *src, int count) {
+        auto copy_recs = [&](auto *dst, const auto *src, int count) {
+            static_assert(sizeof(*dst) == sizeof(*src) && sizeof(*dst) % 8 == 0, "records");
             const double *sp = reinterpret_cast<const double *>(src);
             double *dp = reinterpret_cast<double *>(dst);
-            for (int k = t; k < count * (int)(sizeof(XcRec) / 8); k += XA_T) {
+            for (int k = t; k < count * (int)(sizeof(*dst) / 8); k += XA_T) {
                 dp[k] = __ldcg(sp + k);
             }
         };
-        copy_recs(s_rc, Arb, G);
+        copy_recs(s_rbk, Arb, G);
         __syncthreads();
         // groups of XA_GRP blocks; a lane meeting a block that cannot vouch for
         // its value gives up (the final walk descends there instead)
         {
-            const int g = t >> 3, ln = t & 7;
-            if (g < ngrp && ln < XA_LANES) {
+            const int g = t >> 4, ln = t & 15;
+            if (g < ngrp && ln < XA_LANES_B) {
                 const int b0 = g * XA_GRP, cnt = min(XA_GRP, G - b0);
-                xc_compose_lane([&](int k) -> const XcRec & { return s_rc[b0 + k]; }, cnt, ln,
+                xc_compose_lane([&](int k) -> const XcRecB & { return s_rbk[b0 + k]; }, cnt, ln,
                                 [&](int, double &, XcTrack &tq) { tq.lost = true; }, s_rg[g]);
             }
         }
@@ -486,7 +499,7 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
                         }
                         pos_b = 0;
                     }
-                    while (pos_b < cnt && xc_track(s_rc[b0 + pos_b], v, tr)) {
+                    while (pos_b < cnt && xc_track(s_rbk[b0 + pos_b], v, tr)) {
                         ++pos_b;
                     }
                     if (pos_b < cnt) {
@@ -559,7 +572,7 @@ __global__ void __launch_bounds__(XA_T, 2) k_xappend(const XaArgs A)
     }
 }
 
-constexpr size_t xa_smem_bytes() { return sizeof(XcRec) * 2 * (XA_T + XA_NS + XA_NW); }
+constexpr size_t xa_smem_bytes() { return XA_SMEM_OWN + sizeof(XcRec) * (XA_T + XA_NS + XA_NW); }
 
 int xa_blocks(int n)
 {
@@ -602,7 +615,7 @@ struct XaRun {
         bf.rc.ensure(sizeof(XcRec) * (size_t)G * XA_T);
         bf.rs.ensure(sizeof(XcRec) * (size_t)G * XA_NS);
         bf.rw.ensure(sizeof(XcRec) * (size_t)G * XA_NW);
-        bf.rb.ensure(sizeof(XcRec) * (size_t)G);
+        bf.rb.ensure(sizeof(XcRecB) * (size_t)G);
         bf.agg.ensure(sizeof(double) * 3 * (size_t)G);
         bf.g0.ensure(sizeof(double) * (size_t)G);
         bf.g1.ensure(sizeof(double) * (size_t)G);
@@ -629,7 +642,7 @@ struct XaRun {
         a.rc = bf.rc.as<XcRec>();
         a.rs = bf.rs.as<XcRec>();
         a.rw = bf.rw.as<XcRec>();
-        a.rb = bf.rb.as<XcRec>();
+        a.rb = bf.rb.as<XcRecB>();
         a.agg = bf.agg.as<double>();
         a.ticket = bf.ticket.as<unsigned>();
         return a;
@@ -836,7 +849,7 @@ bool tgemm_exact(cudaStream_t st, int n, int m, int P, const float *BoC, const f
     }
     // blocks per chain: at least 16 rows a chunk; records of all chains
     // within XA_REC_BUDGET bytes
-    const size_t per_block = sizeof(XcRec) * (XA_T + XA_NS + XA_NW + 1);
+    const size_t per_block = sizeof(XcRec) * (XA_T + XA_NS + XA_NW) + sizeof(XcRecB);
     const long long gmax =
         std::max<long long>(1, (long long)(XA_REC_BUDGET / ((size_t)chains * per_block)));
     const int G = (int)std::max<long long>(1, std::min<long long>(xa_blocks(n), gmax));
@@ -845,7 +858,7 @@ bool tgemm_exact(cudaStream_t st, int n, int m, int P, const float *BoC, const f
     bf.rc.ensure(sizeof(XcRec) * cg * XA_T);
     bf.rs.ensure(sizeof(XcRec) * cg * XA_NS);
     bf.rw.ensure(sizeof(XcRec) * cg * XA_NW);
-    bf.rb.ensure(sizeof(XcRec) * cg);
+    bf.rb.ensure(sizeof(XcRecB) * cg);
     bf.agg.ensure(sizeof(double) * 3 * cg);
     bf.g0.ensure(sizeof(double) * cg);
     bf.g1.ensure(sizeof(double) * cg);
@@ -866,7 +879,7 @@ bool tgemm_exact(cudaStream_t st, int n, int m, int P, const float *BoC, const f
     a.rc = bf.rc.as<XcRec>();
     a.rs = bf.rs.as<XcRec>();
     a.rw = bf.rw.as<XcRec>();
-    a.rb = bf.rb.as<XcRec>();
+    a.rb = bf.rb.as<XcRecB>();
     a.agg = bf.agg.as<double>();
     a.ticket = bf.ticket.as<unsigned>();
     const dim3 grid((unsigned)G, (unsigned)chains);

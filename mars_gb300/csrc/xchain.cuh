@@ -305,14 +305,30 @@ struct XcGuess {
 // every ulp the shifted chain rounds to and every rounding, ties included, is
 // translated. hmax[r] carries that largest magnitude up the levels.
 // ---------------------------------------------------------------------------
-struct XcRec {
+//
+// A record may carry R residues (R a power of two, its start's log2 R last
+// bits clear): a composite with R residues vouches for shifts that are
+// multiples of R ulps of its start, so its values may rise log2(R) - 1
+// binades above it.
+template <int R>
+struct XcRecT {
     double start;
-    double end[XC_RUNS];
-    double margin[XC_RUNS];
+    double end[R];
+    double margin[R];
     double zero_end;
-    uint32_t hmax[XC_RUNS];  // largest magnitude high word visited from start + r ulps
+    uint32_t hmax[R];  // largest magnitude high word visited from start + r ulps
     int zero_ok;
     int empty;
+};
+using XcRec = XcRecT<XC_RUNS>;
+
+template <int R>
+struct XcLog2 {
+    static constexpr int value = 1 + XcLog2<R / 2>::value;
+};
+template <>
+struct XcLog2<1> {
+    static constexpr int value = 0;
 };
 
 // The XC_RUNS residue runs of one chunk, and the run from +0 when asked for
@@ -387,7 +403,8 @@ struct XcTrack {
 };
 
 // Extends a walk at t through record c, if c vouches for t.
-XC_HD bool xc_track(const XcRec &c, double &t, XcTrack &tr)
+template <int R>
+XC_HD bool xc_track(const XcRecT<R> &c, double &t, XcTrack &tr)
 {
     if (c.empty) {
         return true;
@@ -403,7 +420,7 @@ XC_HD bool xc_track(const XcRec &c, double &t, XcTrack &tr)
     if ((xc_hi(t) >> 20) != (hc >> 20)) {
         return false;
     }
-    const uint32_t r = xc_lo(t) & (uint32_t)(XC_RUNS - 1);
+    const uint32_t r = xc_lo(t) & (uint32_t)(R - 1);
     const double d = t - xc_words(hc, xc_lo(c.start) | r);  // exact: one binade
     const double md = c.margin[r];
     if (!(fabs(d) <= md)) {
@@ -464,17 +481,19 @@ XC_HD double xc_walk(const RecAt &rec, int K, double t, XcTrack &tr, const Throu
     return t;
 }
 
-// One lane of the composition of the consecutive records rec(0 .. K-1): lane
-// r < XC_RUNS walks from start + r ulps and fills end[r], margin[r], hmax[r];
-// lane XC_RUNS walks from +0 (when the start is +0) and fills zero_end and
+// One lane of the composition of the consecutive records rec(0 .. K-1) into a
+// record with R residues: lane r < R walks from start + r ulps and fills
+// end[r], margin[r], hmax[r]; lane R walks from +0 (when the start is +0) and
+// fills zero_end and
 // zero_ok; lane 0 also sets
 // start and empty. The lanes write disjoint fields of `out`. A walked value is
 // the true chain from its entry (through() re-runs what no record vouches for,
 // or gives up, and the lane's result is then marked invalid); the composite
 // vouches for a shift D of the entry when every value kept its binade under it
-// and no value lay more than one binade above the start.
-template <class RecAt, class Through>
-XC_HD void xc_compose_lane(const RecAt &rec, int K, int lane, const Through &through, XcRec &out)
+// and no value lay more than log2(R) - 1 binades above the start.
+template <class RecAt, class Through, int R>
+XC_HD void xc_compose_lane(const RecAt &rec, int K, int lane, const Through &through,
+                           XcRecT<R> &out)
 {
     int k0 = 0;
     while (k0 < K && rec(k0).empty) {
@@ -485,7 +504,7 @@ XC_HD void xc_compose_lane(const RecAt &rec, int K, int lane, const Through &thr
             out.start = 0.0;
             out.empty = 1;
         }
-        if (lane < XC_RUNS) {
+        if (lane < R) {
             out.end[lane] = 0.0;
             out.margin[lane] = 1.0e300;
             out.hmax[lane] = 0u;
@@ -495,7 +514,8 @@ XC_HD void xc_compose_lane(const RecAt &rec, int K, int lane, const Through &thr
         }
         return;
     }
-    const double S = rec(k0).start;
+    const double S0 = rec(k0).start;  // its last log2 R bits cleared: the composite's start
+    const double S = xc_words(xc_hi(S0), xc_lo(S0) & ~(uint32_t)(R - 1));
     const uint32_t hs = xc_hi(S);
     if (lane == 0) {
         out.start = S;
@@ -504,7 +524,7 @@ XC_HD void xc_compose_lane(const RecAt &rec, int K, int lane, const Through &thr
     const uint32_t Es = (hs >> 20) & 0x7ffu;
     XcTrack tr;
     tr.init(hs);
-    if (lane >= XC_RUNS) {
+    if (lane >= R) {
         // Only a composite guessed to start at exactly 0 (every term before it
         // summed to 0) is likely to be entered at +0; other ones are descended
         // into when that happens.
@@ -523,5 +543,6 @@ XC_HD void xc_compose_lane(const RecAt &rec, int K, int lane, const Through &thr
     const uint32_t Eh = (tr.H >> 20) & 0x7ffu;
     out.end[lane] = t;
     out.hmax[lane] = tr.H;
-    out.margin[lane] = (tr.ok && !tr.lost && Eh <= Es + 1u) ? tr.M : -1.0;
+    out.margin[lane] =
+        (tr.ok && !tr.lost && Eh <= Es + (uint32_t)(XcLog2<R>::value - 1)) ? tr.M : -1.0;
 }

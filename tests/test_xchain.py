@@ -37,6 +37,9 @@ def xlib(tmp_path_factory):
     lib.xc_host_composed.restype = ctypes.c_double
     lib.xc_host_composed.argtypes = [fp, dp, ctypes.c_int, ctypes.c_int, ip, ctypes.c_int,
                                      ctypes.c_int, ctypes.c_double, ip, ip, ip]
+    for name in ("xc_host_kernel4", "xc_host_kernel8"):
+        getattr(lib, name).restype = ctypes.c_double
+        getattr(lib, name).argtypes = [fp, dp, ctypes.c_int, ctypes.c_int, ip, ip]
     return lib
 
 
@@ -207,6 +210,55 @@ def test_composed_walk_is_short(xlib):
     want, got, redone, desc = composed(xlib, v.astype(np.float32), v, 38912, [8, 4, 8, 16])
     assert same(want, got)
     assert redone <= 4 and desc <= 8, (redone, desc)
+
+
+def kernel_levels(lib, a, b, K, rb):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float64)
+    fp = ctypes.POINTER(ctypes.c_float)
+    dp = ctypes.POINTER(ctypes.c_double)
+    re, de = ctypes.c_int(0), ctypes.c_int(0)
+    got = getattr(lib, "xc_host_kernel%d" % rb)(a.ctypes.data_as(fp), b.ctypes.data_as(dp),
+                                                 a.size, K, ctypes.byref(re), ctypes.byref(de))
+    return got, re.value, de.value
+
+
+@pytest.mark.parametrize("K", [1, 64, 1000, 8192])
+def test_kernel_levels_equal_sequential(xlib, K):
+    """The append kernel's own levels (4-residue chunk, sub-group and warp
+    records, 8-residue block and group records whose group lanes give up where
+    a block cannot vouch) give the sequential chain bit for bit."""
+    r = np.random.default_rng(K + 11)
+    for name, a, b in cases(K):
+        bd = b.astype(np.float64)
+        if name in ("signed", "wide"):
+            bd = bd * (1.0 + 2.0 ** -30 * r.standard_normal(bd.size))
+        want = xlib.xc_host_sequential_d(a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                         np.ascontiguousarray(bd).ctypes.data_as(
+                                             ctypes.POINTER(ctypes.c_double)), a.size)
+        for rb in (4, 8):
+            got, _, _ = kernel_levels(xlib, a, bd, K, rb)
+            assert same(want, got) or (np.isnan(want) and np.isnan(got)), (name, K, rb)
+
+
+def test_block_residues_shorten_the_walk(xlib):
+    """Signed dot products at 10^6 rows in the kernel's shape (256 blocks of
+    256 chunks): 8 residues at the block and group levels let the walk cross
+    blocks that 4 would descend into."""
+    r = np.random.default_rng(12)
+    n, K = 1_000_000, 256 * 256
+    tot = {4: 0, 8: 0}
+    for it in range(4):
+        q = r.standard_normal(n).astype(np.float32)
+        v = r.standard_normal(n) * (1.0 + it)
+        v -= q.astype(np.float64) * (q.astype(np.float64) @ v) / float(q.astype(np.float64) @ q)
+        want = xlib.xc_host_sequential_d(q.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                         v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n)
+        for rb in (4, 8):
+            got, _, desc = kernel_levels(xlib, q, v, K, rb)
+            assert same(want, got), (it, rb)
+            tot[rb] += desc
+    assert tot[8] < tot[4], tot
 
 
 def test_translation_is_used(xlib):

@@ -32,6 +32,124 @@ double run_d(const TermD &t, int i0, int i1, double acc)
 }
 }  // namespace
 
+// The append kernel's composition: chunk records (XC_RUNS residues) composed
+// per 8 chunks and per 4 of those (XC_RUNS residues), then per 8 into block
+// records and per 16 blocks into group records (RB residues each), and the
+// final walk over the groups with descents down to re-running rows.
+template <int RB>
+double kernel_composed_impl(const float *a, const double *b, int n, int K, int *redone,
+                            int *descents)
+{
+    const TermD term{a, b};
+    const int L = n > 0 ? (n + K - 1) / K : 0;
+    auto lo = [&](int c) { return c * L < n ? c * L : n; };
+    auto hi = [&](int c) { return lo(c) + L < n ? lo(c) + L : n; };
+    std::vector<XcRec> ch(K);
+    double pre = 0.0;
+    for (int c = 0; c < K; ++c) {
+        XcGuess g;
+        for (int i = lo(c); i < hi(c); ++i) {
+            const float vh = (float)b[i];
+            g.add_scaled(a[i], vh, (float)(b[i] - (double)vh));
+        }
+        XcSpecR sp;
+        sp.begin(pre, pre == 0.0);
+        for (int i = lo(c); i < hi(c); ++i) {
+            sp.step((double)a[i], b[i]);
+        }
+        sp.finish(ch[c], hi(c) <= lo(c));
+        pre += g.value();
+    }
+    auto rows = [&](int c, double &t, XcTrack &tr) {
+        xc_run_track([&](int i, double &x, double &y) {
+            x = (double)a[i];
+            y = b[i];
+        }, lo(c), hi(c), t, tr);
+    };
+    const int NS = (K + 7) / 8, NW = (NS + 3) / 4, NB = (NW + 7) / 8, NG = (NB + 15) / 16;
+    std::vector<XcRec> sub(NS), warp(NW);
+    std::vector<XcRecT<RB>> blk(NB), grp(NG);
+    auto cnt = [](int total, int g, int F) { return total - g * F < F ? total - g * F : F; };
+    auto thr_sub = [&](int s, double &t, XcTrack &tr) {
+        t = xc_walk([&](int k) -> const XcRec & { return ch[s * 8 + k]; }, cnt(K, s, 8), t, tr,
+                    [&](int k, double &u, XcTrack &tq) { rows(s * 8 + k, u, tq); });
+    };
+    auto thr_warp = [&](int w, double &t, XcTrack &tr) {
+        t = xc_walk([&](int k) -> const XcRec & { return sub[w * 4 + k]; }, cnt(NS, w, 4), t, tr,
+                    [&](int k, double &u, XcTrack &tq) { thr_sub(w * 4 + k, u, tq); });
+    };
+    auto thr_blk = [&](int bk, double &t, XcTrack &tr) {
+        t = xc_walk([&](int k) -> const XcRec & { return warp[bk * 8 + k]; }, cnt(NW, bk, 8), t,
+                    tr, [&](int k, double &u, XcTrack &tq) { thr_warp(bk * 8 + k, u, tq); });
+    };
+    for (int s = 0; s < NS; ++s) {
+        for (int lane = 0; lane <= XC_RUNS; ++lane) {
+            xc_compose_lane([&](int k) -> const XcRec & { return ch[s * 8 + k]; }, cnt(K, s, 8),
+                            lane, [&](int k, double &u, XcTrack &tq) { rows(s * 8 + k, u, tq); },
+                            sub[s]);
+        }
+    }
+    for (int w = 0; w < NW; ++w) {
+        for (int lane = 0; lane <= XC_RUNS; ++lane) {
+            xc_compose_lane([&](int k) -> const XcRec & { return sub[w * 4 + k]; }, cnt(NS, w, 4),
+                            lane, [&](int k, double &u, XcTrack &tq) { thr_sub(w * 4 + k, u, tq); },
+                            warp[w]);
+        }
+    }
+    for (int bk = 0; bk < NB; ++bk) {
+        for (int lane = 0; lane <= RB; ++lane) {
+            xc_compose_lane([&](int k) -> const XcRec & { return warp[bk * 8 + k]; },
+                            cnt(NW, bk, 8), lane,
+                            [&](int k, double &u, XcTrack &tq) { thr_warp(bk * 8 + k, u, tq); },
+                            blk[bk]);
+        }
+    }
+    for (int g = 0; g < NG; ++g) {
+        for (int lane = 0; lane <= RB; ++lane) {  // the kernel's group lanes give up on a block
+            xc_compose_lane([&](int k) -> const XcRecT<RB> & { return blk[g * 16 + k]; },
+                            cnt(NB, g, 16), lane, [&](int, double &, XcTrack &tq) { tq.lost = true; },
+                            grp[g]);
+        }
+    }
+    int nre = 0, nde = 0;
+    XcTrack tr;
+    tr.init(0u);
+    double t = 0.0;
+    for (int g = 0; g < NG; ++g) {
+        if (xc_track(grp[g], t, tr)) {
+            continue;
+        }
+        for (int k = 0; k < cnt(NB, g, 16); ++k) {
+            const int bk = g * 16 + k;
+            if (xc_track(blk[bk], t, tr)) {
+                continue;
+            }
+            ++nde;
+            t = xc_walk([&](int w) -> const XcRec & { return warp[bk * 8 + w]; }, cnt(NW, bk, 8), t,
+                        tr, [&](int w, double &u, XcTrack &tq) {
+                            u = xc_walk([&](int q) -> const XcRec & { return sub[(bk * 8 + w) * 4 + q]; },
+                                        cnt(NS, bk * 8 + w, 4), u, tq,
+                                        [&](int q, double &z, XcTrack &tz) {
+                                            const int sg = (bk * 8 + w) * 4 + q;
+                                            z = xc_walk([&](int r) -> const XcRec & { return ch[sg * 8 + r]; },
+                                                        cnt(K, sg, 8), z, tz,
+                                                        [&](int r, double &e, XcTrack &te) {
+                                                            ++nre;
+                                                            rows(sg * 8 + r, e, te);
+                                                        });
+                                        });
+                        });
+        }
+    }
+    if (redone) {
+        *redone = nre;
+    }
+    if (descents) {
+        *descents = nde;
+    }
+    return t;
+}
+
 extern "C" {
 
 double xc_host_sequential_d(const float *a, const double *b, int n)
@@ -135,6 +253,16 @@ double xc_host_composed(const float *a, const double *b, int n, int K, const int
         *descents = nde;
     }
     return t;
+}
+
+// The append kernel's levels with 4 or 8 residues at the block and group levels.
+double xc_host_kernel4(const float *a, const double *b, int n, int K, int *redone, int *descents)
+{
+    return kernel_composed_impl<4>(a, b, n, K, redone, descents);
+}
+double xc_host_kernel8(const float *a, const double *b, int n, int K, int *redone, int *descents)
+{
+    return kernel_composed_impl<8>(a, b, n, K, redone, descents);
 }
 
 // The recurrence as written.
