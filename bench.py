@@ -583,6 +583,7 @@ class EpochSteps:
         self.wall = 0.0
         self.acc = {k: 0.0 for k in STAT_KEYS}
         self.epoch_ms = []      # device ms of every epoch of the first fit
+        self.fit_terms = []     # the current fit's basis size after each of its epochs
         self._prev_span = 0.0
         self.lib = None         # the Counting module of the current fit
         self.walls = None       # (eval, append) host seconds at the region's start
@@ -596,6 +597,7 @@ class EpochSteps:
         if self.timing:
             self._fold(self.algo)  # the old handle's share so far
         self.algo = algo
+        self.fit_terms = []
         st = algo.stats()
         self.t_create.append((seconds, st["h2d_bytes"]))
         self._prev_span = 0.0
@@ -612,6 +614,7 @@ class EpochSteps:
         st = self.algo.stats()
         self.epoch_ms.append(st["ms_span"] - self._prev_span)
         self._prev_span = st["ms_span"]
+        self.fit_terms.append(self.algo.nbasis())
         self.done += 1
         if not self.timing and not self.closed and self.done == self.W:
             self._sync()
@@ -667,7 +670,18 @@ def epoch_fit(X, y, kw, precision, steps, shard=False):
     wall = time.perf_counter() - t0
     st = lib.algo.stats()
     st["orth_max"], st["rss"] = lib.algo.orth_error()
+    st["orth_steps"] = orth_by_step(lib.algo, steps.fit_terms)
     return model, wall, st, lib.knot_evals
+
+
+def orth_by_step(algo, terms):
+    """max |Q^T Q - I| and the RSS (1 - sum(ybo^2), FP64 from Q and y) after
+    every epoch of the fit, from the basis sizes `terms` its epochs reached."""
+    mx, rss = algo.orth_error_by_terms()
+    k = [min(t, len(mx)) - 1 for t in terms if t >= 1]
+    return {"terms": [int(j + 1) for j in k],
+            "max_abs_QtQ_minus_I": [float(mx[j]) for j in k],
+            "rss": [float(rss[j]) for j in k]}
 
 
 def epoch_grid(X, kw):
@@ -888,7 +902,8 @@ def run_epoch_steps(args):
         "phase_ms_per_step": {k[3:]: acc[k] / args.steps for k in STAT_KEYS if
                               k.startswith("ms_")},
         "clocks": clk,
-        "orthogonality": {"max_abs_QtQ_minus_I": st["orth_max"], "rss": st["rss"]},
+        "orthogonality": {"max_abs_QtQ_minus_I": st["orth_max"], "rss": st["rss"],
+                          "per_step": st["orth_steps"]},
     }
     if args.precision == "mixed":
         line["redecided_fraction"] = acc["redecided"] / max(1, acc["candidates"])
@@ -909,6 +924,10 @@ def run_epoch_steps(args):
         line["orthogonality"]["fp64_max_abs_QtQ_minus_I"] = fst["orth_max"]
         line["orthogonality"]["rss_rel_err_vs_fp64"] = (
             abs(st["rss"] - fst["rss"]) / max(abs(fst["rss"]), 1e-300))
+        mine, theirs = st["orth_steps"], fst["orth_steps"]
+        line["orthogonality"]["fp64_per_step_max_abs_QtQ_minus_I"] = theirs["max_abs_QtQ_minus_I"]
+        line["orthogonality"]["rss_rel_err_vs_fp64_per_step"] = [
+            abs(a - b) / max(abs(b), 1e-300) for a, b in zip(mine["rss"], theirs["rss"])]
     if RANK == 0 and not args.no_cpu_baseline:
         threads = cpu_threads()
         e = args.warmup + args.steps // 2

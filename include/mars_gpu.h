@@ -152,6 +152,17 @@ MARS_GPU_API int mars_gpu_get_stats(const mars_gpu_algo *algo, mars_gpu_stats *o
 MARS_GPU_API int mars_gpu_orth_error(mars_gpu_algo *algo, double *max_abs, double *rss);
 
 /*
+ *  The same two figures for every leading basis of the fit: entry k (k <
+ *  min(cap, m), m = the live basis' size, returned in *count) is max
+ *  |Q_k^T Q_k - I| and 1 - sum(ybo^2) over the first k + 1 columns, what the
+ *  fit measured when its step reached k + 1 terms (stored columns do not change
+ *  after their append). max_abs and rss may be NULL. The last entry equals
+ *  mars_gpu_orth_error's pair.
+ */
+MARS_GPU_API int mars_gpu_orth_error_by_terms(mars_gpu_algo *algo, double *max_abs, double *rss,
+                                              size_t cap, size_t *count);
+
+/*
  *  Kernel-level entry points (host arrays in and out), for tests and
  *  micro-benchmarks.
  *

@@ -1128,6 +1128,44 @@ double append_impl(mars_gpu_algo *a, char type, int xcol, int bcol, float h)
     return mse;
 }
 
+// The Gram matrix Q^T Q and Q^T y of the live basis (FP64 chains over the
+// rows), and from them, for each leading basis of k + 1 columns, max |Q^T Q - I|
+// and 1 - sum(ybo^2). Stored columns never change after their append, so
+// entry k is what the fit's step that made k + 1 columns would have measured.
+void orth_error_by_terms(mars_gpu_algo *a, std::vector<double> &mx, std::vector<double> &rss)
+{
+    const int n = (int)a->n, m = (int)a->m;
+    DevBuf T;
+    T.ensure(sizeof(double) * (size_t)m * (m + 1));
+    StoredSrc q{a->BoC.as<float>(), a->n, nullptr};
+    tgemm_fp64(a->st, q, a->Bo.as<double>(), a->ldbo, n, m, m, T.as<double>(),
+               &a->stats.kernel_launches);
+    std::vector<double> G((size_t)m * m);
+    CUDA_CHECK(cudaMemcpyAsync(G.data(), T.ptr, sizeof(double) * m * m, cudaMemcpyDeviceToHost,
+                               a->st));
+    StoredSrc yy{a->y.as<float>(), a->n, nullptr};
+    tgemm_fp64(a->st, yy, a->Bo.as<double>(), a->ldbo, n, m, 1, T.as<double>(),
+               &a->stats.kernel_launches);
+    std::vector<double> r(m);
+    CUDA_CHECK(cudaMemcpyAsync(r.data(), T.ptr, sizeof(double) * m, cudaMemcpyDeviceToHost,
+                               a->st));
+    sync(a);
+    mx.assign(m, 0.0);
+    rss.assign(m, 0.0);
+    double run = 0.0, rs = 0.0;
+    for (int k = 0; k < m; ++k) {
+        // the new row and column k of the leading block
+        for (int c = 0; c <= k; ++c) {
+            const double d = std::fabs(G[(size_t)k * m + c] - (k == c ? 1.0 : 0.0));
+            const double e = std::fabs(G[(size_t)c * m + k] - (k == c ? 1.0 : 0.0));
+            run = std::max(run, std::max(d, e));
+        }
+        rs = std::fma(r[k], r[k], rs);
+        mx[k] = run;
+        rss[k] = 1.0 - rs;
+    }
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1287,38 +1325,35 @@ int mars_gpu_orth_error(mars_gpu_algo *a, double *max_abs, double *rss)
 {
     return guarded([&] {
         verify(a != nullptr, "null handle");
-        const int n = (int)a->n, m = (int)a->m;
-        DevBuf T;
-        T.ensure(sizeof(double) * (size_t)m * (m + 1));
-        StoredSrc q{a->BoC.as<float>(), a->n, nullptr};
-        tgemm_fp64(a->st, q, a->Bo.as<double>(), a->ldbo, n, m, m, T.as<double>(),
-                   &a->stats.kernel_launches);
-        std::vector<double> G((size_t)m * m);
-        CUDA_CHECK(cudaMemcpyAsync(G.data(), T.ptr, sizeof(double) * m * m,
-                                   cudaMemcpyDeviceToHost, a->st));
-        StoredSrc yy{a->y.as<float>(), a->n, nullptr};
-        tgemm_fp64(a->st, yy, a->Bo.as<double>(), a->ldbo, n, m, 1, T.as<double>(),
-                   &a->stats.kernel_launches);
-        std::vector<double> r(m);
-        CUDA_CHECK(cudaMemcpyAsync(r.data(), T.ptr, sizeof(double) * m, cudaMemcpyDeviceToHost,
-                                   a->st));
-        sync(a);
-        double mx = 0.0;
-        for (int j = 0; j < m; ++j) {
-            for (int c = 0; c < m; ++c) {
-                const double d = G[(size_t)j * m + c] - (j == c ? 1.0 : 0.0);
-                mx = std::max(mx, std::fabs(d));
-            }
-        }
-        double rs = 0.0;
-        for (double v : r) {
-            rs = std::fma(v, v, rs);
-        }
+        std::vector<double> mx, rs;
+        orth_error_by_terms(a, mx, rs);
         if (max_abs) {
-            *max_abs = mx;
+            *max_abs = mx.empty() ? 0.0 : mx.back();
         }
         if (rss) {
-            *rss = 1.0 - rs;
+            *rss = rs.empty() ? 1.0 : rs.back();
+        }
+    });
+}
+
+int mars_gpu_orth_error_by_terms(mars_gpu_algo *a, double *max_abs, double *rss, size_t cap,
+                                 size_t *count)
+{
+    return guarded([&] {
+        verify(a != nullptr, "null handle");
+        std::vector<double> mx, rs;
+        orth_error_by_terms(a, mx, rs);
+        const size_t k = std::min(cap, mx.size());
+        for (size_t j = 0; j < k; ++j) {
+            if (max_abs) {
+                max_abs[j] = mx[j];
+            }
+            if (rss) {
+                rss[j] = rs[j];
+            }
+        }
+        if (count) {
+            *count = mx.size();
         }
     });
 }

@@ -81,6 +81,7 @@ def load():
         "mars_gpu_append": (i, [vp, ctypes.c_char, i, i, ctypes.c_float, dp]),
         "mars_gpu_get_stats": (i, [vp, ctypes.POINTER(Stats)]),
         "mars_gpu_orth_error": (i, [vp, dp, dp]),
+        "mars_gpu_orth_error_by_terms": (i, [vp, dp, dp, sz, ctypes.POINTER(sz)]),
         "mars_gpu_orthonormalize": (i, [sz, sz, sz, fp, sz, fp, ip, fp, sz, fp, sz, dp, d, lp]),
         "mars_gpu_orthonormalize_col": (i, [sz, sz, dp, fp, sz, d, dp, lp]),
         "mars_gpu_orthonormalize_noalloc": (i, [sz, sz, sz, vp, sz, sz, vp, ip, vp, sz, vp, sz,
@@ -224,6 +225,18 @@ class MarsAlgo:
         mx, rss = ctypes.c_double(), ctypes.c_double()
         check(self._L.mars_gpu_orth_error(self._h, ctypes.byref(mx), ctypes.byref(rss)))
         return mx.value, rss.value
+
+    def orth_error_by_terms(self):
+        """(max |Q_k^T Q_k - I|, 1 - sum(ybo^2)) for every leading basis of
+        k + 1 columns, as two float64 arrays of the basis' length."""
+        m = self.nbasis()
+        mx, rss = np.zeros(m), np.zeros(m)
+        count = ctypes.c_size_t()
+        dp = ctypes.POINTER(ctypes.c_double)
+        check(self._L.mars_gpu_orth_error_by_terms(self._h, mx.ctypes.data_as(dp),
+                                                    rss.ctypes.data_as(dp), m,
+                                                    ctypes.byref(count)))
+        return mx[:count.value], rss[:count.value]
 
 
 def compiled():

@@ -80,6 +80,13 @@ def test_eval_matches_oracle(name, precision, scoring, gpu, port, monkeypatch):
     mx, rss = a_gpu.orth_error()
     assert mx < 1e-5
     assert rss == pytest.approx(1 - a_gpu.dsse(), rel=1e-6)
+    # the same figures for every leading basis: the last pair is the whole
+    # basis', max |Q^T Q - I| only grows and the RSS only falls with the terms
+    mk, rk = a_gpu.orth_error_by_terms()
+    assert len(mk) == len(rk) == a_gpu.nbasis()
+    assert (mk[-1], rk[-1]) == (mx, rss)
+    assert np.all(np.diff(mk) >= 0) and np.all(np.diff(rk) <= 0)
+    assert np.all(mk < 1e-5) and rk[0] <= 1.0
 
 
 @pytest.mark.parametrize("name", ["hinge_search", "precision_stress_small", "weighted_nan"])
