@@ -100,3 +100,22 @@ def test_epoch_sample_replays_the_reference_basis():
     m = state["algo"].nbasis()
     assert 1 + 3 <= m <= 1 + 6
     assert bench.path_epochs(path) >= 3
+
+
+def test_orth_by_step_follows_the_epochs():
+    """The per-step orthogonality report picks, for each epoch, the entry of
+    the leading basis that epoch reached (a linear term adds one column, a
+    hinge pair two, a rejected column none)."""
+    import numpy as np
+
+    import bench
+
+    class Fake:
+        def orth_error_by_terms(self):
+            return np.arange(1, 8) * 1e-9, 1.0 - np.arange(1, 8) * 0.1
+
+    out = bench.orth_by_step(Fake(), [3, 5, 5, 6, 7])
+    assert out["terms"] == [3, 5, 5, 6, 7]
+    assert out["max_abs_QtQ_minus_I"] == pytest.approx([3e-9, 5e-9, 5e-9, 6e-9, 7e-9])
+    assert out["rss"] == pytest.approx([0.7, 0.5, 0.5, 0.4, 0.3])
+    assert bench.orth_by_step(Fake(), []) == {"terms": [], "max_abs_QtQ_minus_I": [], "rss": []}
