@@ -293,7 +293,7 @@ void create_impl(mars_gpu_algo *a, const float *X, const float *y, const float *
     // Device-resident state.
     a->stats.h2d_bytes += (long long)(sizeof(float) * (n * p + 3 * n + p));
     a->X.ensure(sizeof(float) * std::max<size_t>(1, n * p));
-    if (n * p) {
+    if (n > 0 && p > 0) {
         CUDA_CHECK(cudaMemcpy2DAsync(a->X.ptr, n * sizeof(float), X, ldx * sizeof(float),
                                      n * sizeof(float), p, cudaMemcpyHostToDevice, a->st));
     }

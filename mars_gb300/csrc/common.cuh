@@ -159,7 +159,7 @@ __device__ __forceinline__ void cp_async_wait()
 }
 
 // ---------------------------------------------------------------------------
-// Deterministic block reductions (fixed tree order for a fixed block size).
+// Deterministic warp reduction (fixed butterfly order).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v)
 {
@@ -168,26 +168,6 @@ __device__ __forceinline__ double warp_sum(double v)
         v += __shfl_xor_sync(0xffffffffu, v, o);
     }
     return v;
-}
-
-// Sum over the block; the result is valid in thread 0. `red` holds >= 32 doubles.
-template <int BLOCK>
-__device__ __forceinline__ double block_sum(double v, double *red)
-{
-    static_assert(BLOCK % 32 == 0 && BLOCK <= 1024, "block size");
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    v = warp_sum(v);
-    if (lane == 0) {
-        red[wid] = v;
-    }
-    __syncthreads();
-    double r = 0.0;
-    if (wid == 0) {
-        r = lane < BLOCK / 32 ? red[lane] : 0.0;
-        r = warp_sum(r);
-    }
-    __syncthreads();
-    return r;
 }
 
 }  // namespace mgpu
