@@ -10,8 +10,6 @@ squared norms and DGKS counts. Against the reference goldens (its x86 AVX
 build, whose hinge reductions run in another order) the term path is exact and
 r2 / r2_cv agree to 1e-6 (f4 fields).
 """
-import os
-
 import numpy as np
 import pytest
 
