@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Forward-pass benchmark on one GB300 (or N independent replicas).
 
-Default workload (the metric's own config): precision stress, X n=1,000,000 x
+Default workload: precision stress, X n=1,000,000 x
 p=100 float32 with AR(1) column correlation rho=0.9 and 5 near-duplicate
 columns, y = 2 x_a + 3 x_b + x_a x_b over 5 column pairs + N(0,1),
 max_terms=63, max_degree=3, tail_span=0.02 (the reference's default; synthetic,
@@ -14,8 +14,8 @@ K are timed, and the fit then runs to its end untimed (so the term path can
 be checked against the reference's); with W + K past the fit's epochs the
 timed region continues into a second fit. Inputs are far larger than the
 129 MB L2 (X 400 MB, the projected candidates ~24 GB per epoch), so L2 is not
-flushed between steps. --workload hinge_search (config 2) keeps one full fit
-per step.
+flushed between steps. --workload hinge_search (n=100,000 x p=20) keeps one
+full fit per step.
 
 value        knot-evals/s over the device span of the timed epochs (CUDA
              events on the library's stream; X, y resident in HBM), whole job
@@ -61,18 +61,20 @@ METRIC = "knot-evals/sec & fit time: mixed-prec batched vs FP64 GPU, same term p
 UNIT = "knot-evals/s"
 WORKLOADS = {
     "hinge_search": "hinge_search n=100000 p=20 iid N(0,1), 6 hinges + 3 hinge products, "
-                    "max_terms=31 max_degree=2 tail_span=0 (config 2)",
+                    "max_terms=31 max_degree=2 tail_span=0",
     "precision_stress": "precision_stress n=1000000 p=100 AR(1) rho=0.9 + 5 near-duplicates, "
-                        "max_terms=63 max_degree=3 tail_span=0.02 (config 3; the reference's "
-                        "default tail span)",
+                        "max_terms=63 max_degree=3 tail_span=0.02 (the reference's default "
+                        "tail span)",
     "precision_stress_small": "precision_stress n=30000 p=20 AR(1) rho=0.9 + 3 near-duplicates, "
-                              "max_terms=21 tail_span=0 (a small case of config 3's shape)",
-    "plain_fit": "plain_fit n=10000 p=2 linear_only max_terms=17 (config 1)",
+                              "max_terms=21 tail_span=0 (a small case of precision_stress's "
+                              "shape)",
+    "plain_fit": "plain_fit n=10000 p=2 linear_only max_terms=17",
     "batched": "256 independent fits, n log-uniform 1e3..2e5, p uniform 5..50, 4 random hinges "
-               "+ N(0,1) noise, max_terms=21, tail_span=0 (config 4)",
+               "+ N(0,1) noise, max_terms=21, tail_span=0",
     "expand": "differentiable prediction of a fitted hinge_search model (31 terms) on "
-              "1,000,000 rows: forward + backward (config 5)",
-    "projection": "the mixed fast pass's two-pass projection alone on a slice of config 3: "
+              "1,000,000 rows: forward + backward",
+    "projection": "the mixed fast pass's two-pass projection alone on a slice of "
+                  "precision_stress: "
                   "n=1,000,000 rows, m=32 basis columns, 640 candidates (20 inputs x 32 parents)",
 }
 
@@ -807,7 +809,7 @@ def run_reference_epochs(args):
 
 
 def run_epoch_steps(args):
-    """Default: the config-3 fit, one step per epoch (module docstring)."""
+    """Default: the precision-stress fit, one step per epoch (module docstring)."""
     tdist = dist()
     from mars_gb300 import marslib
 

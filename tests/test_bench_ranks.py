@@ -62,7 +62,7 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert len(lines) == 1  # rank 0 only
     line = lines[0]
     assert line["impl"] == "reference"
-    # config 1 is a linear-only fit: no knots are scored, the time is what is measured
+    # plain_fit is a linear-only fit: no knots are scored, the time is what is measured
     assert line["ms_per_step"] > 0 and line["e2e"]["value"] == line["value"]
     assert line["cpu_baseline"]["kind"] == "port"
     assert line["steps"] == 1 and line["warmup"] == 3

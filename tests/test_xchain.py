@@ -385,3 +385,47 @@ def test_zero_prefix_needs_no_rerun(xlib):
     want, got, redone = run(xlib, z, z, 512)
     assert same(want, got)
     assert redone <= 4, redone
+
+
+def test_kernel_levels_on_a_fits_appends(xlib):
+    """The Gram-Schmidt chains of the first appends of the hinge-search fit
+    (10^5 rows x 20 inputs; the reference's golden term path: hinge columns
+    that are zero on most rows, their products with parents, in the append
+    kernel's 49 blocks)
+    through the kernel's levels give the sequential chains bit for bit."""
+    import json
+
+    from mars_gb300 import workloads
+
+    X, _y, _kw = workloads.hinge_search()
+    with open(os.path.join(HERE, "golden", "hinge_search.json")) as f:
+        model = json.load(f)["model"]
+    n = X.shape[0]
+    K = min(256, -(-n // (256 * 8))) * 256
+    s = 1.0 / np.sqrt((X.astype(np.float64) ** 2).mean(0))
+    b0 = (np.ones(n) / np.sqrt(n)).astype(np.float32)
+    B, Q = [b0], [b0]
+    fp = ctypes.POINTER(ctypes.c_float)
+    dp = ctypes.POINTER(ctypes.c_double)
+    chains = 0
+    for t in model[1:9]:
+        xp, bp, sx = X[:, t["input"]], B[t["basis"]], np.float32(s[t["input"]])
+        h = np.float32(t["hinge"]) if t["hinge"] is not None else None
+        if t["type"] == "l":
+            val = (sx * bp) * xp
+        elif t["type"] == "+":
+            val = (sx * bp) * np.maximum(xp - h, np.float32(0))
+        else:
+            val = (sx * bp) * np.maximum(h - xp, np.float32(0))
+        v = val.astype(np.float64)
+        for q in [val] + Q:
+            want = xlib.xc_host_sequential_d(q.ctypes.data_as(fp), v.ctypes.data_as(dp), n)
+            got, _, _ = kernel_levels(xlib, q, v, K, 8)
+            assert same(want, got), (t, chains)
+            chains += 1
+            if q is not val:
+                v = v - float(q.astype(np.float64) @ v) * q.astype(np.float64)
+        B.append((val / np.float32(np.sqrt(np.sum(val.astype(np.float64) ** 2)))).astype(
+            np.float32))
+        Q.append((v / np.sqrt(v @ v)).astype(np.float32))
+    assert chains == sum(1 + k for k in range(1, 9))
