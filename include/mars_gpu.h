@@ -103,8 +103,7 @@ MARS_GPU_API int mars_gpu_device_count(void);
  *  Errors: "target Y is all zero or NANs", "not all columns in X are finite".
  *  X is copied to the device and also borrowed, like the reference's
  *  MarsAlgo borrows it: it must stay valid and unchanged until
- *  mars_gpu_destroy (the host keeps the reference-order FP64 state of the fit,
- *  the append and the exact re-scoring of near-tied candidates read it).
+ *  mars_gpu_destroy (mars_gpu_eval reads each knot, X[k, i], from it).
  */
 MARS_GPU_API int mars_gpu_create(const float *X, const float *y, const float *w, size_t n, size_t p,
                     size_t ldx, size_t max_terms, mars_gpu_algo **out);
