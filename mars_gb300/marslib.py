@@ -7,7 +7,8 @@ messages. Every call goes to ``lib/libmars_gpu.so``; there is no CPU path,
 so a missing library or GPU is an error, never a silent fallback.
 
 Extras over the reference: ``dsse()``, ``set_precision('fp64'|'mixed')``,
-``stats()`` and ``orth_error()`` (max |Q^T Q - I| and the FP64 RSS).
+``stats()``, ``orth_error()`` (max |Q^T Q - I| and the FP64 RSS) and
+``orth_error_by_terms()`` (the same for every leading basis).
 """
 import ctypes
 import os
