@@ -62,6 +62,18 @@ def test_large_golden_inputs_unchanged(name):
     assert len(g["model"]) >= 2
 
 
+def test_largest_batched_fits_term_paths(port_lib):
+    """The port gives the reference's term paths on the four largest of the
+    256 batched fits (n 1.6-1.8e5, p 40-47; ~10 s of CPU each)."""
+    names = [c for c in cases.LARGE_CASES if c.startswith("batched_top_")]
+    fits = workloads.batched_fits_top(k=len(names))
+    for name, (X, y, kw) in zip(names, fits):
+        g = load_fit(name)
+        assert workloads.digest(X, y) == g["digest"], name
+        model = forward_pass(port_lib, X, y, None, threads=-1, **kw)
+        assert_same_path(model, g)
+
+
 @pytest.mark.parametrize("name", cases.EVAL_CASES)
 def test_golden_eval_vectors(name, port):
     import oracle
