@@ -13,7 +13,8 @@
 //      each chunk's entry value; the chunk runs the chain speculatively from it
 //      (XcSpecR) and leaves a record;
 //   3. the records compose level by level (8 chunks, 4 sub-groups of a warp, 8
-//      warps of a block) into one record per block;
+//      warps of a block) into one record per block, which carries 8 residues
+//      where the lower levels carry 4;
 //   4. the last block to finish (a ticket, no waiting) composes the blocks in
 //      groups of 16, walks the groups from the true start 0 -- descending into
 //      the sub-records, down to re-running rows, wherever a record cannot vouch
